@@ -1,0 +1,162 @@
+/* lenia_gb300.h -- C ABI of the GB300 Lenia engine (sm_103a).
+ *
+ * Drop-in device engine for leniax's Lenia hot path:
+ *   leniax/core.py:13-49          core.update            -> lgx_update
+ *   leniax/runner.py:119-164      runner.run_scan        -> lgx_run (trajectories on)
+ *   leniax/runner.py:167-215      runner.run_scan_mem_optimized -> lgx_run
+ *   leniax/statistics.py:11-128   compute_stats          -> lgx_run (stats output)
+ *   leniax/statistics.py:134-205  check_heuristics / N   -> lgx_run (n_continue)
+ *   leniax/growth_functions.py:256-264 growth register   -> LGX_GF_* ids
+ *   leniax/core.py:322-326        get_state register     -> LGX_STATE_* ids
+ *
+ * Conventions
+ *  - Plain C: raw device pointers, element counts, a cudaStream_t passed as
+ *    void*.  No host synchronisation inside any call; all work is ordered on
+ *    the given stream.  Calls on the same plan from several host threads are
+ *    safe as long as each uses its own workspace.
+ *  - All tensors are caller owned and C-contiguous float32.  Spectra are
+ *    complex64 stored as interleaved (re, im) float pairs.
+ *  - The kernel spectrum is leniax's full complex spectrum
+ *    K[1, C, max_k, *world] (kernels.py:145-152) sliced to its Hermitian half
+ *    K[..., :W/2+1]: shape [C, max_k, *world[:-1], W/2+1].
+ *  - Return value 0 (LGX_OK) on success, otherwise an LGX_ERR_* code;
+ *    lgx_last_error() returns the message of the calling thread's last error.
+ *    The engine never falls back to a CPU path.
+ */
+#ifndef LENIA_GB300_H
+#define LENIA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LGX_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define LGX_API __attribute__((visibility("default")))
+#else
+#define LGX_API
+#endif
+
+/* status codes */
+#define LGX_OK 0
+#define LGX_ERR_INVALID 1     /* bad shape / argument / null pointer        */
+#define LGX_ERR_UNSUPPORTED 2 /* size, slug or combination not implemented   */
+#define LGX_ERR_CUDA 3        /* CUDA runtime error                          */
+#define LGX_ERR_WORKSPACE 4   /* workspace smaller than lgx_workspace_bytes  */
+#define LGX_ERR_TIMEOUT 5     /* a bounded device-side wait expired          */
+#define LGX_ERR_NONFINITE 6   /* reserved: non-finite input detected         */
+
+/* growth functions, leniax/growth_functions.py:256-264 */
+#define LGX_GF_POLY_QUAD4 0
+#define LGX_GF_GAUSSIAN 1
+#define LGX_GF_GAUSSIAN_TARGET 2
+#define LGX_GF_STEP 3
+#define LGX_GF_STAIRCASE 4
+#define LGX_GF_TRIANGLE 5
+#define LGX_GF_IDENTITY 6
+
+/* state updates, leniax/core.py:322-326 */
+#define LGX_STATE_V1 0     /* clip(s + dt*f, 0, 1)  */
+#define LGX_STATE_V2 1     /* s*(1-dt) + dt*f       */
+#define LGX_STATE_SIMPLE 2 /* s + dt*f              */
+
+/* engine selection for lgx_run */
+#define LGX_ENGINE_AUTO 0
+#define LGX_ENGINE_RESIDENT 1 /* one world per CTA slice, state in registers across steps */
+#define LGX_ENGINE_STREAMED 2 /* multi-pass, spectra through HBM/L2, any C/K             */
+#define LGX_ENGINE_PLAIN 3    /* one world per launch, one step per launch (reference)  */
+
+/* number of scalar statistics besides the C channel masses */
+#define LGX_NSTAT_SCALAR 11
+
+/* Static description of a Lenia model: what leniax's build_update_fn
+ * (helpers.py:401-427) and KernelMapping (kernels.py:10-63) close over. */
+typedef struct lgx_model_desc {
+  int nb_dims;          /* 2 or 3                                            */
+  int world[3];         /* world axis sizes, outermost first (nb_dims used)  */
+  int nb_channels;      /* C                                                 */
+  int nb_kernels;       /* K: true kernels, in leniax's channel-sorted order */
+  int max_k;            /* kernel slots per channel in the spectrum          */
+  const int* kernel_cin;  /* [K] channel read by kernel k                    */
+  const int* kernel_slot; /* [K] slot j of kernel k in spectrum[c_in, j]     */
+  const int* growth_fn;   /* [K] LGX_GF_* id of kernel k                     */
+  int state_fn;           /* LGX_STATE_*                                     */
+  int weighted_average;   /* 1: weighted_mean, 0: weighted_sum (core.py:202-242) */
+} lgx_model_desc;
+
+typedef struct lgx_plan lgx_plan;
+
+/* A batched rollout: leniax run_scan / run_scan_mem_optimized.
+ * Worlds are indexed (sol, init); a solution owns its spectrum, growth
+ * parameters, weights and T; inits of a solution share them. */
+typedef struct lgx_rollout {
+  int n_sols;            /* Ns (1 for run_scan)                                */
+  int n_init;            /* Ni worlds per solution                             */
+  int steps;             /* max_run_iter                                       */
+  const float* cells0;   /* [Ns, Ni, C, *world]                                */
+  const float* k_half;   /* [Ns, C, max_k, *world[:-1], W/2+1] complex64        */
+  const float* gf_params;/* [Ns, K, 2]   (m, s) per kernel                      */
+  const float* weights;  /* [Ns, C, K]   kernels_weight_per_channel             */
+  const float* T;        /* [Ns]         dt = 1/T                               */
+  float stats_R;         /* static R of compute_stats (statistics.py:22-24)     */
+  float stats_T;         /* static T of compute_stats                           */
+  float* final_cells;    /* [Ns, Ni, C, *world] or NULL                         */
+  float* stats;          /* [Ns, steps, Ni, C + LGX_NSTAT_SCALAR] or NULL:
+                            channel_mass[C], mass, mass_volume, mass_density,
+                            growth, growth_volume, growth_density, mass_speed,
+                            mass_angle_speed, mass_growth_dist, inertia,
+                            potential_volume (statistics.py:102-115)            */
+  float* n_continue;     /* [Ns, Ni] leniax N = sum_t check_heuristics, or NULL */
+  float* n_box;          /* [Ns, Ni] box stop set N (mass < 1e-3, mass > 0.9*area,
+                            live cell on the border), or NULL                   */
+  float* traj_cells;     /* [steps, Ns*Ni, C, *world] pre-update states, or NULL */
+  float* traj_field;     /* [steps, Ns*Ni, C, *world] or NULL                    */
+  float* traj_potential; /* [steps, Ns*Ni, K, *world] or NULL                    */
+  int engine;            /* LGX_ENGINE_*                                         */
+} lgx_rollout;
+
+/* ABI version (LGX_ABI_VERSION). */
+LGX_API int lgx_version(void);
+
+/* Message of the calling thread's last error ("" if none). */
+LGX_API const char* lgx_last_error(void);
+
+/* Validate a model and build a plan (host only, no device work).
+ * Replaces helpers.build_update_fn (helpers.py:401-427). */
+LGX_API int lgx_plan_create(const lgx_model_desc* desc, lgx_plan** out_plan);
+
+/* Release a plan. */
+LGX_API void lgx_plan_destroy(lgx_plan* plan);
+
+/* Engine lgx_run would pick for this plan and batch (LGX_ENGINE_*), or -1. */
+LGX_API int lgx_select_engine(const lgx_plan* plan, int n_sols, int n_init, int requested);
+
+/* Workspace bytes lgx_run needs for this batch and engine. */
+LGX_API size_t lgx_run_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init, int steps, int engine);
+
+/* Batched rollout, leniax runner.run_scan / run_scan_mem_optimized
+ * (runner.py:119-215) including compute_stats and check_heuristics. */
+LGX_API int lgx_run(const lgx_plan* plan, const lgx_rollout* job, void* workspace, size_t workspace_bytes,
+            void* stream);
+
+/* Workspace bytes lgx_update needs for n worlds. */
+LGX_API size_t lgx_update_workspace_bytes(const lgx_plan* plan, int n);
+
+/* One Euler step of n worlds sharing one spectrum: leniax core.update
+ * (core.py:13-49) with get_potential_fft / get_field / get_state.
+ *   state [n, C, *world]; dt: 1 value, or n values when dt_per_world != 0;
+ *   gf_params [K, 2]; weights [C, K]; outputs state_out [n, C, *world],
+ *   field_out [n, C, *world] and potential_out [n, K, *world] (the latter two
+ *   may be NULL). */
+LGX_API int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_half, const float* gf_params,
+               const float* weights, const float* dt, int dt_per_world, float* state_out, float* field_out,
+               float* potential_out, void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LENIA_GB300_H */

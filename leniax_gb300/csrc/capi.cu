@@ -1,0 +1,392 @@
+// C ABI of the GB300 Lenia engine: plan validation, workspace layout and
+// dispatch to the resident / streamed / plain engines.  See
+// include/lenia_gb300.h for the contract.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "common.cuh"
+#include "engine.h"
+
+using namespace lgx;
+
+struct lgx_plan {
+  Model m;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(LGX_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
+}
+
+inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Bump allocator over a caller-owned workspace.
+struct Carve {
+  char* base;
+  size_t off = 0, cap;
+  Carve(void* b, size_t c) : base(static_cast<char*>(b)), cap(c) {}
+  template <class T>
+  T* take(size_t count) {
+    T* p = reinterpret_cast<T*>(base + off);
+    off = al256(off + count * sizeof(T));
+    return p;
+  }
+};
+
+bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
+
+int select_engine(const Model& m, int requested) {
+  if (requested == LGX_ENGINE_RESIDENT) return resident_supported(m) ? LGX_ENGINE_RESIDENT : -1;
+  if (requested == LGX_ENGINE_STREAMED) return streamed_supported(m) ? LGX_ENGINE_STREAMED : -1;
+  if (requested == LGX_ENGINE_PLAIN) return streamed_supported(m) ? LGX_ENGINE_PLAIN : -1;
+  if (requested != LGX_ENGINE_AUTO) return -1;
+  if (resident_supported(m)) return LGX_ENGINE_RESIDENT;
+  if (streamed_supported(m)) return LGX_ENGINE_STREAMED;
+  return -1;
+}
+
+size_t resident_ws(const Model& m, int n_sols, int n_init, int steps) {
+  size_t b = 0;
+  b += al256((size_t)n_sols * m.H * resident_kpitch(m.H) * sizeof(float2));
+  b += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
+  return b;
+}
+
+size_t streamed_ws(const Model& m, int n_sols, int n_init, int steps, bool with_raw) {
+  const int nw = n_sols * n_init;
+  size_t b = streamed_workspace_bytes(m, nw, n_sols);
+  b += 2 * al256((size_t)nw * m.C * m.cells * sizeof(float));  // state ping-pong
+  if (with_raw) b += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
+  return b;
+}
+
+struct StreamedBufs {
+  float2 *spec, *prod, *kp;
+  float* partial;
+  int* shift;
+  float *sa, *sb, *raw;
+};
+
+StreamedBufs carve_streamed(const Model& m, int n_sols, int n_init, int steps, void* ws, size_t ws_bytes,
+                            bool with_raw) {
+  Carve cv(ws, ws_bytes);
+  const int nw = n_sols * n_init;
+  StreamedBufs b;
+  b.spec = cv.take<float2>((size_t)nw * m.C * m.cells / 2);
+  b.prod = cv.take<float2>((size_t)nw * m.K * m.cells / 2);
+  b.kp = cv.take<float2>((size_t)n_sols * m.C * m.max_k * m.H * (m.W / 2 + 2));
+  b.partial = cv.take<float>((size_t)nw * streamed_blocks_per_world(m) * raw_stride(m.C));
+  b.shift = cv.take<int>((size_t)nw * 3);
+  b.sa = cv.take<float>((size_t)nw * m.C * m.cells);
+  b.sb = cv.take<float>((size_t)nw * m.C * m.cells);
+  b.raw = with_raw ? cv.take<float>((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C)) : nullptr;
+  return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lgx_version(void) { return LGX_ABI_VERSION; }
+
+const char* lgx_last_error(void) { return g_err.c_str(); }
+
+int lgx_plan_create(const lgx_model_desc* d, lgx_plan** out) {
+  if (!d || !out) return fail(LGX_ERR_INVALID, "lgx_plan_create: null argument");
+  *out = nullptr;
+  if (d->nb_dims != 2 && d->nb_dims != 3) return fail(LGX_ERR_INVALID, "nb_dims must be 2 or 3 (got %d)", d->nb_dims);
+  if (d->nb_channels < 1 || d->nb_channels > kMaxChannels)
+    return fail(LGX_ERR_INVALID, "nb_channels must be in [1, %d] (got %d)", kMaxChannels, d->nb_channels);
+  if (d->nb_kernels < 1 || d->nb_kernels > kMaxKernels)
+    return fail(LGX_ERR_INVALID, "nb_kernels must be in [1, %d] (got %d)", kMaxKernels, d->nb_kernels);
+  if (d->max_k < 1) return fail(LGX_ERR_INVALID, "max_k must be >= 1");
+  if (!d->kernel_cin || !d->kernel_slot || !d->growth_fn) return fail(LGX_ERR_INVALID, "null kernel table");
+  if (d->state_fn < LGX_STATE_V1 || d->state_fn > LGX_STATE_SIMPLE)
+    return fail(LGX_ERR_INVALID, "unknown state function id %d", d->state_fn);
+  Model m;
+  std::memset(&m, 0, sizeof(m));
+  m.nb_dims = d->nb_dims;
+  for (int i = 0; i < d->nb_dims; ++i) {
+    if (!is_pow2(d->world[i]) || d->world[i] < 8)
+      return fail(LGX_ERR_UNSUPPORTED, "world axis %d has size %d: power-of-two sizes >= 8 only", i, d->world[i]);
+    m.world[i] = d->world[i];
+  }
+  m.C = d->nb_channels;
+  m.K = d->nb_kernels;
+  m.max_k = d->max_k;
+  int per_ch[kMaxChannels] = {0};
+  for (int k = 0; k < m.K; ++k) {
+    const int c = d->kernel_cin[k], s = d->kernel_slot[k], g = d->growth_fn[k];
+    if (c < 0 || c >= m.C) return fail(LGX_ERR_INVALID, "kernel %d reads channel %d of %d", k, c, m.C);
+    if (s < 0 || s >= m.max_k) return fail(LGX_ERR_INVALID, "kernel %d slot %d >= max_k %d", k, s, m.max_k);
+    if (g < LGX_GF_POLY_QUAD4 || g > LGX_GF_IDENTITY)
+      return fail(LGX_ERR_UNSUPPORTED, "kernel %d: unknown growth function id %d", k, g);
+    m.cin[k] = c;
+    m.slot[k] = s;
+    m.gf[k] = g;
+    per_ch[c]++;
+  }
+  for (int c = 0; c < m.C; ++c)
+    if (per_ch[c] > m.max_k) return fail(LGX_ERR_INVALID, "channel %d has more kernels than max_k", c);
+  m.state_fn = d->state_fn;
+  m.mean = d->weighted_average ? 1 : 0;
+  if (m.nb_dims == 2) {
+    m.D = 1;
+    m.H = m.world[0];
+    m.W = m.world[1];
+  } else {
+    m.D = m.world[0];
+    m.H = m.world[1];
+    m.W = m.world[2];
+  }
+  m.cells = (long)m.D * m.H * m.W;
+  lgx_plan* p = new (std::nothrow) lgx_plan;
+  if (!p) return fail(LGX_ERR_INVALID, "out of host memory");
+  p->m = m;
+  *out = p;
+  g_err.clear();
+  return LGX_OK;
+}
+
+void lgx_plan_destroy(lgx_plan* plan) { delete plan; }
+
+int lgx_select_engine(const lgx_plan* plan, int n_sols, int n_init, int requested) {
+  if (!plan || n_sols < 1 || n_init < 1) return -1;
+  return select_engine(plan->m, requested);
+}
+
+size_t lgx_run_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init, int steps, int engine) {
+  if (!plan || n_sols < 1 || n_init < 1 || steps < 0) return 0;
+  const int e = select_engine(plan->m, engine);
+  if (e == LGX_ENGINE_RESIDENT) return resident_ws(plan->m, n_sols, n_init, steps);
+  if (e == LGX_ENGINE_STREAMED || e == LGX_ENGINE_PLAIN) return streamed_ws(plan->m, n_sols, n_init, steps, true);
+  return 0;
+}
+
+int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_bytes, void* stream) {
+  if (!plan || !j) return fail(LGX_ERR_INVALID, "lgx_run: null plan or job");
+  const Model& m = plan->m;
+  if (j->n_sols < 1 || j->n_init < 1 || j->steps < 0)
+    return fail(LGX_ERR_INVALID, "lgx_run: bad batch (n_sols=%d n_init=%d steps=%d)", j->n_sols, j->n_init, j->steps);
+  if (!j->cells0 || !j->k_half || !j->gf_params || !j->weights || !j->T)
+    return fail(LGX_ERR_INVALID, "lgx_run: null input tensor");
+  if (!(j->stats_R > 0.f) || !(j->stats_T > 0.f)) return fail(LGX_ERR_INVALID, "lgx_run: stats_R and stats_T must be > 0");
+  const int e = select_engine(m, j->engine);
+  if (e < 0) return fail(LGX_ERR_UNSUPPORTED, "lgx_run: no engine for this model (engine=%d, C=%d, K=%d, size=%d)",
+                         j->engine, m.C, m.K, m.H);
+  const size_t need = lgx_run_workspace_bytes(plan, j->n_sols, j->n_init, j->steps, e);
+  if (!ws || ws_bytes < need) return fail(LGX_ERR_WORKSPACE, "lgx_run: workspace %zu < %zu bytes", ws_bytes, need);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int nw = j->n_sols * j->n_init;
+  const size_t plane = (size_t)m.C * m.cells;
+  cudaError_t ce;
+  if (j->steps == 0) {
+    if (j->final_cells) {
+      ce = cudaMemcpyAsync(j->final_cells, j->cells0, (size_t)nw * plane * sizeof(float), cudaMemcpyDeviceToDevice, st);
+      if (ce != cudaSuccess) return cuda_fail(ce, "lgx_run copy");
+    }
+    if (j->n_continue) cudaMemsetAsync(j->n_continue, 0, (size_t)nw * sizeof(float), st);
+    if (j->n_box) cudaMemsetAsync(j->n_box, 0, (size_t)nw * sizeof(float), st);
+    return LGX_OK;
+  }
+  float* raw = nullptr;
+  if (e == LGX_ENGINE_RESIDENT) {
+    Carve cv(ws, ws_bytes);
+    float2* kp = cv.take<float2>((size_t)j->n_sols * m.H * resident_kpitch(m.H));
+    raw = cv.take<float>((size_t)j->n_sols * j->steps * j->n_init * raw_stride(m.C));
+    ce = launch_prepare_resident_spectrum(m.H, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    ResidentArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.n_worlds = nw;
+    a.n_init = j->n_init;
+    a.steps = j->steps;
+    a.gf_id = m.gf[0];
+    a.state_fn = m.state_fn;
+    a.mean = m.mean;
+    a.cells0 = j->cells0;
+    a.kp = kp;
+    a.gf = j->gf_params;
+    a.w = j->weights;
+    a.T = j->T;
+    a.final_cells = j->final_cells;
+    a.raw = raw;
+    a.traj_cells = j->traj_cells;
+    a.traj_field = j->traj_field;
+    a.traj_pot = j->traj_potential;
+    const int wpc = 512 / ((m.H / 2) * (m.H == 128 ? 8 : 4));
+    const int items = (nw + wpc - 1) / wpc;
+    const int grid = std::max(1, std::min(items, resident_max_grid(m.H)));
+    ce = launch_resident(m.H, a, grid, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "resident kernel");
+  } else {
+    StreamedBufs b = carve_streamed(m, j->n_sols, j->n_init, j->steps, ws, ws_bytes, true);
+    raw = b.raw;
+    ce = launch_prepare_streamed_spectrum(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), b.kp, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    ce = cudaMemsetAsync(b.shift, 0, (size_t)nw * 3 * sizeof(int), st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "memset");
+    const long kp_sol = (long)m.C * m.max_k * m.H * (m.W / 2 + 2);
+    const long raws = raw_stride(m.C);
+    const bool plain = (e == LGX_ENGINE_PLAIN);
+    const float* cur = j->cells0;
+    for (int s = 0; s < j->steps; ++s) {
+      float* out = (s == j->steps - 1 && j->final_cells) ? j->final_cells : ((s & 1) ? b.sb : b.sa);
+      if (j->traj_cells) {
+        ce = cudaMemcpyAsync(j->traj_cells + (size_t)s * nw * plane, cur, (size_t)nw * plane * sizeof(float),
+                             cudaMemcpyDeviceToDevice, st);
+        if (ce != cudaSuccess) return cuda_fail(ce, "trajectory copy");
+      }
+      StreamedStep ss;
+      ss.m = &m;
+      ss.kp_sol_stride = kp_sol;
+      ss.gf_sol_stride = 2L * m.K;
+      ss.w_sol_stride = (long)m.C * m.K;
+      ss.dt_mode = 2;
+      ss.raw_sol_stride = (long)j->steps * j->n_init * raws;
+      ss.raw_world_stride = raws;
+      if (!plain) {
+        ss.n_worlds = nw;
+        ss.n_init = j->n_init;
+        ss.state = cur;
+        ss.state_out = out;
+        ss.kp = b.kp;
+        ss.gf = j->gf_params;
+        ss.w = j->weights;
+        ss.dt = j->T;
+        ss.field_out = j->traj_field ? j->traj_field + (size_t)s * nw * plane : nullptr;
+        ss.pot_out = j->traj_potential ? j->traj_potential + (size_t)s * nw * m.K * m.cells : nullptr;
+        ss.raw = raw + (size_t)s * j->n_init * raws;
+        ss.shift = b.shift;
+        ss.spec = b.spec;
+        ss.prod = b.prod;
+        ss.partial = b.partial;
+        ce = launch_streamed_step(ss, st);
+        if (ce != cudaSuccess) return cuda_fail(ce, "streamed step");
+      } else {
+        // one world per launch: the reference one-world-per-launch kernel sequence
+        for (int wdx = 0; wdx < nw; ++wdx) {
+          const int sol = wdx / j->n_init, init = wdx % j->n_init;
+          ss.n_worlds = 1;
+          ss.n_init = 1;
+          ss.state = cur + (size_t)wdx * plane;
+          ss.state_out = out + (size_t)wdx * plane;
+          ss.kp = b.kp + sol * kp_sol;
+          ss.gf = j->gf_params + (size_t)sol * 2 * m.K;
+          ss.w = j->weights + (size_t)sol * m.C * m.K;
+          ss.dt = j->T + sol;
+          ss.field_out = j->traj_field ? j->traj_field + ((size_t)s * nw + wdx) * plane : nullptr;
+          ss.pot_out = j->traj_potential ? j->traj_potential + ((size_t)s * nw + wdx) * m.K * m.cells : nullptr;
+          ss.raw = raw + (((size_t)sol * j->steps + s) * j->n_init + init) * raws;
+          ss.shift = b.shift + 3 * wdx;
+          ss.spec = b.spec;
+          ss.prod = b.prod;
+          ss.partial = b.partial;
+          ce = launch_streamed_step(ss, st);
+          if (ce != cudaSuccess) return cuda_fail(ce, "plain step");
+        }
+      }
+      cur = out;
+    }
+    if (j->final_cells && cur != j->final_cells) {
+      ce = cudaMemcpyAsync(j->final_cells, cur, (size_t)nw * plane * sizeof(float), cudaMemcpyDeviceToDevice, st);
+      if (ce != cudaSuccess) return cuda_fail(ce, "final copy");
+    }
+  }
+  StatsArgs sa;
+  std::memset(&sa, 0, sizeof(sa));
+  sa.n_sols = j->n_sols;
+  sa.n_init = j->n_init;
+  sa.steps = j->steps;
+  sa.C = m.C;
+  sa.nb_dims = m.nb_dims;
+  for (int i = 0; i < 3; ++i) sa.world[i] = m.world[i];
+  sa.R = j->stats_R;
+  sa.T = j->stats_T;
+  sa.raw = raw;
+  sa.stats = j->stats;
+  sa.n_continue = j->n_continue;
+  sa.n_box = j->n_box;
+  ce = launch_stats(sa, st);
+  if (ce != cudaSuccess) return cuda_fail(ce, "stats kernels");
+  g_err.clear();
+  return LGX_OK;
+}
+
+size_t lgx_update_workspace_bytes(const lgx_plan* plan, int n) {
+  if (!plan || n < 1) return 0;
+  const Model& m = plan->m;
+  if (resident_supported(m)) return resident_ws(m, 1, n, 1) + al256(sizeof(float));
+  if (streamed_supported(m)) return streamed_ws(m, 1, n, 1, false) + al256((size_t)n * sizeof(float));
+  return 0;
+}
+
+int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_half, const float* gf_params,
+               const float* weights, const float* dt, int dt_per_world, float* state_out, float* field_out,
+               float* potential_out, void* ws, size_t ws_bytes, void* stream) {
+  if (!plan) return fail(LGX_ERR_INVALID, "lgx_update: null plan");
+  const Model& m = plan->m;
+  if (n < 1) return fail(LGX_ERR_INVALID, "lgx_update: n must be >= 1");
+  if (!state || !k_half || !gf_params || !weights || !dt || !state_out)
+    return fail(LGX_ERR_INVALID, "lgx_update: null tensor");
+  const size_t need = lgx_update_workspace_bytes(plan, n);
+  if (need == 0) return fail(LGX_ERR_UNSUPPORTED, "lgx_update: no engine for this model");
+  if (!ws || ws_bytes < need) return fail(LGX_ERR_WORKSPACE, "lgx_update: workspace %zu < %zu bytes", ws_bytes, need);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t ce;
+  if (!streamed_supported(m) && !resident_supported(m)) return fail(LGX_ERR_UNSUPPORTED, "lgx_update: unsupported");
+  if (streamed_supported(m)) {
+    StreamedBufs b = carve_streamed(m, 1, n, 1, ws, ws_bytes, false);
+    ce = launch_prepare_streamed_spectrum(m, 1, reinterpret_cast<const float2*>(k_half), b.kp, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    ce = cudaMemsetAsync(b.shift, 0, (size_t)n * 3 * sizeof(int), st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "memset");
+    StreamedStep ss;
+    ss.m = &m;
+    ss.n_worlds = n;
+    ss.n_init = n;
+    ss.state = state;
+    ss.state_out = state_out;
+    ss.kp = b.kp;
+    ss.kp_sol_stride = 0;
+    ss.gf = gf_params;
+    ss.gf_sol_stride = 0;
+    ss.w = weights;
+    ss.w_sol_stride = 0;
+    ss.dt = dt;
+    ss.dt_mode = dt_per_world ? 1 : 0;
+    ss.field_out = field_out;
+    ss.pot_out = potential_out;
+    ss.raw = nullptr;
+    ss.raw_world_stride = 0;
+    ss.raw_sol_stride = 0;
+    ss.shift = b.shift;
+    ss.spec = b.spec;
+    ss.prod = b.prod;
+    ss.partial = b.partial;
+    ce = launch_streamed_step(ss, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "update step");
+    g_err.clear();
+    return LGX_OK;
+  }
+  return fail(LGX_ERR_UNSUPPORTED, "lgx_update: unsupported world size");
+}
+
+}  // extern "C"

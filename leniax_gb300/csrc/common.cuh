@@ -1,0 +1,101 @@
+// Shared device helpers of the Lenia engine: growth functions, state updates,
+// raw-moment layout and small reductions.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lenia_gb300.h"
+
+namespace lgx {
+
+constexpr float kEps = 1e-7f;  // leniax/constant.py:7
+
+// Raw per-(world, step) moments written by the step kernels and turned into
+// leniax's statistics by the stats kernel.  Coordinates are the centred ones
+// of statistics.py:28-33 on the world rolled by the carried shift
+// (utils.py:269-293); axis a is world axis a (outermost first).
+enum RawSlot : int {
+  RAW_M00 = 0,      // sum of cells
+  RAW_G00 = 1,      // sum of max(field, 0)
+  RAW_CNT_POT = 2,  // #(potential > eps) over all kernels
+  RAW_CNT_MASS = 3, // #(cells > eps)
+  RAW_CNT_GROW = 4, // #(max(field,0) > eps)
+  RAW_MX = 5,       // 3 slots: sum cells * c_a
+  RAW_GX = 8,       // 3 slots: sum max(field,0) * c_a
+  RAW_MX2 = 11,     // 3 slots: sum cells * c_a^2
+  RAW_BORDER = 14,  // 1 if a live cell (> eps) lies on the outer layer of the un-centred world
+  RAW_RESERVED = 15,
+  RAW_CM = 16,      // C slots: per-channel sum of cells
+};
+__host__ __device__ constexpr int raw_stride(int C) { return RAW_CM + C; }
+
+// Growth functions, leniax/growth_functions.py (same operation order).
+__device__ __forceinline__ float growth_fn(int id, float x, float m, float s) {
+  switch (id) {
+    case LGX_GF_POLY_QUAD4: {  // growth_functions.py:38-45
+      float d = x - m;
+      float o = 1.f - (d * d) / (9.f * (s * s));
+      o = fmaxf(0.f, o);
+      o = o * o;
+      o = o * o;
+      return 2.f * o - 1.f;
+    }
+    case LGX_GF_GAUSSIAN: {  // growth_functions.py:76-82
+      float d = (x - m) / s;
+      float o = expf(-(d * d) / 2.f);
+      return 2.f * o - 1.f;
+    }
+    case LGX_GF_GAUSSIAN_TARGET: {  // growth_functions.py:113-119
+      float d = (x - m) / s;
+      return expf(-(d * d) / 2.f);
+    }
+    case LGX_GF_STEP: {  // growth_functions.py:154-160
+      return fabsf(x - m) <= s ? 1.f : -1.f;
+    }
+    case LGX_GF_STAIRCASE: {  // growth_functions.py:194-201
+      float o = 0.f;
+      if (x >= m - s && x < m - s / 2.f) o += 0.5f;
+      if (x >= m - s / 2.f && x <= m + s / 2.f) o += 1.f;
+      if (x > m + s / 2.f && x <= m + s) o += 0.5f;
+      return 2.f * o - 1.f;
+    }
+    case LGX_GF_TRIANGLE: {  // growth_functions.py:234-243
+      float left = m - s, right = m + s, o = 0.f;
+      if (x >= left && x < m) o += (x - left) / (m - left);
+      if (x >= m && x <= right) o += (x - right) / (m - right);
+      return 2.f * o - 1.f;
+    }
+    default:  // LGX_GF_IDENTITY, growth_functions.py:246-253
+      return x;
+  }
+}
+
+// State updates, leniax/core.py:245-319.
+__device__ __forceinline__ float state_fn(int id, float s, float f, float dt) {
+  if (id == LGX_STATE_V1) {
+    float n = s + dt * f;
+    return fminf(fmaxf(n, 0.f), 1.f);
+  } else if (id == LGX_STATE_V2) {
+    return s * (1.f - dt) + dt * f;
+  }
+  return s + dt * f;
+}
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Named barrier over `count` threads (count a multiple of 32).
+__device__ __forceinline__ void named_bar(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+// Non-negative modulo for the carried torus shift (jnp `%`, statistics.py:119).
+__device__ __forceinline__ int pmod(int a, int n) {
+  int r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+}  // namespace lgx

@@ -1,0 +1,102 @@
+// Internal interfaces between the C ABI layer and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/lenia_gb300.h"
+
+namespace lgx {
+
+constexpr int kMaxKernels = 64;
+constexpr int kMaxChannels = 16;
+
+struct Model {
+  int nb_dims;
+  int world[3];
+  int C, K, max_k;
+  int cin[kMaxKernels];
+  int slot[kMaxKernels];
+  int gf[kMaxKernels];
+  int state_fn;
+  int mean;
+  // derived
+  int H, W, D;  // D = 1 for 2D
+  long cells;   // D*H*W
+};
+
+// ---------------------------------------------------------------- resident
+// Prepared spectrum pitch (float2) of the resident engine for an N x N world.
+inline int resident_kpitch(int N) { return N / 2 + 2; }
+bool resident_supported(const Model& m);
+size_t resident_smem_bytes(int N);
+
+struct ResidentArgs {
+  int n_worlds, n_init, steps;
+  int gf_id, state_fn, mean;
+  const float* cells0;  // [n_worlds, N, N]
+  const float2* kp;     // [Ns, N, kpitch]
+  const float* gf;      // [Ns, K=1, 2]
+  const float* w;       // [Ns, C=1, K=1]
+  const float* T;       // [Ns]
+  float* final_cells;   // [n_worlds, N, N] or null
+  float* raw;           // [Ns, steps, Ni, raw_stride(1)]
+  float* traj_cells;    // [steps, n_worlds, N, N] or null
+  float* traj_field;
+  float* traj_pot;
+  int* status;          // device error word (0 = ok)
+};
+cudaError_t launch_resident(int N, const ResidentArgs& a, int grid, cudaStream_t st);
+int resident_max_grid(int N);
+
+// Prepare the resident spectra: kp[s][ky][c] from the half spectrum.
+cudaError_t launch_prepare_resident_spectrum(int N, int n_sols, const float2* k_half, float2* kp,
+                                             cudaStream_t st);
+
+// ---------------------------------------------------------------- streamed
+struct StreamedArgs;  // defined in streamed.cu
+bool streamed_supported(const Model& m);
+size_t streamed_workspace_bytes(const Model& m, int n_worlds, int n_sols);
+int streamed_blocks_per_world(const Model& m);
+// One step of n_worlds worlds (all solutions): see streamed.cu.
+struct StreamedStep {
+  const Model* m;
+  int n_worlds, n_init;
+  const float* state;      // [n_worlds, C, *world]
+  float* state_out;        // [n_worlds, C, *world]
+  const float2* kp;        // [Ns, C, max_k, H, W/2+2] prepared (scaled) spectra, per solution
+  long kp_sol_stride;      // float2 elements between solutions (0: shared)
+  const float* gf;         // [Ns, K, 2]
+  long gf_sol_stride;
+  const float* w;          // [Ns, C, K]
+  long w_sol_stride;
+  const float* dt;         // per world (dt_world=1) or per solution
+  int dt_mode;             // 0: scalar dt[0]; 1: dt[world]; 2: 1/T[sol]
+  float* field_out;        // [n_worlds, C, *world] or null
+  float* pot_out;          // [n_worlds, K, *world] or null
+  float* raw;              // raw moments [.., RAWS] for this step (indexed by world), or null
+  long raw_world_stride;   // stride between worlds in floats (sol/init mapping below)
+  long raw_sol_stride;
+  int* shift;              // [n_worlds, 3] carried torus shift (read; updated by the stats reducer)
+  float2* spec;            // workspace [n_worlds, C, H/2, W] packed row spectra
+  float2* prod;            // workspace [n_worlds, K, H/2, W] packed product spectra
+  float* partial;          // workspace per-block raw partials
+};
+cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st);
+cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,
+                                             cudaStream_t st);
+
+// ---------------------------------------------------------------- stats
+// Turn raw moments [Ns, steps, Ni, RAWS] into leniax stats / N / N_box.
+struct StatsArgs {
+  int n_sols, n_init, steps, C, nb_dims;
+  int world[3];
+  float R, T;
+  const float* raw;
+  float* stats;       // [Ns, steps, Ni, C + 11] or null
+  float* n_continue;  // [Ns, Ni] or null
+  float* n_box;       // [Ns, Ni] or null
+};
+cudaError_t launch_stats(const StatsArgs& a, cudaStream_t st);
+
+}  // namespace lgx

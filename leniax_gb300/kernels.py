@@ -1,0 +1,196 @@
+"""Kernel construction and mapping: the inputs of the Lenia hot path.
+
+Mirror of leniax ``kernels.py`` (``KernelMapping`` 10-63,
+``get_kernels_and_mapping`` 66-158, ``circle_2d`` 176-212) and
+``kernel_functions.py`` (7-261).  This is the once-per-configuration boundary
+preparation (host side, like the reference); the per-step hot path runs in the
+CUDA engine.  The spectrum is returned as a CUDA complex64 tensor
+``[1, C, max_k, *world]`` exactly as leniax returns it (fftshift then fftn of
+the world-centred kernels, kernels.py:145-152).
+"""
+import math
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from .constant import EPSILON
+
+
+# ---------------------------------------------------------------- kernel functions
+def poly_quad(params, X):
+    """kernel_functions.py:7-37"""
+    return (4 * X * (1 - X))**params[0]
+
+
+def gauss_bump(params, X):
+    """kernel_functions.py:40-69"""
+    q = params[0]
+    with np.errstate(over='ignore', under='ignore'):
+        return np.exp(q * (q - 1 / (X * (1 - X) + X.dtype.type(EPSILON))))
+
+
+def step(params, X):
+    """kernel_functions.py:72-102"""
+    q = params[0]
+    return ((X >= q) * (X <= 1 - q)).astype(X.dtype)
+
+
+def gauss(params, X):
+    """kernel_functions.py:105-134"""
+    q = params[0]
+    out = ((X - q) / (X.dtype.type(0.3) * q))**2
+    return np.exp(-out / 2)
+
+
+def threshold(params, X):
+    """kernel_functions.py:137-167"""
+    return (X >= params[0]).astype(X.dtype)
+
+
+def staircase(params, X):
+    """kernel_functions.py:170-208"""
+    m, s = params[0], params[1]
+    out = 0.5 * (X >= m - s) * (X < m - s / 2)
+    out = out + 1 * (X >= m - s / 2) * (X <= m + s / 2)
+    out = out + 0.5 * (X > m + s / 2) * (X <= m + s)
+    return out.astype(X.dtype)
+
+
+def triangle(params, X):
+    """kernel_functions.py:211-250"""
+    m, s = params[0], params[1]
+    left, right = m - s, m + s
+    out = (X >= left) * (X < m) * (X - left) / (m - left)
+    out = out + (X >= m) * (X <= right) * (X - right) / (m - right)
+    return out.astype(X.dtype)
+
+
+kf_register = {
+    'poly_quad': poly_quad,
+    'gauss_bump': gauss_bump,
+    'gauss': gauss,
+    'step': step,
+    'threshold': threshold,
+    'staircase': staircase,
+    'triangle': triangle,
+}
+
+
+# ---------------------------------------------------------------- kernels
+def circle_nd(R, k_params, kf_slug, kf_params, nb_dims=2) -> np.ndarray:
+    """Ring kernel of leniax ``circle_2d`` (kernels.py:176-212), float32; for
+    ``nb_dims == 3`` the distance runs over the three axes (this engine's
+    extension: leniax builds 2D kernels only)."""
+    f32 = np.float32
+    r = k_params[0]
+    bs = np.asarray(k_params[1], dtype=f32)
+    k_radius_px = math.ceil(r * R)
+    coords = np.indices([k_radius_px * 2] * nb_dims).astype(f32)
+    centered = (coords - f32(k_radius_px)) / f32(r * R)
+    distances = np.sqrt(np.sum(centered**2, axis=0))
+    nb_b = bs.shape[0]
+    B_dist = f32(nb_b) * distances
+    bs_mat = bs[np.minimum(np.floor(B_dist).astype(np.int64), nb_b - 1)]
+    raw_kernel = kf_register[kf_slug](np.asarray(kf_params, dtype=f32), np.mod(B_dist, f32(1)))
+    kernel = (distances < 1) * raw_kernel * bs_mat
+    kernel = (kernel / kernel.sum()).astype(f32)
+    return kernel[np.newaxis]
+
+
+def circle_2d(R, k_params, kf_slug, kf_params):
+    """kernels.py:176-212"""
+    return circle_nd(R, k_params, kf_slug, kf_params, 2)
+
+
+def raw(R, k_params, kf_slug, kf_params):
+    """kernels.py:161-173"""
+    return np.asarray(k_params, dtype=np.float32)
+
+
+register = {'raw': raw, 'circle_2d': circle_2d}
+
+
+class KernelMapping:
+    """kernels.py:10-63: explicit description of the kernel graph."""
+
+    def __init__(self, nb_channels: int, nb_kernels: int):
+        self.cin_kernels: List[List[int]] = [[] for _ in range(nb_channels)]
+        self.cin_k_params: List[List] = [[] for _ in range(nb_channels)]
+        self.cin_kfs: List[List[str]] = [[] for _ in range(nb_channels)]
+        self.cin_gfs: List[List[str]] = [[] for _ in range(nb_channels)]
+        self.cin_gf_params: List[List] = [[] for _ in range(nb_channels)]
+        self.kernels_weight_per_channel = [[0.] * nb_kernels for _ in range(nb_channels)]
+        self.true_channels: Optional[List[bool]] = None
+
+    def get_k_params(self):
+        return [item for sub in self.cin_k_params for item in sub]
+
+    def get_gf_params(self, device=None) -> torch.Tensor:
+        flat = [item for sub in self.cin_gf_params for item in sub]
+        return torch.tensor(flat, dtype=torch.float32, device=device)
+
+    def get_kernels_weight_per_channel(self, device=None) -> torch.Tensor:
+        return torch.tensor(self.kernels_weight_per_channel, dtype=torch.float32, device=device)
+
+    # engine view -------------------------------------------------------------
+    def kernel_table(self) -> Tuple[List[int], List[int], List[str], int]:
+        """(c_in, slot, growth slug) of every true kernel in leniax's flattened
+        order, and max_k (kernels.py:122-143; helpers.py:452-458)."""
+        max_k = max(map(len, self.cin_kernels))
+        cin, slot, gfs = [], [], []
+        for c, (lst, gl) in enumerate(zip(self.cin_kernels, self.cin_gfs)):
+            for j, _ in enumerate(lst):
+                cin.append(c)
+                slot.append(j)
+                gfs.append(gl[j])
+        return cin, slot, gfs, max_k
+
+
+def get_kernels_and_mapping(kernels_params: List[Dict], world_size: Sequence[int], nb_channels: int, R: float,
+                            fft: bool = True, device=None) -> Tuple[torch.Tensor, KernelMapping]:
+    """kernels.py:66-158.  Returns the spectrum ``[1, C, max_k, *world]``
+    complex64 (``fft=True``) on ``device`` (default: current CUDA device)."""
+    if device is None:
+        device = torch.device('cuda', torch.cuda.current_device()) if torch.cuda.is_available() else 'cpu'
+    nb_dims = len(world_size)
+    kernels_params.sort(key=lambda d: d['c_in'])  # kernels.py:90 (stable, in place as in leniax)
+    mapping = KernelMapping(nb_channels, len(kernels_params))
+    padded = []
+    for kernel_idx, p in enumerate(kernels_params):
+        slug = p.get('k_slug', 'circle_2d')
+        if slug == 'circle_2d':
+            k = circle_nd(R, p['k_params'], p['kf_slug'], p['kf_params'], nb_dims)
+        else:
+            k = register[slug](R, p['k_params'], p['kf_slug'], p['kf_params'])
+        pads = [(0, 0)]
+        for ws, ks in zip(world_size, k.shape[1:]):
+            need = ws - ks
+            pads.append(((need // 2), need // 2 + (need % 2)))
+        padded.append(np.pad(k, pads))
+        c_in = p['c_in']
+        mapping.cin_kernels[c_in].append(kernel_idx)
+        mapping.cin_gfs[c_in].append(p['gf_slug'])
+        mapping.cin_gf_params[c_in].append(p['gf_params'])
+        mapping.cin_kfs[c_in].append(p['kf_slug'])
+        mapping.cin_k_params[c_in].append(p['k_params'])
+        mapping.kernels_weight_per_channel[p['c_out']][kernel_idx] = p['h']
+    kernels = np.concatenate(padded, axis=0).astype(np.float32)
+    kshape = kernels.shape[1:]
+    max_k = max(map(len, mapping.cin_kernels))
+    per_channel, true_channels = [], []
+    for lst in mapping.cin_kernels:
+        K_tmp = kernels[np.array(lst, dtype=np.int64)] if lst else np.zeros((0, ) + kshape, np.float32)
+        missing = max_k - K_tmp.shape[0]
+        true_channels += [True] * K_tmp.shape[0] + [False] * missing
+        if missing:
+            K_tmp = np.concatenate([K_tmp, np.zeros((missing, ) + kshape, np.float32)])
+        per_channel.append(K_tmp)
+    mapping.true_channels = None if all(true_channels) else true_channels
+    if not fft:
+        return torch.from_numpy(np.concatenate(per_channel)[:, np.newaxis]).to(device), mapping
+    axes = tuple(range(-1, -nb_dims - 1, -1))
+    K = np.stack(per_channel)[np.newaxis]  # [1, C, max_k, *ws]
+    K = np.fft.fftshift(K, axes=axes)
+    K = np.fft.fftn(K.astype(np.complex64), axes=axes).astype(np.complex64)
+    return torch.from_numpy(np.ascontiguousarray(K)).to(device), mapping

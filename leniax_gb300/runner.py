@@ -1,0 +1,158 @@
+"""Scan drivers on the GB300 engine: drop-in for leniax ``runner.py``.
+
+``run_scan`` (runner.py:119-164) and ``run_scan_mem_optimized``
+(runner.py:167-215) keep leniax's positional arguments and output layouts and
+run the whole rollout -- Euler steps, per-step statistics, the stop
+heuristics -- on the device in one engine call (``lgx_run``).  ``run``
+(runner.py:16-116) is the eager driver with leniax's total-mass heuristics.
+"""
+from typing import Dict, Optional, Tuple
+
+import torch
+
+from . import _lib
+from .constant import EPSILON, START_CHECK_STOP
+from .core import UpdateFn, _require_cuda, _stream_handle, half_spectrum, workspace
+from .statistics import ComputeStatsFn, split_stats
+from . import statistics as lstat
+
+
+def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, gf_params, w, T, max_run_iter,
+             keep_intermediary: bool, engine: str, with_box: bool):
+    """cells0 [Ns, Ni, C, *world], K [Ns, C, max_k, *world(-half)], gf [Ns, K, 2], w [Ns, C, K], T [Ns]."""
+    m = update_fn.model
+    _require_cuda('cells0', cells0)
+    dev = cells0.device
+    Ns, Ni = cells0.shape[0], cells0.shape[1]
+    if tuple(cells0.shape[2:]) != (m.C, ) + m.world:
+        raise ValueError(f'cells0 {tuple(cells0.shape)} does not match [Ns, Ni, {m.C}, *{m.world}]')
+    steps = int(max_run_iter)
+    if steps < 0:
+        raise ValueError('max_run_iter must be >= 0')
+    cells0 = cells0.contiguous()
+    kh = half_spectrum(K.to(dev), m.world)
+    if kh.shape[0] != Ns:
+        raise ValueError('K must hold one spectrum per solution')
+    gf = gf_params.to(dev, torch.float32).reshape(Ns, m.K, 2).contiguous()
+    ww = w.to(dev, torch.float32).reshape(Ns, m.C, m.K).contiguous()
+    Tt = torch.as_tensor(T, dtype=torch.float32, device=dev).reshape(-1)
+    if Tt.numel() == 1 and Ns > 1:
+        Tt = Tt.expand(Ns)
+    Tt = Tt.contiguous()
+    nw = Ns * Ni
+    S = m.C + _lib.NSTAT_SCALAR
+    final = torch.empty_like(cells0)
+    stats = torch.empty((Ns, steps, Ni, S), dtype=torch.float32, device=dev)
+    ncont = torch.empty((Ns, Ni), dtype=torch.float32, device=dev)
+    nbox = torch.empty((Ns, Ni), dtype=torch.float32, device=dev) if with_box else None
+    traj = None
+    if keep_intermediary:
+        traj = (torch.empty((steps, nw, m.C) + m.world, dtype=torch.float32, device=dev),
+                torch.empty((steps, nw, m.C) + m.world, dtype=torch.float32, device=dev),
+                torch.empty((steps, nw, m.K) + m.world, dtype=torch.float32, device=dev))
+    lib = _lib.load()
+    eng = _lib.ENGINES[engine]
+    if lib.lgx_select_engine(m.plan.handle, Ns, Ni, eng) < 0:
+        raise _lib.LgxError(_lib.LGX_ERR_UNSUPPORTED, f'no {engine} engine for this model')
+    ws = workspace(lib.lgx_run_workspace_bytes(m.plan.handle, Ns, Ni, steps, eng), dev)
+    job = _lib.Rollout()
+    job.n_sols, job.n_init, job.steps = Ns, Ni, steps
+    job.cells0 = cells0.data_ptr()
+    job.k_half = kh.data_ptr()
+    job.gf_params = gf.data_ptr()
+    job.weights = ww.data_ptr()
+    job.T = Tt.data_ptr()
+    job.stats_R = compute_stats_fn.R
+    job.stats_T = compute_stats_fn.T
+    job.final_cells = final.data_ptr()
+    job.stats = stats.data_ptr() if steps else None
+    job.n_continue = ncont.data_ptr()
+    job.n_box = nbox.data_ptr() if nbox is not None else None
+    if traj is not None:
+        job.traj_cells, job.traj_field, job.traj_potential = (t.data_ptr() for t in traj)
+    job.engine = eng
+    _lib.check(lib.lgx_run(m.plan.handle, job, ws.data_ptr(), ws.numel(), _stream_handle(dev)))
+    return final, stats, ncont, nbox, traj
+
+
+def run_scan(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
+             update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, engine: str = 'auto',
+             with_box: bool = False):
+    """runner.py:119-164.
+
+    cells0 ``[N_init, C, *world]``; K ``[1, C, max_k, *world]`` complex64;
+    returns ``(cells, field, potential, stats)`` with ``cells``/``field``
+    ``[T, N_init, C, *world]``, ``potential`` ``[T, N_init, K, *world]`` and
+    ``stats[k]`` ``[T, N_init]`` (``channel_mass`` ``[T, N_init, C]``) plus
+    ``stats['N']`` ``[N_init]`` (and ``'N_box'`` with ``with_box``).
+    """
+    m = update_fn.model
+    Ni = cells0.shape[0]
+    final, stats, ncont, nbox, traj = _rollout(update_fn, compute_stats_fn, cells0.unsqueeze(0), K.reshape(
+        (1, ) + tuple(K.shape[1:])), gf_params.unsqueeze(0), kernels_weight_per_channel.unsqueeze(0), T, max_run_iter,
+                                               True, engine, with_box)
+    sd = split_stats(stats[0], m.C)
+    sd['N'] = ncont[0]
+    if nbox is not None:
+        sd['N_box'] = nbox[0]
+    cells, field, potential = traj
+    return cells, field, potential, sd
+
+
+def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
+                           update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, engine: str = 'auto',
+                           with_box: bool = False):
+    """runner.py:167-215: all solutions x inits in one engine launch.
+
+    cells0 ``[N_sols, N_init, C, *world]``; K ``[N_sols, 1, C, max_k, *world]``;
+    gf_params ``[N_sols, K, 2]``; weights ``[N_sols, C, K]``; T ``[N_sols]``.
+    Returns ``(stats, final_cells)``: ``stats[k]`` ``[N_sols, T, N_init]``
+    (``channel_mass`` ``[N_sols, T, N_init, C]``), ``stats['N']``
+    ``[N_sols, N_init]``; ``final_cells`` ``[N_sols, N_init, C, *world]``.
+    """
+    m = update_fn.model
+    Ns = cells0.shape[0]
+    Kr = K.reshape((Ns, ) + tuple(K.shape[2:])) if K.dim() == 3 + len(m.world) + 1 else K
+    final, stats, ncont, nbox, _ = _rollout(update_fn, compute_stats_fn, cells0, Kr, gf_params,
+                                            kernels_weight_per_channel, T, max_run_iter, False, engine, with_box)
+    sd = split_stats(stats, m.C)
+    sd['N'] = ncont
+    if nbox is not None:
+        sd['N_box'] = nbox
+    return sd, final
+
+
+def run(rng_key, cells, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
+        update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, stat_trunc: bool = False, engine: str = 'auto'):
+    """runner.py:16-116: single configuration with the eager total-mass
+    heuristics.  The rollout runs on the device in one call; the reference's
+    early ``break`` (runner.py:103-104) truncates the returned trajectory."""
+    assert max_run_iter > 0, f'max_run_iter must be positive, value given: {max_run_iter}'
+    assert cells.shape[0] == 1
+    all_cells, all_fields, all_pots, stats = run_scan(rng_key, cells, K, gf_params, kernels_weight_per_channel, T,
+                                                      max_run_iter, R, update_fn, compute_stats_fn, engine)
+    mass = stats['mass']
+    init_mass = cells.sum()
+    dev = mass.device
+    prev_mass = init_mass
+    prev_sign = torch.zeros(1, dtype=torch.int32, device=dev)
+    counters = lstat.init_counters(1, dev)
+    should = torch.ones(1, dtype=torch.int32, device=dev)
+    last = max_run_iter - 1
+    for it in range(max_run_iter):
+        mt = mass[it]
+        cond = lstat.min_mass_heuristic(EPSILON, mt) & lstat.max_mass_heuristic(init_mass, mt)
+        sign = torch.sign(mt - prev_mass)
+        c1, counters['nb_monotone_step'] = lstat.monotonic_heuristic(sign, prev_sign, counters['nb_monotone_step'])
+        c2, counters['nb_max_volume_step'] = lstat.mass_volume_heuristic(stats['mass_volume'][it],
+                                                                         counters['nb_max_volume_step'])
+        should = should * (cond & c1 & c2)
+        prev_mass = mt
+        prev_sign = sign
+        if stat_trunc and it >= START_CHECK_STOP and int(should[0]) == 0:
+            last = it
+            break
+    n = last + 1
+    out_stats = {k: v[:n] for k, v in stats.items() if k not in ('N', 'N_box')}
+    out_stats['N'] = torch.tensor(last, device=dev)
+    return all_cells[:n], all_fields[:n], all_pots[:n], out_stats

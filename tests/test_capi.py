@@ -1,0 +1,92 @@
+"""C ABI: the library loads, exports every symbol include/*.h declares, and
+validates plans on the host (no device work; runs without a GPU)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from leniax_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    syms = set()
+    for h in glob.glob(os.path.join(ROOT, 'include', '*.h')):
+        txt = open(h).read()
+        syms |= set(re.findall(r'LGX_API\s+[\w\s\*]+?\b(lgx_\w+)\s*\(', txt))
+    return syms
+
+
+def test_header_declares_expected_api():
+    syms = declared_symbols()
+    assert set(_lib.EXPORTED) <= syms, set(_lib.EXPORTED) - syms
+
+
+def test_library_exports_every_declared_symbol():
+    lib = _lib.load()
+    for s in declared_symbols():
+        assert hasattr(lib, s), s
+    assert lib.lgx_version() == 1
+
+
+def _plan(**kw):
+    args = dict(nb_dims=2, world=(128, 128), nb_channels=1, kernel_cin=[0], kernel_slot=[0], growth_ids=[1],
+                max_k=1, state_fn=0, weighted_average=True)
+    args.update(kw)
+    return _lib.Plan(**args)
+
+
+def test_plan_accepts_valid_models():
+    p = _plan()
+    lib = _lib.load()
+    assert lib.lgx_select_engine(p.handle, 1, 4, 0) == 1  # resident for C=1 K=1 128^2
+    assert lib.lgx_select_engine(p.handle, 1, 4, 2) == 2
+    p2 = _plan(nb_channels=3, kernel_cin=[0, 1, 2], kernel_slot=[0, 0, 0], growth_ids=[1, 1, 0], world=(256, 256))
+    assert lib.lgx_select_engine(p2.handle, 1, 4, 0) == 2  # streamed
+    assert lib.lgx_run_workspace_bytes(p2.handle, 2, 3, 16, 0) > 0
+
+
+@pytest.mark.parametrize('kw,code', [
+    (dict(world=(100, 128)), _lib.LGX_ERR_UNSUPPORTED),
+    (dict(nb_dims=4), _lib.LGX_ERR_INVALID),
+    (dict(kernel_cin=[1]), _lib.LGX_ERR_INVALID),
+    (dict(growth_ids=[42]), _lib.LGX_ERR_UNSUPPORTED),
+    (dict(state_fn=7), _lib.LGX_ERR_INVALID),
+    (dict(kernel_slot=[3]), _lib.LGX_ERR_INVALID),
+    (dict(nb_channels=0), _lib.LGX_ERR_INVALID),
+])
+def test_plan_rejects_bad_models(kw, code):
+    with pytest.raises(_lib.LgxError) as e:
+        _plan(**kw)
+    assert e.value.code == code
+    assert _lib.load().lgx_last_error()
+
+
+def test_run_rejects_bad_jobs_without_device_work():
+    p = _plan()
+    lib = _lib.load()
+    job = _lib.Rollout()
+    job.n_sols, job.n_init, job.steps = 1, 1, 4
+    assert lib.lgx_run(p.handle, ctypes.byref(job), None, 0, None) == _lib.LGX_ERR_INVALID  # null tensors
+    buf = (ctypes.c_float * 16)()
+    addr = ctypes.addressof(buf)
+    job.cells0 = job.k_half = job.gf_params = job.weights = job.T = addr
+    job.stats_R, job.stats_T = 13., 10.
+    assert lib.lgx_run(p.handle, ctypes.byref(job), None, 0, None) == _lib.LGX_ERR_WORKSPACE
+    job.n_init = 0
+    assert lib.lgx_run(p.handle, ctypes.byref(job), None, 0, None) == _lib.LGX_ERR_INVALID
+    job.n_init, job.stats_R = 1, 0.
+    assert lib.lgx_run(p.handle, ctypes.byref(job), None, 0, None) == _lib.LGX_ERR_INVALID
+
+
+def test_update_fn_refuses_cpu_tensors():
+    import torch
+    from leniax_gb300 import helpers, kernels
+    from tests.cases import bump_kernel_params
+    K, m = kernels.get_kernels_and_mapping(bump_kernel_params(), [64, 64], 1, 13, device='cpu')
+    u = helpers.build_update_fn(K.shape, m)
+    with pytest.raises(ValueError, match='CUDA'):
+        u(None, torch.zeros(1, 1, 64, 64), K, m.get_gf_params(), m.get_kernels_weight_per_channel(), 0.1)
