@@ -1,0 +1,362 @@
+"""Benchmark: batched Lenia search rollout on the GB300 engine.
+
+Workload (search batch, drop-in for leniax run_scan_mem_optimized): 1024
+worlds of 128x128, C=1 K=1, kernel R=13 one ring exp(4 - 1/(r(1-r))), gaussian
+growth m=0.15 s=0.015, dt=0.1, 1024 Euler steps, uniform[0,1) 48x48 central
+patches scaled by a per-world factor in [0.5, 1] (PCG64 seed 1), per-step
+leniax statistics + mass centroid, leniax stop count N and the box stop set.
+
+One bench "step" = one full rollout of that batch (1024 worlds x 1024 Euler
+steps).  Metric: cell-updates/s = worlds * cells * Euler steps / time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N > 1) each rank runs its own 1024-world batch (worlds are
+independent: weak scaling, no collective on the data path); rank 0 prints the
+JSON line with the max time over ranks.
+"""
+import argparse
+import json
+import os
+import statistics as pystats
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'cell-updates/s'
+WORKLOAD = 'search-1024x128x128-c1k1-1024steps'
+N_WORLDS, SIZE, STEPS_EULER, PATCH, R, T_RATE = 1024, 128, 1024, 48, 13, 10.0
+KPARAMS = [{
+    'k_slug': 'circle_2d', 'k_params': [1.0, [1.0]], 'kf_slug': 'gauss_bump', 'kf_params': [1.0], 'gf_slug': 'gaussian',
+    'gf_params': [0.15, 0.015], 'h': 1.0, 'c_in': 0, 'c_out': 0
+}]
+# per world-step algorithmic flops (P = cells per channel, C = K = 1):
+#   (C+K)*2.5*P*log2(P) + 6*K*(P/2+1) + 8*K*P + 2*K*P + 4*C*P + 10*C*P
+P_CELLS = SIZE * SIZE
+FLOPS_PER_WORLD_STEP = 2 * 2.5 * P_CELLS * np.log2(P_CELLS) + 6 * (P_CELLS // 2 + 1) + (8 + 2 + 4 + 10) * P_CELLS
+CPU_SAMPLE_WORLDS, CPU_SAMPLE_STEPS = 64, 320
+PLAIN_SAMPLE_WORLDS, PLAIN_SAMPLE_STEPS = 4, 64
+
+
+def make_inputs(n_worlds, seed=1):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    cells = np.zeros((1, n_worlds, 1, SIZE, SIZE), np.float32)
+    lo = (SIZE - PATCH) // 2
+    noise = rng.random((n_worlds, PATCH, PATCH), dtype=np.float32)
+    factor = rng.uniform(0.5, 1.0, size=(n_worlds, 1, 1)).astype(np.float32)
+    cells[0, :, 0, lo:lo + PATCH, lo:lo + PATCH] = noise * factor
+    return cells
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except Exception:
+        return os.cpu_count() or 1
+
+
+def cpu_baseline():
+    """FP32 numpy/scipy restatement of the path (the oracle) on the host cores,
+    timed on a bounded sample of the workload."""
+    from oracle import lenia_oracle as O
+    cores = host_cores()
+    K, mp = O.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, np.float32)
+    model = O.Model(mp)
+    cells = make_inputs(CPU_SAMPLE_WORLDS, seed=1)[0]
+    O.run_scan(cells, K, mp['gf_params'], mp['weights'], T_RATE, 4, R, model, keep_intermediary=False, workers=cores)
+    t0 = time.perf_counter()
+    O.run_scan(cells, K, mp['gf_params'], mp['weights'], T_RATE, CPU_SAMPLE_STEPS, R, model, keep_intermediary=False,
+               workers=cores, with_box=True)
+    dt = time.perf_counter() - t0
+    value = CPU_SAMPLE_WORLDS * P_CELLS * CPU_SAMPLE_STEPS / dt
+    return {
+        'value': value, 'unit': METRIC, 'cores': cores, 'kind': 'port',
+        'sample': f'{CPU_SAMPLE_WORLDS} worlds x {CPU_SAMPLE_STEPS} steps of the workload '
+                  f'(numpy/scipy.fft FP32 restatement, scipy workers={cores}), {dt:.1f} s'
+    }
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), f'--query-gpu={self.Q}',
+                                          '--format=csv,noheader,nounits', '-lms', '200'], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['nvidia-smi unavailable']}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        return {'sm_mhz': pystats.median(sm) if sm else None, 'sm_max_mhz': smax, 'reasons': sorted(reasons),
+                'samples': len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except Exception:
+        return {}
+
+
+def committed_traffic():
+    """DRAM bytes per launch of the resident kernel from the committed ncu
+    summary (profiles/), scaled to this workload, or None."""
+    try:
+        d = json.load(open(os.path.join(ROOT, 'profiles', 'resident_traffic.json')))
+        return d.get('dram_bytes_per_launch_full_workload')
+    except Exception:
+        return None
+
+
+def run_ours(args, rank, world_size):
+    import torch
+    from leniax_gb300 import _lib, helpers, kernels, runner, statistics
+
+    dev = torch.device('cuda', int(os.environ.get('LOCAL_RANK', 0)))
+    torch.cuda.set_device(dev)
+    lib = _lib.load()
+    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, dev)
+    upd = helpers.build_update_fn(K.shape, mp)
+    stats_fn = statistics.ComputeStatsFn([SIZE, SIZE], R, T_RATE)
+    cells_np = make_inputs(N_WORLDS, seed=1 + rank)
+    cells = torch.from_numpy(cells_np).to(dev)
+    Kb, gf, w = K[None], mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None]
+    Tt = torch.tensor([T_RATE], device=dev)
+
+    # device-resident rollout through the engine (inputs already in HBM)
+    m = upd.model
+    kh = torch.view_as_real(Kb.reshape(1, 1, 1, SIZE, SIZE)[..., :SIZE // 2 + 1].contiguous())
+    gfc, wc = gf.contiguous(), w.contiguous()
+    final = torch.empty_like(cells)
+    st = torch.empty((1, STEPS_EULER, N_WORLDS, 1 + _lib.NSTAT_SCALAR), device=dev)
+    ncont = torch.empty((1, N_WORLDS), device=dev)
+    nbox = torch.empty((1, N_WORLDS), device=dev)
+    cen = torch.empty((1, STEPS_EULER, N_WORLDS, 2), device=dev)
+    eng = _lib.ENGINES['auto']
+    ws = torch.empty(lib.lgx_run_workspace_bytes(m.plan.handle, 1, N_WORLDS, STEPS_EULER, eng), dtype=torch.uint8,
+                     device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ev_main = [torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)]
+    for e in ev_main:
+        e.record(stream)  # materialise the cudaEvent_t handles
+    job = _lib.Rollout()
+    job.n_sols, job.n_init, job.steps = 1, N_WORLDS, STEPS_EULER
+    job.cells0, job.k_half, job.gf_params, job.weights, job.T = (cells.data_ptr(), kh.data_ptr(), gfc.data_ptr(),
+                                                                  wc.data_ptr(), Tt.data_ptr())
+    job.stats_R, job.stats_T = R, T_RATE
+    job.final_cells, job.stats, job.n_continue, job.n_box = (final.data_ptr(), st.data_ptr(), ncont.data_ptr(),
+                                                              nbox.data_ptr())
+    job.centroid = cen.data_ptr()
+    job.engine = eng
+    job.main_events[0] = ev_main[0].cuda_event
+    job.main_events[1] = ev_main[1].cuda_event
+    engine_used = {1: 'resident', 2: 'streamed'}.get(lib.lgx_select_engine(m.plan.handle, 1, N_WORLDS, eng), '?')
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > 129 MB L2
+
+    def rollout():
+        _lib.check(lib.lgx_run(m.plan.handle, job, ws.data_ptr(), ws.numel(), stream.cuda_stream))
+
+    for _ in range(args.warmup):
+        rollout()
+    torch.cuda.synchronize()
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(dev.index)
+    sampler.start()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    main_ms = []
+    for i in range(args.steps):
+        flush.zero_()  # L2 flush between timed iterations (outside the timed events)
+        evs[i][0].record(stream)
+        rollout()
+        evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        main_ms.append(ev_main[0].elapsed_time(ev_main[1]))
+    torch.cuda.synchronize()
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    if world_size > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    cell_updates = N_WORLDS * P_CELLS * STEPS_EULER
+    value = world_size * cell_updates * args.steps / (total_ms / 1e3)
+    n_alive = float(nbox.mean().item())
+
+    # roofline of the dominant kernel (FP32-pipe bound)
+    kern_ms = pystats.median(main_ms)
+    flops_launch = FLOPS_PER_WORLD_STEP * N_WORLDS * STEPS_EULER
+    sink = torch.empty(4096, device=dev)
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    pb = sms * 8
+    lib.lgx_fp32_probe(sink.data_ptr(), pb, 64, stream.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    iters = 4096
+    pf = lib.lgx_fp32_probe(sink.data_ptr(), pb, iters, stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp32_peak = pf / (e0.elapsed_time(e1) / 1e3) / 1e12
+    achieved = flops_launch / (kern_ms / 1e3) / 1e12
+
+    # end to end through the public API: pinned host inputs -> device -> rollout -> host results
+    host_cells = torch.from_numpy(cells_np).pin_memory()
+    e2e_times = []
+    h2d = host_cells.numel() * 4  # the batch of initial states; spectra and parameters stay resident
+    d2h = 0
+    for i in range(max(2, min(args.steps, 3)) + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        c_dev = host_cells.to(dev, non_blocking=True)
+        sd, fin = runner.run_scan_mem_optimized(None, c_dev, Kb, gf, w, Tt, STEPS_EULER, R, upd, stats_fn,
+                                                with_box=True, with_centroid=True)
+        outs = [sd['mass'].to('cpu', non_blocking=True), sd['mass_centroid'].to('cpu', non_blocking=True),
+                sd['N'].to('cpu', non_blocking=True), sd['N_box'].to('cpu', non_blocking=True),
+                fin.to('cpu', non_blocking=True)]
+        torch.cuda.synchronize()
+        if i > 0:
+            e2e_times.append(time.perf_counter() - t0)
+        d2h = sum(o.numel() * 4 for o in outs)
+    e2e_value = world_size * cell_updates / pystats.median(e2e_times)
+
+    # plain one-world-per-launch engine on a sample of the same workload
+    sub = cells[:, :PLAIN_SAMPLE_WORLDS].contiguous()
+    runner.run_scan_mem_optimized(None, sub, Kb, gf, w, Tt, 4, R, upd, stats_fn, engine='plain')
+    torch.cuda.synchronize()
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    runner.run_scan_mem_optimized(None, sub, Kb, gf, w, Tt, PLAIN_SAMPLE_STEPS, R, upd, stats_fn, engine='plain')
+    p1.record(stream)
+    torch.cuda.synchronize()
+    plain_value = PLAIN_SAMPLE_WORLDS * P_CELLS * PLAIN_SAMPLE_STEPS / (p0.elapsed_time(p1) / 1e3)
+
+    gpu_launches = args.steps * 4  # prepare spectrum, resident kernel, stats, heuristics per rollout
+    out = {
+        'metric': METRIC,
+        'value': value,
+        'unit': METRIC,
+        'n_gpus': world_size,
+        'steps': args.steps,
+        'warmup': args.warmup,
+        'ms_per_step': ms_per_step,
+        'higher_is_better': True,
+        'scaling': 'weak',
+        'vs_baseline': None,
+        'dtype': 'f32',
+        'data': 'synthetic (PCG64 seeded uniform patches)',
+        'config': {
+            'workload': WORKLOAD, 'worlds_per_gpu': N_WORLDS, 'world': [SIZE, SIZE], 'channels': 1, 'kernels': 1,
+            'euler_steps_per_step': STEPS_EULER, 'engine': engine_used, 'parallelism': f'replicas{world_size}',
+            'l2': 'flushed between timed iterations (256 MB write)', 'stats': 'leniax 12 stats + centroid per step',
+            'stop_sets': ['leniax check_heuristics', 'box (mass<1e-3, mass>0.9 area, border)'],
+            'mean_stop_step_box_set': n_alive
+        },
+        'e2e': {'value': e2e_value, 'unit': METRIC, 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
+        'roofline': {
+            'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s', 'frac': achieved / fp32_peak,
+            'traffic': committed_traffic(), 'kernel': 'resident_kernel<128,8>', 'kernel_ms': kern_ms,
+            'flops_per_launch': flops_launch,
+            'peak_source': 'measured in-bench (FFMA probe kernel, burst); MEASURED_PEAKS.json has no FP32 entry'
+        },
+        'plain': {
+            'value': plain_value, 'unit': METRIC,
+            'sample': f'{PLAIN_SAMPLE_WORLDS} worlds x {PLAIN_SAMPLE_STEPS} steps, one world and one step per launch',
+            'speedup_batched_vs_plain': value / world_size / plain_value
+        },
+        'clocks': clocks,
+        'gpu_launches': gpu_launches,
+        'hbm_peak_gbs_measured': measured_peaks().get('hbm_gbs'),
+    }
+    return out
+
+
+def run_reference(args):
+    """Reference arm: the reference's CPU algorithm for this path (leniax's JAX
+    is not installable here, so its numpy restatement), all host threads."""
+    cb = cpu_baseline()
+    return {
+        'impl': 'reference', 'metric': METRIC, 'value': cb['value'], 'unit': METRIC, 'n_gpus': args.gpus,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': None, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (PCG64 seeded uniform patches)',
+        'config': {'workload': WORKLOAD, 'parallelism': 'host cores'},
+        'cpu_baseline': cb,
+        'e2e': {'value': cb['value'], 'unit': METRIC, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    args = ap.parse_args()
+    world_size = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    if args.impl == 'reference':
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world_size > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get('LOCAL_RANK', 0)))
+        torch.distributed.init_process_group('nccl')
+    out = run_ours(args, rank, world_size)
+    if rank == 0:
+        out['cpu_baseline'] = cpu_baseline()
+        print(json.dumps(out))
+    if world_size > 1:
+        import torch
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == '__main__':
+    main()

@@ -117,6 +117,14 @@ typedef struct lgx_rollout {
   float* traj_field;     /* [steps, Ns*Ni, C, *world] or NULL                    */
   float* traj_potential; /* [steps, Ns*Ni, K, *world] or NULL                    */
   int engine;            /* LGX_ENGINE_*                                         */
+  float* centroid;       /* [Ns, steps, Ni, nb_dims] per-step mass centroid as an
+                            absolute torus position in [0, size) per axis (the
+                            centred-frame centroid of statistics.py:83 plus the
+                            carried shift), or NULL                              */
+  void* main_events[2];  /* optional cudaEvent_t pair the engine records on the
+                            stream right before and after its dominant kernel(s)
+                            (the resident kernel, or the streamed step loop), so
+                            callers can time them without a host sync; NULL to skip */
 } lgx_rollout;
 
 /* ABI version (LGX_ABI_VERSION). */
@@ -155,6 +163,13 @@ LGX_API size_t lgx_update_workspace_bytes(const lgx_plan* plan, int n);
 LGX_API int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_half, const float* gf_params,
                const float* weights, const float* dt, int dt_per_world, float* state_out, float* field_out,
                float* potential_out, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Measurement helper (no counterpart in the reference): launch a pure-FMA
+ * kernel of `blocks` x 256 threads and return the number of FP32 flops it
+ * performs (or -1).  Timing it with events gives the FP32-pipe peak used as
+ * the roofline of the resident engine.  `sink` is a device buffer of at
+ * least `blocks` floats (written only if an impossible value appears). */
+LGX_API long long lgx_fp32_probe(float* sink, int blocks, int iters, void* stream);
 
 #ifdef __cplusplus
 }

@@ -34,7 +34,7 @@ NSTAT_SCALAR = 11
 
 EXPORTED = (
     'lgx_version', 'lgx_last_error', 'lgx_plan_create', 'lgx_plan_destroy', 'lgx_select_engine',
-    'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update'
+    'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update', 'lgx_fp32_probe'
 )
 
 
@@ -84,6 +84,8 @@ class Rollout(ctypes.Structure):
         ('traj_field', _fp),
         ('traj_potential', _fp),
         ('engine', ctypes.c_int),
+        ('centroid', _fp),
+        ('main_events', _fp * 2),
     ]
 
 
@@ -119,6 +121,8 @@ def load():
         lib.lgx_update.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 5 + [ctypes.c_int] + \
             [ctypes.c_void_p] * 3 + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
         lib.lgx_update.restype = ctypes.c_int
+        lib.lgx_fp32_probe.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
+        lib.lgx_fp32_probe.restype = ctypes.c_longlong
         if lib.lgx_version() != 1:
             raise RuntimeError('leniax_gb300 engine ABI version mismatch')
         _lib = lib

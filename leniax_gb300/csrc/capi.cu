@@ -234,8 +234,10 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     const int wpc = 512 / ((m.H / 2) * (m.H == 128 ? 8 : 4));
     const int items = (nw + wpc - 1) / wpc;
     const int grid = std::max(1, std::min(items, resident_max_grid(m.H)));
+    if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
     ce = launch_resident(m.H, a, grid, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "resident kernel");
+    if (j->main_events[1]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[1]), st);
   } else {
     StreamedBufs b = carve_streamed(m, j->n_sols, j->n_init, j->steps, ws, ws_bytes, true);
     raw = b.raw;
@@ -247,6 +249,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     const long raws = raw_stride(m.C);
     const bool plain = (e == LGX_ENGINE_PLAIN);
     const float* cur = j->cells0;
+    if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
     for (int s = 0; s < j->steps; ++s) {
       float* out = (s == j->steps - 1 && j->final_cells) ? j->final_cells : ((s & 1) ? b.sb : b.sa);
       if (j->traj_cells) {
@@ -305,6 +308,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
       }
       cur = out;
     }
+    if (j->main_events[1]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[1]), st);
     if (j->final_cells && cur != j->final_cells) {
       ce = cudaMemcpyAsync(j->final_cells, cur, (size_t)nw * plane * sizeof(float), cudaMemcpyDeviceToDevice, st);
       if (ce != cudaSuccess) return cuda_fail(ce, "final copy");
@@ -324,6 +328,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
   sa.stats = j->stats;
   sa.n_continue = j->n_continue;
   sa.n_box = j->n_box;
+  sa.centroid = j->centroid;
   ce = launch_stats(sa, st);
   if (ce != cudaSuccess) return cuda_fail(ce, "stats kernels");
   g_err.clear();

@@ -24,8 +24,8 @@ enum RawSlot : int {
   RAW_GX = 8,       // 3 slots: sum max(field,0) * c_a
   RAW_MX2 = 11,     // 3 slots: sum cells * c_a^2
   RAW_BORDER = 14,  // 1 if a live cell (> eps) lies on the outer layer of the un-centred world
-  RAW_RESERVED = 15,
-  RAW_CM = 16,      // C slots: per-channel sum of cells
+  RAW_SHIFT = 15,   // 3 slots: carried torus shift used to centre this step (per axis)
+  RAW_CM = 18,      // C slots: per-channel sum of cells
 };
 __host__ __device__ constexpr int raw_stride(int C) { return RAW_CM + C; }
 

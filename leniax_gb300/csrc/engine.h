@@ -96,6 +96,7 @@ struct StatsArgs {
   float* stats;       // [Ns, steps, Ni, C + 11] or null
   float* n_continue;  // [Ns, Ni] or null
   float* n_box;       // [Ns, Ni] or null
+  float* centroid;    // [Ns, steps, Ni, nb_dims] or null
 };
 cudaError_t launch_stats(const StatsArgs& a, cudaStream_t st);
 

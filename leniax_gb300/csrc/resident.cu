@@ -305,6 +305,7 @@ __global__ void __launch_bounds__(512, 1) resident_kernel(ResidentArgs a) {
       named_bar(bar_id, NT);
       // --------------------------------------------- per-step finalisation
       if (wid == 0) {
+        const int sy = shv[0], sx = shv[1];  // shift that centred this step
         float v = 0.f;
         if (lane < 12) {
           for (int w = 0; w < NW; ++w) v += part[w * 16 + lane];
@@ -323,13 +324,14 @@ __global__ void __launch_bounds__(512, 1) resident_kernel(ResidentArgs a) {
         } else if (lane < 16) {
           const int zero_slots[3] = {RAW_MX + 2, RAW_GX + 2, RAW_MX2 + 2};
           rw[zero_slots[lane - 13]] = 0.f;
-        } else if (lane == 16) {
-          rw[RAW_RESERVED] = 0.f;
+        } else if (lane < 19) {
+          rw[RAW_SHIFT + lane - 16] = (lane == 16) ? (float)sy : (lane == 17 ? (float)sx : 0.f);
         }
+        __syncwarp();
         if (lane == 0) {
           const float cy = mxy / (m00 + kEps), cx = mxx / (m00 + kEps);
-          shv[0] = pmod(shv[0] + (int)cy, N);
-          shv[1] = pmod(shv[1] + (int)cx, N);
+          shv[0] = pmod(sy + (int)cy, N);
+          shv[1] = pmod(sx + (int)cx, N);
         }
       }
     }

@@ -20,78 +20,125 @@ constexpr float kRad2Deg = 57.295779513082320876798f;  // 180/pi
 struct Ctx {
   int nd, C, steps, n_init;
   float R, dt;
+  int world[3];
 };
 
-__device__ __forceinline__ const float* raw_at(const float* raw, const Ctx& c, int sol, int step, int init) {
+// Per-axis triples are kept as named scalars and returned by value (no
+// partially written local arrays): an earlier array-based form of this kernel
+// was mis-optimised by nvcc 13.0 at -O3 (correct only at -G).
+struct Tri {
+  float a0, a1, a2;
+};
+
+__device__ __forceinline__ const float* raw_at(const float* raw, const Ctx c, int sol, int step, int init) {
   return raw + (((size_t)sol * c.steps + step) * c.n_init + init) * raw_stride(c.C);
 }
 
-__device__ __forceinline__ void centroid(const float* r, int nd, float* out) {
-  const float m00 = r[RAW_M00];
-  for (int a = 0; a < nd; ++a) out[a] = r[RAW_MX + a] / (m00 + kEps);
+// mass centroid of a step's moments (statistics.py:83)
+__device__ __forceinline__ Tri centroid(const float* r, int nd) {
+  const float den = r[RAW_M00] + kEps;
+  Tri o;
+  o.a0 = r[RAW_MX + 0] / den;
+  o.a1 = nd > 1 ? r[RAW_MX + 1] / den : 0.f;
+  o.a2 = nd > 2 ? r[RAW_MX + 2] / den : 0.f;
+  return o;
 }
 
-// carried (fractional) centroid entering step t
-__device__ __forceinline__ void prev_frac(const float* raw, const Ctx& c, int sol, int step, int init, float* out) {
-  if (step == 0) {
-    for (int a = 0; a < 3; ++a) out[a] = 0.f;
-    return;
-  }
-  float cc[3] = {0.f, 0.f, 0.f};
-  centroid(raw_at(raw, c, sol, step - 1, init), c.nd, cc);
-  for (int a = 0; a < 3; ++a) out[a] = cc[a] - truncf(cc[a]);
+__device__ __forceinline__ Tri frac(Tri c) {  // x - trunc(x): the carried centroid (statistics.py:124)
+  Tri o;
+  o.a0 = c.a0 - truncf(c.a0);
+  o.a1 = c.a1 - truncf(c.a1);
+  o.a2 = c.a2 - truncf(c.a2);
+  return o;
 }
 
-__device__ __forceinline__ float angle_of(const float* delta, float dist, const Ctx& c) {
-  const float ang = atan2f(delta[1], delta[0]) * kRad2Deg;  // jnp.degrees(arctan2(d1, d0))
-  return ang * ((dist / c.R > 0.001f) ? 1.f : 0.f);
+__device__ __forceinline__ Tri sub(Tri a, Tri b) {
+  Tri o;
+  o.a0 = a.a0 - b.a0;
+  o.a1 = a.a1 - b.a1;
+  o.a2 = a.a2 - b.a2;
+  return o;
 }
 
-__global__ void stats_kernel(Ctx c, int n_sols, const float* __restrict__ raw, float* __restrict__ stats) {
+__device__ __forceinline__ float norm(Tri d, int nd) {
+  float s = d.a0 * d.a0;
+  if (nd > 1) s += d.a1 * d.a1;
+  if (nd > 2) s += d.a2 * d.a2;
+  return sqrtf(s);
+}
+
+// jnp.degrees(arctan2(delta[1], delta[0])) * (dist / R > 0.001)   (statistics.py:89)
+__device__ __forceinline__ float angle_of(Tri d, float dist, float R) {
+  const float ang = atan2f(d.a1, d.a0) * kRad2Deg;
+  return ang * ((dist / R > 0.001f) ? 1.f : 0.f);
+}
+
+// Absolute torus position of the centroid: centred-frame centroid + N/2 +
+// carried shift, wrapped to [0, N).
+__device__ __forceinline__ float wrap_pos(float cen, float shift, int n) {
+  float p = fmodf(cen + (float)(n / 2) + shift, (float)n);
+  return p < 0.f ? p + (float)n : p;
+}
+
+__global__ void stats_kernel(Ctx c, int n_sols, const float* __restrict__ raw, float* __restrict__ stats,
+                             float* __restrict__ centroid_out) {
   const long total = (long)n_sols * c.steps * c.n_init;
   const long i = blockIdx.x * (long)blockDim.x + threadIdx.x;
   if (i >= total) return;
   const int init = (int)(i % c.n_init);
   const int step = (int)((i / c.n_init) % c.steps);
   const int sol = (int)(i / ((long)c.n_init * c.steps));
+  const int nd = c.nd;
   const float* r = raw_at(raw, c, sol, step, init);
   const float R2 = c.R * c.R;
   const float m00 = r[RAW_M00], g00 = r[RAW_G00];
-  float cen[3] = {0.f, 0.f, 0.f}, pc[3];
-  centroid(r, c.nd, cen);
-  prev_frac(raw, c, sol, step, init, pc);
-  float delta[3] = {0.f, 0.f, 0.f}, d2 = 0.f;
-  for (int a = 0; a < c.nd; ++a) {
-    delta[a] = cen[a] - pc[a];
-    d2 += delta[a] * delta[a];
-  }
-  const float dist_m = sqrtf(d2);
-  const float mass_angle = angle_of(delta, dist_m, c);
+  const Tri zero = {0.f, 0.f, 0.f};
+  const Tri cen = centroid(r, nd);
+  // carried centroid entering this step, and the angle carried from the previous step
+  Tri pc = zero;
   float prev_angle = 0.f;
   if (step > 0) {
-    float c1[3] = {0.f, 0.f, 0.f}, p1[3], dl[3] = {0.f, 0.f, 0.f}, e2 = 0.f;
-    centroid(raw_at(raw, c, sol, step - 1, init), c.nd, c1);
-    prev_frac(raw, c, sol, step - 1, init, p1);
-    for (int a = 0; a < c.nd; ++a) {
-      dl[a] = c1[a] - p1[a];
-      e2 += dl[a] * dl[a];
+    const Tri c1 = centroid(raw_at(raw, c, sol, step - 1, init), nd);
+    pc = frac(c1);
+    const Tri p1 = (step > 1) ? frac(centroid(raw_at(raw, c, sol, step - 2, init), nd)) : zero;
+    const Tri d1 = sub(c1, p1);
+    prev_angle = angle_of(d1, norm(d1, nd), c.R);
+  }
+  const Tri delta = sub(cen, pc);
+  const float dist_m = norm(delta, nd);
+  const float mass_angle = angle_of(delta, dist_m, c.R);
+  // growth centroid distance and inertia (statistics.py:93-100)
+  const float gden = g00 + kEps, mden = m00 * m00 + kEps;
+  float gcd2, inertia;
+  {
+    const float g0 = r[RAW_GX + 0] / gden - cen.a0;
+    gcd2 = g0 * g0;
+    inertia = (r[RAW_MX2 + 0] - cen.a0 * r[RAW_MX + 0]) / mden;
+    if (nd > 1) {
+      const float g1 = r[RAW_GX + 1] / gden - cen.a1;
+      gcd2 += g1 * g1;
+      inertia += (r[RAW_MX2 + 1] - cen.a1 * r[RAW_MX + 1]) / mden;
     }
-    prev_angle = angle_of(dl, sqrtf(e2), c);
+    if (nd > 2) {
+      const float g2 = r[RAW_GX + 2] / gden - cen.a2;
+      gcd2 += g2 * g2;
+      inertia += (r[RAW_MX2 + 2] - cen.a2 * r[RAW_MX + 2]) / mden;
+    }
   }
-  float gcd2 = 0.f, inertia = 0.f;
-  for (int a = 0; a < c.nd; ++a) {
-    const float gc = r[RAW_GX + a] / (g00 + kEps);
-    gcd2 += (gc - cen[a]) * (gc - cen[a]);
-    const float mux2 = r[RAW_MX2 + a] - cen[a] * r[RAW_MX + a];
-    inertia += mux2 / (m00 * m00 + kEps);
-  }
-  float ang = mass_angle - prev_angle + 540.f;  // python-style modulo (jnp %)
+  const float ang = mass_angle - prev_angle + 540.f;  // python-style modulo (jnp %)
   float md = fmodf(ang, 360.f);
-  if (md != 0.f && md < 0.f) md += 360.f;
+  if (md < 0.f) md += 360.f;
   const float mass = m00 / R2;
   const float mass_volume = r[RAW_CNT_MASS] / R2;
   const float growth = g00 / R2;
   const float growth_volume = r[RAW_CNT_GROW] / R2;
+  if (centroid_out) {
+    float* co = centroid_out + i * (size_t)nd;
+    co[0] = wrap_pos(cen.a0, r[RAW_SHIFT + 0], c.world[0]);
+    if (nd > 1) co[1] = wrap_pos(cen.a1, r[RAW_SHIFT + 1], c.world[1]);
+    if (nd > 2) co[2] = wrap_pos(cen.a2, r[RAW_SHIFT + 2], c.world[2]);
+  }
+  if (!stats) return;
   float* o = stats + i * (size_t)(c.C + LGX_NSTAT_SCALAR);
   for (int ch = 0; ch < c.C; ++ch) o[ch] = r[RAW_CM + ch] / R2;
   float* s = o + c.C;
@@ -158,10 +205,11 @@ cudaError_t launch_stats(const StatsArgs& a, cudaStream_t st) {
   c.n_init = a.n_init;
   c.R = a.R;
   c.dt = 1.f / a.T;
+  for (int d = 0; d < 3; ++d) c.world[d] = a.world[d];
   if (a.steps <= 0) return cudaSuccess;
-  if (a.stats) {
+  if (a.stats || a.centroid) {
     const long total = (long)a.n_sols * a.steps * a.n_init;
-    stats_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c, a.n_sols, a.raw, a.stats);
+    stats_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c, a.n_sols, a.raw, a.stats, a.centroid);
   }
   if (a.n_continue || a.n_box) {
     float area = (float)a.C;

@@ -357,7 +357,7 @@ __global__ void __launch_bounds__(128) row_inv_kernel(int n_worlds, int n_init, 
     rd[RAW_MX2 + 1] = acc[10];
     rd[RAW_MX2 + 2] = 0.f;
     rd[RAW_BORDER] = anyb ? 1.f : 0.f;
-    rd[RAW_RESERVED] = 0.f;
+    rd[RAW_SHIFT + 0] = rd[RAW_SHIFT + 1] = rd[RAW_SHIFT + 2] = 0.f;
     for (int co = 0; co < C; ++co) rd[RAW_CM + co] = cm_part[co];
   }
   __syncthreads();
@@ -382,22 +382,27 @@ __global__ void reduce_kernel(int n_worlds, int n_init, int bpw, int C, int H, i
   const int sol = n / n_init, init = n - sol * n_init;
   float* rw = raw ? raw + sol * raw_sol_stride + init * raw_init_stride : nullptr;
   float m00 = 0.f, mxy = 0.f, mxx = 0.f;
+  const int sh0 = shift[3 * n], sh1 = shift[3 * n + 1];
   for (int s = lane; s < RAWS; s += 32) {
     float v = 0.f;
     for (int b = 0; b < bpw; ++b) v += partial[((size_t)n * bpw + b) * RAWS + s];
     if (s == RAW_BORDER) v = v > 0.f ? 1.f : 0.f;
+    if (s == RAW_SHIFT) v = (float)sh0;
+    if (s == RAW_SHIFT + 1) v = (float)sh1;
+    if (s == RAW_SHIFT + 2) v = 0.f;
     if (rw) rw[s] = v;
     if (s == RAW_M00) m00 = v;
     if (s == RAW_MX) mxy = v;
     if (s == RAW_MX + 1) mxx = v;
   }
+  __syncwarp();
   m00 = __shfl_sync(0xffffffffu, m00, RAW_M00);
   mxy = __shfl_sync(0xffffffffu, mxy, RAW_MX);
   mxx = __shfl_sync(0xffffffffu, mxx, RAW_MX + 1);
   if (lane == 0) {
     const float cy = mxy / (m00 + kEps), cx = mxx / (m00 + kEps);
-    shift[3 * n] = pmod(shift[3 * n] + (int)cy, H);
-    shift[3 * n + 1] = pmod(shift[3 * n + 1] + (int)cx, W);
+    shift[3 * n] = pmod(sh0 + (int)cy, H);
+    shift[3 * n + 1] = pmod(sh1 + (int)cx, W);
   }
 }
 

@@ -18,7 +18,7 @@ from . import statistics as lstat
 
 
 def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, gf_params, w, T, max_run_iter,
-             keep_intermediary: bool, engine: str, with_box: bool):
+             keep_intermediary: bool, engine: str, with_box: bool, with_centroid: bool = False):
     """cells0 [Ns, Ni, C, *world], K [Ns, C, max_k, *world(-half)], gf [Ns, K, 2], w [Ns, C, K], T [Ns]."""
     m = update_fn.model
     _require_cuda('cells0', cells0)
@@ -45,6 +45,7 @@ def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, g
     stats = torch.empty((Ns, steps, Ni, S), dtype=torch.float32, device=dev)
     ncont = torch.empty((Ns, Ni), dtype=torch.float32, device=dev)
     nbox = torch.empty((Ns, Ni), dtype=torch.float32, device=dev) if with_box else None
+    cen = torch.empty((Ns, steps, Ni, len(m.world)), dtype=torch.float32, device=dev) if with_centroid else None
     traj = None
     if keep_intermediary:
         traj = (torch.empty((steps, nw, m.C) + m.world, dtype=torch.float32, device=dev),
@@ -71,37 +72,42 @@ def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, g
     if traj is not None:
         job.traj_cells, job.traj_field, job.traj_potential = (t.data_ptr() for t in traj)
     job.engine = eng
+    job.centroid = cen.data_ptr() if (cen is not None and steps) else None
     _lib.check(lib.lgx_run(m.plan.handle, job, ws.data_ptr(), ws.numel(), _stream_handle(dev)))
-    return final, stats, ncont, nbox, traj
+    return final, stats, ncont, nbox, traj, cen
 
 
 def run_scan(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
              update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, engine: str = 'auto',
-             with_box: bool = False):
+             with_box: bool = False, with_centroid: bool = False):
     """runner.py:119-164.
 
     cells0 ``[N_init, C, *world]``; K ``[1, C, max_k, *world]`` complex64;
     returns ``(cells, field, potential, stats)`` with ``cells``/``field``
     ``[T, N_init, C, *world]``, ``potential`` ``[T, N_init, K, *world]`` and
     ``stats[k]`` ``[T, N_init]`` (``channel_mass`` ``[T, N_init, C]``) plus
-    ``stats['N']`` ``[N_init]`` (and ``'N_box'`` with ``with_box``).
+    ``stats['N']`` ``[N_init]``.  Extensions: ``with_box`` adds ``'N_box'``
+    (box stop set) and ``with_centroid`` adds ``'mass_centroid'`` ``[T,
+    N_init, nb_dims]``, the per-step mass centroid as an absolute torus
+    position.
     """
     m = update_fn.model
-    Ni = cells0.shape[0]
-    final, stats, ncont, nbox, traj = _rollout(update_fn, compute_stats_fn, cells0.unsqueeze(0), K.reshape(
+    final, stats, ncont, nbox, traj, cen = _rollout(update_fn, compute_stats_fn, cells0.unsqueeze(0), K.reshape(
         (1, ) + tuple(K.shape[1:])), gf_params.unsqueeze(0), kernels_weight_per_channel.unsqueeze(0), T, max_run_iter,
-                                               True, engine, with_box)
+                                                    True, engine, with_box, with_centroid)
     sd = split_stats(stats[0], m.C)
     sd['N'] = ncont[0]
     if nbox is not None:
         sd['N_box'] = nbox[0]
+    if cen is not None:
+        sd['mass_centroid'] = cen[0]
     cells, field, potential = traj
     return cells, field, potential, sd
 
 
 def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
                            update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, engine: str = 'auto',
-                           with_box: bool = False):
+                           with_box: bool = False, with_centroid: bool = False):
     """runner.py:167-215: all solutions x inits in one engine launch.
 
     cells0 ``[N_sols, N_init, C, *world]``; K ``[N_sols, 1, C, max_k, *world]``;
@@ -113,12 +119,15 @@ def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_cha
     m = update_fn.model
     Ns = cells0.shape[0]
     Kr = K.reshape((Ns, ) + tuple(K.shape[2:])) if K.dim() == 3 + len(m.world) + 1 else K
-    final, stats, ncont, nbox, _ = _rollout(update_fn, compute_stats_fn, cells0, Kr, gf_params,
-                                            kernels_weight_per_channel, T, max_run_iter, False, engine, with_box)
+    final, stats, ncont, nbox, _, cen = _rollout(update_fn, compute_stats_fn, cells0, Kr, gf_params,
+                                                 kernels_weight_per_channel, T, max_run_iter, False, engine, with_box,
+                                                 with_centroid)
     sd = split_stats(stats, m.C)
     sd['N'] = ncont
     if nbox is not None:
         sd['N_box'] = nbox
+    if cen is not None:
+        sd['mass_centroid'] = cen
     return sd, final
 
 

@@ -506,6 +506,10 @@ def compute_stats(cells, field, potential, prev_shift, prev_centroid, prev_angle
         'potential_volume': potential_volume,
     }
     stats = {k: np.asarray(v, dtype=dtype) for k, v in stats.items()}
+    # absolute torus position of the centroid (this project's extra output):
+    # centred-frame centroid + size//2 + carried shift, wrapped to [0, size)
+    sizes = np.array(ws, dtype=np.float64).reshape(-1, 1)
+    stats['mass_centroid'] = np.mod(mass_centroid + (sizes // 2) + prev_shift.T, sizes).T.astype(dtype)
     shift_idx = np.trunc(mass_centroid).astype(np.int64).T
     total_shift = np.mod(prev_shift + shift_idx, np.array(ws, dtype=np.int64)).astype(np.int32)
     frac = (mass_centroid - np.trunc(mass_centroid)).astype(dtype)
@@ -585,7 +589,7 @@ BOX_MAX_FRAC = 0.9
 def box_stop_flags(cells):
     """Per-world boolean ``continue`` flag of the box stop set for one step."""
     nd = cells.ndim - 2
-    area = float(np.prod(cells.shape[2:]))
+    area = float(np.prod(cells.shape[1:]))  # channels x world cells
     raw = cells.reshape(cells.shape[0], -1).sum(axis=1)
     alive = cells > EPSILON
     touch = np.zeros(cells.shape[0], dtype=bool)
@@ -619,13 +623,13 @@ def run_scan(cells0, K, gf_params, weights, T, max_run_iter, R, model: Model, T_
     centroid = np.zeros((nd, N), dtype=dtype)
     angle = np.zeros(N, dtype=dtype)
     cells = cells0
-    all_stats = {k: [] for k in STAT_KEYS}
+    all_stats = {k: [] for k in STAT_KEYS + ('mass_centroid', )}
     ys_cells, ys_field, ys_pot = [], [], []
     box = []
     for _ in range(max_run_iter):
         new_cells, field, potential = update(cells, K, gf_params, weights, dt, model, workers)
         st, shift, centroid, angle = compute_stats(cells, field, potential, shift, centroid, angle, R, T_static)
-        for k in STAT_KEYS:
+        for k in all_stats:
             all_stats[k].append(st[k])
         if with_box:
             box.append(box_stop_flags(cells))

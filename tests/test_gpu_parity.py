@@ -123,17 +123,25 @@ def test_rollout_matches_fp64_oracle(cuda, engine):
     stats_fn = statistics.ComputeStatsFn([128, 128], 13, 10)
     sd, fin = runner.run_scan_mem_optimized(None, torch.from_numpy(cells[None]).to(dev), K[None],
                                             mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None],
-                                            torch.tensor([10.]), 128, 13, upd, stats_fn, engine=engine)
+                                            torch.tensor([10.]), 128, 13, upd, stats_fn, engine=engine,
+                                            with_centroid=True)
     fin = fin.cpu().numpy()[0]
     assert np.abs(fin - fin64).max() <= 1e-4
     mass = sd['mass'][0, :, 0].cpu().numpy()
     m64 = st64['mass'][:, 0]
-    assert (np.abs(mass - m64) / np.abs(m64)).max() <= 1e-4
-    # centroid (raw moments / mass) via inertia-free path: compare growth & mass speeds where mass moves
+    alive = m64 > 1e-3  # this world decays; relative errors are taken while it has mass
+    assert alive.sum() > 10
+    assert (np.abs(mass - m64)[alive] / m64[alive]).max() <= 1e-4
+    assert np.abs(mass[~alive] - m64[~alive]).max() <= 1e-6
+    cen = sd['mass_centroid'][0, :, 0].cpu().numpy()  # [T, 2] absolute torus positions
+    c64 = st64['mass_centroid'][:, 0]
+    d = np.abs(cen - c64)
+    d = np.minimum(d, 128 - d)  # circular difference
+    assert (d[alive] / np.maximum(c64[alive], 1.0)).max() <= 1e-4
     for key in ('mass_volume', 'growth', 'potential_volume', 'inertia'):
         a = sd[key][0, :, 0].cpu().numpy()
         b = st64[key][:, 0]
-        assert (np.abs(a - b) / np.maximum(np.abs(b), 1e-3)).max() <= 1e-3, key
+        assert (np.abs(a - b) / np.maximum(np.abs(b), 1e-3))[alive].max() <= 1e-3, key
     assert int(sd['N'][0, 0]) == int(st64['N'][0])
 
 
@@ -158,12 +166,19 @@ def test_mem_optimized_batch_matches_oracle_and_engines_agree(cuda):
                                                      torch.stack(gfs), torch.stack(ws), Ts, steps, R, upd, stats_fn,
                                                      engine=engine, with_box=True)
     for s in range(Ns):
-        Ko, mpo, model = oracle_model(bump_kernel_params(m=ms[s], s=0.02), [size, size], 1, R)
-        st, fin = O.run_scan(cells[s], Ko, mpo['gf_params'], mpo['weights'], Ts[s].item(), steps, R, model,
-                             T_static=10, keep_intermediary=False, with_box=True)
+        res = {}
+        for dt in (np.float32, np.float64):
+            Ko, mpo, model = oracle_model(bump_kernel_params(m=ms[s], s=0.02), [size, size], 1, R, dtype=dt)
+            res[dt] = O.run_scan(cells[s].astype(dt), Ko, mpo['gf_params'], mpo['weights'], Ts[s].item(), steps, R,
+                                 model, T_static=10, keep_intermediary=False, with_box=True)
+        st, fin = res[np.float64]
+        # noise worlds are chaotic: FP32 rounding differences grow over the
+        # rollout.  The engine must stay within a few times the oracle's own
+        # FP32-vs-FP64 spread.
+        spread = np.abs(res[np.float32][1] - fin).max()
         for engine, (sd, fin_e) in outs.items():
             fe = fin_e[s].cpu().numpy()
-            assert np.abs(fe - fin).max() < 5e-4, engine
+            assert np.abs(fe - fin).max() <= max(2e-4, 8 * spread), (engine, spread)
             np.testing.assert_array_equal(sd['N'][s].cpu().numpy(), st['N'], err_msg=engine)
             np.testing.assert_array_equal(sd['N_box'][s].cpu().numpy(), st['N_box'], err_msg=engine)
             mass = sd['mass'][s].cpu().numpy()
@@ -209,4 +224,9 @@ def test_trajectory_outputs_match_oracle(cuda):
         for k in statistics.STAT_KEYS:
             a, b = st[k].cpu().numpy(), st_o[k]
             assert a.shape == b.shape, k
-            assert np.allclose(a, b, rtol=1e-4, atol=1e-4), (engine, k, np.abs(a - b).max())
+            # the *_volume statistics count cells above EPSILON=1e-7; far from the
+            # creature the FFT potential is round-off noise of that size, so a
+            # few cells may flip between two FP32 implementations
+            atol = 8 / 13.**2 if k.endswith('volume') or k.endswith('density') else 1e-4
+            assert np.allclose(a, b, rtol=1e-4, atol=atol), (engine, k, np.abs(a - b).max())
+        assert np.abs(st['N'].cpu().numpy() - st_o['N']).max() == 0
