@@ -171,6 +171,39 @@ LGX_API int lgx_update(const lgx_plan* plan, int n, const float* state, const fl
  * least `blocks` floats (written only if an impossible value appears). */
 LGX_API long long lgx_fp32_probe(float* sink, int blocks, int iters, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Allocation-free rollout.  No counterpart in the reference: leniax runs on
+ * JAX, which owns all device buffers.
+ *
+ * lgx_run_noalloc is lgx_run for resident models (2D, C=1, K=1, square worlds
+ * of 32, 64 or 128) for callers that cannot allocate device memory when they
+ * call the engine -- typically a host runtime that reserves nearly all GPU
+ * memory for its own pool at start-up (a JAX/XLA process calling this engine
+ * from a custom call, say), where a cudaMalloc fails or competes with that
+ * pool, or a latency-sensitive caller that must not pay for the implicit
+ * synchronisation of cudaMalloc/cudaFree.  The caller passes inputs and
+ * outputs only (job->main_events and job->engine are ignored).
+ *
+ * The engine's scratch is a fixed device array of LGX_NOALLOC_SCRATCH_BYTES
+ * that every GPU loading this library holds until the process exits.  The
+ * first call on a device resolves the array's device address with that device
+ * current; make that first call before any stream capture.  The call itself
+ * performs no allocation.  All calls on a device share the one array: calls
+ * whose GPU work overlaps (other streams, other host threads) race on it and
+ * must be serialised by the caller.  Batches needing more scratch than the
+ * array holds (lgx_noalloc_scratch_bytes) are rejected with LGX_ERR_WORKSPACE;
+ * messages are read with lgx_noalloc_last_error(). */
+#define LGX_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+
+/* Scratch bytes a batch needs (0 for an invalid request). */
+LGX_API size_t lgx_noalloc_scratch_bytes(const lgx_plan* plan, int n_sols, int n_init, int steps);
+
+/* lgx_run without a workspace: see above. */
+LGX_API int lgx_run_noalloc(const lgx_plan* plan, const lgx_rollout* job, void* stream);
+
+/* Message of the calling thread's last lgx_run_noalloc error ("" if none). */
+LGX_API const char* lgx_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

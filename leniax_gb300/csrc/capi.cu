@@ -395,3 +395,8 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
 }
 
 }  // extern "C"
+
+// Read-only view of a plan's model for other translation units of the engine.
+namespace lgx {
+const Model* plan_model(const lgx_plan* plan) { return plan ? &plan->m : nullptr; }
+}  // namespace lgx

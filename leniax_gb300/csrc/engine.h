@@ -25,6 +25,9 @@ struct Model {
   long cells;   // D*H*W
 };
 
+// The model a plan was built from (capi.cu).
+const Model* plan_model(const lgx_plan* plan);
+
 // ---------------------------------------------------------------- resident
 // Prepared spectrum pitch (float2) of the resident engine for an N x N world.
 inline int resident_kpitch(int N) { return N / 2 + 2; }
