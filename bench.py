@@ -317,6 +317,25 @@ def run_ours(args, rank, world_size):
     return out
 
 
+def profile_case(args):
+    """One warm-up plus one timed rollout of a reduced batch (same per-step work
+    per world and launch shape as the benchmark), for ncu captures."""
+    import torch
+    from leniax_gb300 import helpers, kernels, runner, statistics
+    dev = torch.device('cuda', 0)
+    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, dev)
+    upd = helpers.build_update_fn(K.shape, mp)
+    stats_fn = statistics.ComputeStatsFn([SIZE, SIZE], R, T_RATE)
+    cells = torch.from_numpy(make_inputs(args.profile_worlds, seed=1)).to(dev)
+    gf, w, Tt = mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([T_RATE])
+    for _ in range(2):
+        sd, fin = runner.run_scan_mem_optimized(None, cells, K[None], gf, w, Tt, args.profile_steps, R, upd, stats_fn,
+                                                with_box=True, with_centroid=True)
+    torch.cuda.synchronize()
+    print(json.dumps({'profile_case': f'{args.profile_worlds} worlds x {args.profile_steps} steps',
+                      'mean_N_box': float(sd['N_box'].mean())}))
+
+
 def run_reference(args):
     """Reference arm: the reference's CPU algorithm for this path (leniax's JAX
     is not installable here, so its numpy restatement), all host threads."""
@@ -337,7 +356,15 @@ def main():
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--profile-case', action='store_true',
+                    help='profiling case for ncu: one warm-up and one rollout of --profile-worlds worlds x '
+                         '--profile-steps Euler steps, nothing else')
+    ap.add_argument('--profile-worlds', type=int, default=2048)
+    ap.add_argument('--profile-steps', type=int, default=16)
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     world_size = int(os.environ.get('WORLD_SIZE', '1'))
     rank = int(os.environ.get('RANK', '0'))
     if args.impl == 'reference':

@@ -39,8 +39,13 @@ __device__ __forceinline__ void sfor(F&& f) {
   sfor_impl(f, std::make_integer_sequence<int, N>{});
 }
 
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add/sub on Blackwell's packed FP32x2 pipe (one instruction per
+// complex value; a - b is fma(b, -1, a), exact to one rounding like a - b).
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+// a + conj(b) and a - conj(b)
+__device__ __forceinline__ float2 caddc(float2 a, float2 b) { return __ffma2_rn(b, make_float2(1.f, -1.f), a); }
+__device__ __forceinline__ float2 csubc(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, 1.f), a); }
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
