@@ -164,6 +164,55 @@ LGX_API int lgx_update(const lgx_plan* plan, int n, const float* state, const fl
                const float* weights, const float* dt, int dt_per_world, float* state_out, float* field_out,
                float* potential_out, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Differentiation.  leniax differentiates its rollout with jax.grad through
+ * the FFT (runner.py:363-448, make_pipeline_fn / make_gradient_fn); this
+ * engine provides the adjoint by hand.  Models: 2D, C = 1, K = 1, square
+ * worlds of 32..256.  The caller checkpoints states with lgx_run, recomputes
+ * each segment's states s_t and potentials u_t (lgx_run trajectories), and
+ * walks the segments backwards with lgx_adjoint. */
+#define LGX_CLIP_GRAD_STE 0  /* clip gradient = 1 (leniax get_state v1, core.py:267-270) */
+#define LGX_CLIP_GRAD_MASK 1 /* clip gradient = 1 where 0 < s + dt f < 1, else 0 */
+
+typedef struct lgx_adjoint_job {
+  int n_sols, n_init, steps;    /* batch as in lgx_rollout; steps of this segment */
+  const float* k_half;          /* [Ns, 1, 1, H, W/2+1] complex64 kernel spectra       */
+  const float* gf_params;       /* [Ns, 1, 2]                                         */
+  const float* weights;         /* [Ns, 1, 1]                                         */
+  const float* T;               /* [Ns]   dt = 1/T                                    */
+  const float* traj_cells;      /* [steps, Ns*Ni, 1, H, W] states entering each step  */
+  const float* traj_potential;  /* [steps, Ns*Ni, 1, H, W] potentials of each step    */
+  const float* lambda_in;       /* [Ns*Ni, 1, H, W] dL/d(state after the segment)     */
+  float* lambda_out;            /* [Ns*Ni, 1, H, W] dL/d(state before the segment); must
+                                   not alias lambda_in                                 */
+  float* kernel_grad_acc;       /* [Ns*Ni, H/2, W] complex64 accumulator, zeroed by the
+                                   caller before the first (last-in-time) segment     */
+  float* grad_gf;               /* [Ns, 1, 2] dL/d(m, s), accumulated (+=)            */
+  float* grad_weights;          /* [Ns, 1, 1] dL/dw, accumulated (+=)                 */
+  int clip_grad;                /* LGX_CLIP_GRAD_*                                    */
+} lgx_adjoint_job;
+
+/* Workspace bytes of lgx_adjoint for a batch. */
+LGX_API size_t lgx_adjoint_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init);
+
+/* Reverse one segment of a rollout (see above). */
+LGX_API int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* job, void* workspace, size_t workspace_bytes,
+                        void* stream);
+
+/* dL/d(real kernel) [Ns, H, W] from the accumulator after the last segment:
+ * the gradient with respect to the world-sized, fftshifted real kernel whose
+ * fftn is the spectrum (kernels.py:145-149); chain it to ring weights b etc.
+ * on the caller side.  Workspace: lgx_adjoint_workspace_bytes. */
+LGX_API int lgx_adjoint_kernel_grad(const lgx_plan* plan, int n_sols, int n_init, const float* kernel_grad_acc,
+                                    float* grad_kernel, void* workspace, size_t workspace_bytes, void* stream);
+
+/* leniax's kernel spectrum on the device: fftn of `planes` real H x W planes
+ * (world-sized, fftshifted kernels, kernels.py:145-149) written as Hermitian
+ * halves [planes, H, W/2+1] complex64.  Square worlds of 32..256.  Workspace:
+ * planes * H * W * 4 bytes. */
+LGX_API int lgx_kernel_spectrum(int H, int W, int planes, const float* k_real, float* k_half, void* workspace,
+                                size_t workspace_bytes, void* stream);
+
 /* Measurement helper (no counterpart in the reference): launch a pure-FMA
  * kernel of `blocks` x 256 threads and return the number of FP32 flops it
  * performs (or -1).  Timing it with events gives the FP32-pipe peak used as

@@ -400,3 +400,111 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
 namespace lgx {
 const Model* plan_model(const lgx_plan* plan) { return plan ? &plan->m : nullptr; }
 }  // namespace lgx
+
+// ------------------------------------------------------------------ adjoint
+namespace {
+
+size_t adjoint_ws(const Model& m, int n_sols, int n_init) {
+  const size_t nw = (size_t)n_sols * n_init, cells = (size_t)m.H * m.W;
+  size_t b = 0;
+  b += al256((size_t)n_sols * m.H * (m.W / 2 + 2) * sizeof(float2));  // kp
+  b += 2 * al256(nw * cells * sizeof(float));                         // lam_a, lam_b
+  b += al256(nw * 2 * cells * sizeof(float));                         // as planes
+  b += al256(nw * cells * sizeof(float2));                            // spec (2 planes x N/2 x N)
+  b += al256(nw * cells / 2 * sizeof(float2));                        // prod
+  b += al256(nw * 64 * 3 * sizeof(float));                            // partial
+  return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t lgx_adjoint_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init) {
+  if (!plan || n_sols < 1 || n_init < 1 || !adjoint_supported(plan->m)) return 0;
+  return adjoint_ws(plan->m, n_sols, n_init);
+}
+
+int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t ws_bytes, void* stream) {
+  if (!plan || !j) return fail(LGX_ERR_INVALID, "lgx_adjoint: null plan or job");
+  const Model& m = plan->m;
+  if (!adjoint_supported(m))
+    return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint: 2D, C=1, K=1, square 32..256 worlds only");
+  if (j->n_sols < 1 || j->n_init < 1 || j->steps < 1) return fail(LGX_ERR_INVALID, "lgx_adjoint: bad batch");
+  if (!j->k_half || !j->gf_params || !j->weights || !j->T || !j->traj_cells || !j->traj_potential ||
+      !j->lambda_in || !j->lambda_out || !j->kernel_grad_acc || !j->grad_gf || !j->grad_weights)
+    return fail(LGX_ERR_INVALID, "lgx_adjoint: null tensor");
+  if (j->lambda_in == j->lambda_out) return fail(LGX_ERR_INVALID, "lgx_adjoint: lambda_out aliases lambda_in");
+  if (j->clip_grad != LGX_CLIP_GRAD_STE && j->clip_grad != LGX_CLIP_GRAD_MASK)
+    return fail(LGX_ERR_INVALID, "lgx_adjoint: unknown clip_grad %d", j->clip_grad);
+  const size_t need = adjoint_ws(m, j->n_sols, j->n_init);
+  if (!ws || ws_bytes < need) return fail(LGX_ERR_WORKSPACE, "lgx_adjoint: workspace %zu < %zu bytes", ws_bytes, need);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t nw = (size_t)j->n_sols * j->n_init, cells = (size_t)m.H * m.W;
+  Carve cv(ws, ws_bytes);
+  AdjointSegment a;
+  std::memset(&a, 0, sizeof(a));
+  float2* kp = cv.take<float2>((size_t)j->n_sols * m.H * (m.W / 2 + 2));
+  a.lam_a = cv.take<float>(nw * cells);
+  a.lam_b = cv.take<float>(nw * cells);
+  a.as_planes = cv.take<float>(nw * 2 * cells);
+  a.spec = cv.take<float2>(nw * cells);
+  a.prod = cv.take<float2>(nw * cells / 2);
+  a.partial = cv.take<float>(nw * 64 * 3);
+  cudaError_t ce = launch_prepare_streamed_spectrum(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
+  if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+  a.n_sols = j->n_sols;
+  a.n_init = j->n_init;
+  a.steps = j->steps;
+  a.gf_id = m.gf[0];
+  a.state_fn = m.state_fn;
+  a.mean = m.mean;
+  a.clip_mask = j->clip_grad == LGX_CLIP_GRAD_MASK;
+  a.gf_params = j->gf_params;
+  a.weights = j->weights;
+  a.T = j->T;
+  a.kp = kp;
+  a.traj_cells = j->traj_cells;
+  a.traj_potential = j->traj_potential;
+  a.lambda_in = j->lambda_in;
+  a.lambda_out = j->lambda_out;
+  a.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
+  a.grad_gf = j->grad_gf;
+  a.grad_w = j->grad_weights;
+  ce = launch_adjoint_segment(m.H, a, st);
+  if (ce != cudaSuccess) return cuda_fail(ce, "adjoint segment");
+  g_err.clear();
+  return LGX_OK;
+}
+
+int lgx_adjoint_kernel_grad(const lgx_plan* plan, int n_sols, int n_init, const float* acc, float* grad_kernel,
+                            void* ws, size_t ws_bytes, void* stream) {
+  if (!plan || !acc || !grad_kernel) return fail(LGX_ERR_INVALID, "lgx_adjoint_kernel_grad: null argument");
+  const Model& m = plan->m;
+  if (!adjoint_supported(m)) return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint_kernel_grad: unsupported model");
+  if (n_sols < 1 || n_init < 1) return fail(LGX_ERR_INVALID, "lgx_adjoint_kernel_grad: bad batch");
+  const size_t need = adjoint_ws(m, n_sols, n_init);
+  if (!ws || ws_bytes < need)
+    return fail(LGX_ERR_WORKSPACE, "lgx_adjoint_kernel_grad: workspace %zu < %zu bytes", ws_bytes, need);
+  float2* prod = reinterpret_cast<float2*>(ws);
+  cudaError_t ce = launch_gk_finish(m.H, n_sols, n_init, reinterpret_cast<const float2*>(acc), prod, grad_kernel,
+                                    static_cast<cudaStream_t>(stream));
+  if (ce != cudaSuccess) return cuda_fail(ce, "kernel gradient");
+  g_err.clear();
+  return LGX_OK;
+}
+
+int lgx_kernel_spectrum(int H, int W, int planes, const float* k_real, float* k_half, void* ws, size_t ws_bytes,
+                        void* stream) {
+  if (!k_real || !k_half || planes < 1) return fail(LGX_ERR_INVALID, "lgx_kernel_spectrum: bad argument");
+  if (!spectrum_supported(H, W)) return fail(LGX_ERR_UNSUPPORTED, "lgx_kernel_spectrum: square 32..256 only");
+  const size_t need = (size_t)planes * H * W * sizeof(float);
+  if (!ws || ws_bytes < need) return fail(LGX_ERR_WORKSPACE, "lgx_kernel_spectrum: workspace %zu < %zu", ws_bytes, need);
+  cudaError_t ce = launch_spectrum(H, planes, k_real, reinterpret_cast<float2*>(ws), reinterpret_cast<float2*>(k_half),
+                                   static_cast<cudaStream_t>(stream));
+  if (ce != cudaSuccess) return cuda_fail(ce, "kernel spectrum");
+  g_err.clear();
+  return LGX_OK;
+}
+
+}  // extern "C"

@@ -89,6 +89,34 @@ cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st);
 cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,
                                              cudaStream_t st);
 
+// ---------------------------------------------------------------- adjoint
+struct AdjointSegment {
+  int n_sols, n_init, steps;
+  int gf_id, state_fn, mean, clip_mask;
+  const float* gf_params;       // [Ns, 2]
+  const float* weights;         // [Ns]
+  const float* T;               // [Ns]
+  const float2* kp;             // prepared spectra [Ns, N, N/2+2]
+  const float* traj_cells;      // [steps, nw, N, N]
+  const float* traj_potential;  // [steps, nw, N, N]
+  const float* lambda_in;       // [nw, N, N]
+  float* lambda_out;            // [nw, N, N]
+  float *lam_a, *lam_b;         // [nw, N, N] ping-pong
+  float* as_planes;             // [nw, 2, N, N]
+  float2* spec;                 // [nw, 2, N/2, N]
+  float2* prod;                 // [nw, N/2, N]
+  float* partial;               // [nw, 64, 3]
+  float2* gk;                   // [nw, N/2, N] kernel-gradient accumulator (column domain)
+  float* grad_gf;               // [Ns, 2]   +=
+  float* grad_w;                // [Ns]      +=
+};
+bool adjoint_supported(const Model& m);
+bool spectrum_supported(int H, int W);
+cudaError_t launch_adjoint_segment(int N, const AdjointSegment& j, cudaStream_t st);
+cudaError_t launch_gk_finish(int N, int n_sols, int n_init, const float2* gk, float2* prod, float* out,
+                             cudaStream_t st);
+cudaError_t launch_spectrum(int N, int planes, const float* k_real, float2* spec, float2* out, cudaStream_t st);
+
 // ---------------------------------------------------------------- stats
 // Turn raw moments [Ns, steps, Ni, RAWS] into leniax stats / N / N_box.
 struct StatsArgs {

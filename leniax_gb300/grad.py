@@ -1,0 +1,218 @@
+"""Differentiable Lenia rollouts on the GB300 engine.
+
+leniax differentiates a rollout with ``jax.value_and_grad`` through the FFT
+(``runner.py:363-448``: ``make_pipeline_fn`` / ``make_gradient_fn``; the v1
+clip's gradient is the straight-through estimator, ``core.py:267-270``).
+Here the reverse pass is the engine's hand-written adjoint (``lgx_adjoint``)
+behind a ``torch.autograd.Function``:
+
+* forward: ``steps`` Euler steps, keeping the state every ``checkpoint_every``
+  steps in HBM;
+* backward: for each segment, newest first, recompute its states and
+  potentials from the checkpoint, then run the adjoint steps (conjugate-
+  spectrum correlation, growth derivative, clip gradient ``'ste'`` or
+  ``'mask'``).
+
+Gradients flow to the initial cells, the world-sized fftshifted real kernel
+(and through :func:`ring_kernel` to the ring weights ``b``), the growth
+parameters ``(m, s)`` and the kernel weights.  Models: 2D, one channel, one
+kernel, square worlds of 32..256.
+"""
+import ctypes
+import math
+from typing import Sequence
+
+import torch
+
+from . import _lib
+from .core import UpdateFn, _require_cuda, _stream_handle, workspace
+
+CLIP_GRAD = {'ste': 0, 'mask': 1}
+
+
+def _bind(lib):
+    if getattr(lib, '_lgx_grad_bound', False):
+        return lib
+    lib.lgx_adjoint_workspace_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.lgx_adjoint_workspace_bytes.restype = ctypes.c_size_t
+    lib.lgx_adjoint.argtypes = [ctypes.c_void_p, ctypes.POINTER(AdjointJob), ctypes.c_void_p, ctypes.c_size_t,
+                                ctypes.c_void_p]
+    lib.lgx_adjoint.restype = ctypes.c_int
+    lib.lgx_adjoint_kernel_grad.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.lgx_adjoint_kernel_grad.restype = ctypes.c_int
+    lib.lgx_kernel_spectrum.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.lgx_kernel_spectrum.restype = ctypes.c_int
+    lib._lgx_grad_bound = True
+    return lib
+
+
+class AdjointJob(ctypes.Structure):
+    _fp = ctypes.c_void_p
+    _fields_ = [
+        ('n_sols', ctypes.c_int), ('n_init', ctypes.c_int), ('steps', ctypes.c_int), ('k_half', _fp),
+        ('gf_params', _fp), ('weights', _fp), ('T', _fp), ('traj_cells', _fp), ('traj_potential', _fp),
+        ('lambda_in', _fp), ('lambda_out', _fp), ('kernel_grad_acc', _fp), ('grad_gf', _fp), ('grad_weights', _fp),
+        ('clip_grad', ctypes.c_int)
+    ]
+
+
+def kernel_spectrum(k_real: torch.Tensor) -> torch.Tensor:
+    """fftn of world-sized fftshifted real kernels ``[..., H, W]`` on the
+    device (leniax ``kernels.py:145-149``) -> Hermitian halves
+    ``[..., H, W//2+1]`` complex64."""
+    _require_cuda('k_real', k_real)
+    H, W = k_real.shape[-2:]
+    lead = k_real.shape[:-2]
+    planes = int(math.prod(lead)) if lead else 1
+    kr = k_real.contiguous()
+    out = torch.empty(lead + (H, W // 2 + 1), dtype=torch.complex64, device=k_real.device)
+    lib = _bind(_lib.load())
+    ws = workspace(planes * H * W * 4, k_real.device)
+    _lib.check(lib.lgx_kernel_spectrum(H, W, planes, kr.data_ptr(), out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                       _stream_handle(k_real.device)))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# differentiable kernel construction (kernels.py:176-212 with kernel_functions)
+def _kf_torch(slug, q, X):
+    if slug == 'gauss_bump':  # kernel_functions.py:40-69
+        return torch.exp(q * (q - 1 / (X * (1 - X) + 1e-7)))
+    if slug == 'poly_quad':  # kernel_functions.py:7-37
+        return (4 * X * (1 - X))**q
+    if slug == 'gauss':  # kernel_functions.py:105-134
+        return torch.exp(-(((X - q) / (0.3 * q))**2) / 2)
+    raise NotImplementedError(f'kernel function {slug!r} has no differentiable form here')
+
+
+def ring_kernel(R: float, r: float, b: torch.Tensor, kf_slug: str, kf_params: Sequence[float],
+                world: Sequence[int]) -> torch.Tensor:
+    """World-sized, fftshifted ring kernel (what leniax FFTs), differentiable
+    in the ring weights ``b`` (1-D tensor).  Mirrors ``circle_2d``
+    (kernels.py:176-212), the centring pad (kernels.py:93-101) and the
+    fftshift (kernels.py:148)."""
+    dev, dt = b.device, torch.float32
+    k = math.ceil(r * R)
+    idx = torch.arange(2 * k, device=dev, dtype=dt) - k
+    yy, xx = torch.meshgrid(idx, idx, indexing='ij')
+    dist = torch.sqrt((yy / (r * R))**2 + (xx / (r * R))**2)
+    nb = b.shape[0]
+    bdist = nb * dist
+    ring = torch.clamp(torch.floor(bdist).long(), max=nb - 1)
+    raw = _kf_torch(kf_slug, float(kf_params[0]), torch.remainder(bdist, 1.0))
+    kern = (dist < 1).to(dt) * raw * b[ring]
+    kern = kern / kern.sum()
+    H, W = world
+    ph, pw = (H - 2 * k) // 2, (W - 2 * k) // 2
+    full = torch.nn.functional.pad(kern, (pw, W - 2 * k - pw, ph, H - 2 * k - ph))
+    # fftshift of an even-sized world: index H/2 (the kernel centre) moves to 0
+    return torch.roll(full, shifts=(-(H // 2), -(W // 2)), dims=(0, 1))
+
+
+# ---------------------------------------------------------------------------
+class LeniaRolloutFunction(torch.autograd.Function):
+    """``final = LeniaRolloutFunction.apply(cells0, k_real, gf_params, weights,
+    T, update_fn, steps, checkpoint_every, clip_grad)``
+
+    cells0 ``[Ns, Ni, 1, H, W]``; k_real ``[Ns, H, W]`` world-sized fftshifted
+    kernels; gf_params ``[Ns, 1, 2]``; weights ``[Ns, 1, 1]``; T ``[Ns]``.
+    Returns the state after ``steps`` steps ``[Ns, Ni, 1, H, W]``.
+    """
+
+    @staticmethod
+    def forward(ctx, cells0, k_real, gf_params, weights, T, update_fn: UpdateFn, steps: int, checkpoint_every: int,
+                clip_grad: str):
+        m = update_fn.model
+        dev = cells0.device
+        Ns, Ni = cells0.shape[:2]
+        k_half = kernel_spectrum(k_real.detach().float()).reshape(Ns, 1, 1, m.world[0], m.world[1] // 2 + 1)
+        gf = gf_params.detach().float().reshape(Ns, 1, 2).contiguous()
+        w = weights.detach().float().reshape(Ns, 1, 1).contiguous()
+        Tt = torch.as_tensor(T, dtype=torch.float32, device=dev).reshape(-1).expand(Ns).contiguous()
+        k = max(1, int(checkpoint_every))
+        ckpts = [cells0.detach().contiguous()]
+        cur = ckpts[0]
+        done = 0
+        while done < steps:
+            n = min(k, steps - done)
+            cur = _segment(update_fn, cur, k_half, gf, w, Tt, n, traj=False)
+            done += n
+            if done < steps:
+                ckpts.append(cur)
+        ctx.save_for_backward(k_half, gf, w, Tt, *ckpts)
+        ctx.update_fn, ctx.steps, ctx.k, ctx.clip = update_fn, steps, k, CLIP_GRAD[clip_grad]
+        return cur
+
+    @staticmethod
+    def backward(ctx, grad_final):
+        k_half, gf, w, Tt, *ckpts = ctx.saved_tensors
+        update_fn, steps, k = ctx.update_fn, ctx.steps, ctx.k
+        m = update_fn.model
+        dev = grad_final.device
+        Ns, Ni = ckpts[0].shape[:2]
+        H, W = m.world
+        lib = _bind(_lib.load())
+        nw = Ns * Ni
+        lam = grad_final.detach().float().contiguous().clone()
+        lam_out = torch.empty_like(lam)
+        acc = torch.zeros((nw, H // 2, W), dtype=torch.complex64, device=dev)
+        g_gf = torch.zeros((Ns, 1, 2), dtype=torch.float32, device=dev)
+        g_w = torch.zeros((Ns, 1, 1), dtype=torch.float32, device=dev)
+        ws = workspace(lib.lgx_adjoint_workspace_bytes(update_fn.model.plan.handle, Ns, Ni), dev)
+        seg_starts = list(range(0, steps, k))
+        for j in reversed(range(len(seg_starts))):
+            n = min(k, steps - seg_starts[j])
+            tc, tp = _segment(update_fn, ckpts[j], k_half, gf, w, Tt, n, traj=True)
+            job = AdjointJob()
+            job.n_sols, job.n_init, job.steps = Ns, Ni, n
+            job.k_half, job.gf_params, job.weights, job.T = (k_half.data_ptr(), gf.data_ptr(), w.data_ptr(),
+                                                             Tt.data_ptr())
+            job.traj_cells, job.traj_potential = tc.data_ptr(), tp.data_ptr()
+            job.lambda_in, job.lambda_out = lam.data_ptr(), lam_out.data_ptr()
+            job.kernel_grad_acc = acc.data_ptr()
+            job.grad_gf, job.grad_weights = g_gf.data_ptr(), g_w.data_ptr()
+            job.clip_grad = ctx.clip
+            _lib.check(lib.lgx_adjoint(update_fn.model.plan.handle, job, ws.data_ptr(), ws.numel(),
+                                       _stream_handle(dev)))
+            lam, lam_out = lam_out, lam
+        g_k = torch.empty((Ns, H, W), dtype=torch.float32, device=dev)
+        _lib.check(lib.lgx_adjoint_kernel_grad(update_fn.model.plan.handle, Ns, Ni, acc.data_ptr(), g_k.data_ptr(),
+                                               ws.data_ptr(), ws.numel(), _stream_handle(dev)))
+        return lam, g_k, g_gf, g_w, None, None, None, None, None
+
+
+def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj):
+    """n Euler steps from `cells` through lgx_run (no statistics needed)."""
+    m = update_fn.model
+    dev = cells.device
+    Ns, Ni = cells.shape[:2]
+    lib = _lib.load()
+    final = torch.empty_like(cells)
+    job = _lib.Rollout()
+    job.n_sols, job.n_init, job.steps = Ns, Ni, n
+    kh = torch.view_as_real(k_half.contiguous())
+    job.cells0, job.k_half, job.gf_params, job.weights, job.T = (cells.data_ptr(), kh.data_ptr(), gf.data_ptr(),
+                                                                  w.data_ptr(), Tt.data_ptr())
+    job.stats_R, job.stats_T = 1.0, 1.0
+    job.final_cells = final.data_ptr()
+    tc = tp = None
+    if traj:
+        tc = torch.empty((n, Ns * Ni, 1) + m.world, dtype=torch.float32, device=dev)
+        tp = torch.empty_like(tc)
+        job.traj_cells, job.traj_potential = tc.data_ptr(), tp.data_ptr()
+    eng = _lib.ENGINES['auto']
+    ws = workspace(lib.lgx_run_workspace_bytes(m.plan.handle, Ns, Ni, n, eng), dev)
+    job.engine = eng
+    _lib.check(lib.lgx_run(m.plan.handle, job, ws.data_ptr(), ws.numel(), _stream_handle(dev)))
+    return (tc, tp) if traj else final
+
+
+def rollout(cells0, k_real, gf_params, weights, T, update_fn: UpdateFn, steps: int, checkpoint_every: int = 16,
+            clip_grad: str = 'ste'):
+    """Differentiable rollout (see :class:`LeniaRolloutFunction`)."""
+    if clip_grad not in CLIP_GRAD:
+        raise ValueError("clip_grad must be 'ste' or 'mask'")
+    return LeniaRolloutFunction.apply(cells0, k_real, gf_params, weights, T, update_fn, steps, checkpoint_every,
+                                      clip_grad)
