@@ -277,6 +277,8 @@ def run_ours(args, rank, world_size):
     torch.cuda.synchronize()
     plain_value = PLAIN_SAMPLE_WORLDS * P_CELLS * PLAIN_SAMPLE_STEPS / (p0.elapsed_time(p1) / 1e3)
 
+    adjoint = measure_adjoint(dev)
+
     gpu_launches = args.steps * 4  # prepare spectrum, resident kernel, stats, heuristics per rollout
     out = {
         'metric': METRIC,
@@ -310,11 +312,60 @@ def run_ours(args, rank, world_size):
             'sample': f'{PLAIN_SAMPLE_WORLDS} worlds x {PLAIN_SAMPLE_STEPS} steps, one world and one step per launch',
             'speedup_batched_vs_plain': value / world_size / plain_value
         },
+        'adjoint': adjoint,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
         'hbm_peak_gbs_measured': measured_peaks().get('hbm_gbs'),
     }
     return out
+
+
+def measure_adjoint(dev, worlds=64, steps=256, ckpt=16, reps=3):
+    """Differentiation workload: 64 worlds of 128x128 (the single-world model),
+    256 steps with checkpoints every 16, MSE of the final state against a
+    target made by the forward engine from the same inits at m=0.16, s=0.017;
+    gradients with respect to the initial cells, m, s and the ring weights b
+    (two rings, so dL/db is not identically zero).  Reports fwd+bwd
+    world-steps/s timed with CUDA events around forward + backward."""
+    import torch
+    from leniax_gb300 import grad as lgrad
+    from leniax_gb300 import helpers, kernels
+    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, dev)
+    upd = helpers.build_update_fn(K.shape, mp)
+    cells = torch.from_numpy(make_inputs(worlds, seed=4)).to(dev)
+    T = torch.tensor([T_RATE])
+    b_t = torch.tensor([1.0, 1.0], device=dev)
+    with torch.no_grad():
+        kt = lgrad.ring_kernel(R, 1.0, b_t, 'gauss_bump', [1.0], [SIZE, SIZE])[None]
+        target = lgrad.rollout(cells, kt, torch.tensor([[[0.16, 0.017]]], device=dev), torch.ones((1, 1, 1),
+                                                                                                  device=dev), T,
+                               upd, steps, ckpt)
+    times = []
+    for i in range(reps + 1):
+        c0 = cells.clone().requires_grad_(True)
+        b = torch.tensor([0.9, 1.0], device=dev, requires_grad=True)
+        gf = torch.tensor([[[0.15, 0.015]]], device=dev, requires_grad=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        kr = lgrad.ring_kernel(R, 1.0, b, 'gauss_bump', [1.0], [SIZE, SIZE])[None]
+        fin = lgrad.rollout(c0, kr, gf, torch.ones((1, 1, 1), device=dev), T, upd, steps, ckpt)
+        loss = ((fin - target)**2).mean()
+        loss.backward()
+        e1.record()
+        torch.cuda.synchronize()
+        if i > 0:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    t = pystats.median(times)
+    return {
+        'metric': 'fwd+bwd world-steps/s', 'value': worlds * steps / t, 'unit': 'world-steps/s',
+        'cell_updates_per_s': worlds * steps * P_CELLS / t, 'seconds': t,
+        'config': f'{worlds} worlds x 128x128, {steps} steps, checkpoint every {ckpt}, grads wrt cells0, m, s, b',
+        'loss': float(loss.detach()), 'grad_norms': {
+            'cells0': float(c0.grad.norm()), 'm': float(gf.grad[0, 0, 0]), 's': float(gf.grad[0, 0, 1]),
+            'b': [float(x) for x in b.grad]
+        }
+    }
 
 
 def profile_case(args):
