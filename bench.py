@@ -361,9 +361,14 @@ def measure_adjoint(dev, worlds=64, steps=256, ckpt=16, reps=3):
         'metric': 'fwd+bwd world-steps/s', 'value': worlds * steps / t, 'unit': 'world-steps/s',
         'cell_updates_per_s': worlds * steps * P_CELLS / t, 'seconds': t,
         'config': f'{worlds} worlds x 128x128, {steps} steps, checkpoint every {ckpt}, grads wrt cells0, m, s, b',
-        'loss': float(loss.detach()), 'grad_norms': {
-            'cells0': float(c0.grad.norm()), 'm': float(gf.grad[0, 0, 0]), 's': float(gf.grad[0, 0, 1]),
-            'b': [float(x) for x in b.grad]
+        'loss': float(loss.detach()),
+        # 256 steps of noise worlds are chaotic: the straight-through gradients of
+        # leniax's v1 clip grow without bound over the horizon, so only their
+        # finiteness is reported (gradient accuracy is checked at short horizons
+        # in tests/test_gpu_adjoint.py)
+        'grads_finite': {
+            'cells0': bool(torch.isfinite(c0.grad).all()), 'm_s': bool(torch.isfinite(gf.grad).all()),
+            'b': bool(torch.isfinite(b.grad).all())
         }
     }
 
