@@ -253,6 +253,68 @@ LGX_API int lgx_run_noalloc(const lgx_plan* plan, const lgx_rollout* job, void* 
 /* Message of the calling thread's last lgx_run_noalloc error ("" if none). */
 LGX_API const char* lgx_noalloc_last_error(void);
 
+/* ---------------------------------------------------------------------------
+ * Uneven batch: thousands of worlds of different sizes, dimensions, kernels,
+ * growth parameters and time steps in ONE persistent launch.  Replaces
+ * leniax's vmap over identically shaped worlds (leniax/runner.py:167-215,
+ * run_scan_mem_optimized) when a search mixes world shapes.
+ *
+ * Worlds are grouped in classes of one shape.  Every world carries its own
+ * kernel spectrum, growth parameters (m, s), kernel weight and T, and is
+ * updated as core.update with one kernel on one channel (C = K = 1).
+ * Supported shapes: 2D 32^2, 64^2, 128^2, 256^2; 3D 32^3, 64^3.
+ *
+ * lgx_batch_run only launches kernels and stream-ordered copies on `stream`
+ * (no host synchronisation, no allocation), so it can be captured in a CUDA
+ * graph; replays rebuild the work queue on the device.
+ * ------------------------------------------------------------------------- */
+#define LGX_BATCH_MAX_CLASSES 8
+
+/* Queue order of the work items. */
+#define LGX_ORDER_LARGEST_FIRST 0 /* classes by estimated item cost, largest first */
+#define LGX_ORDER_AS_GIVEN 1      /* classes in the order of the classes array */
+#define LGX_ORDER_EXPLICIT 2      /* classes in the order of job->class_order */
+
+typedef struct lgx_batch_class {
+  int nb_dims;   /* 2 or 3 */
+  int size;      /* side of the (square / cubic) torus */
+  int n_worlds;  /* >= 0 */
+  int gf_id;     /* LGX_GF_* */
+  int state_fn;  /* LGX_STATE_* */
+  int mean;      /* 1: weighted_mean, 0: weighted_sum (core.py:202-242) */
+  const float* cells0;    /* [n_worlds, size^nb_dims] */
+  const float* k_half;    /* [n_worlds, size^(nb_dims-1), size/2+1] complex64: each world's
+                             kernel spectrum (kernels.py:145-152) sliced to its Hermitian half */
+  const float* gf_params; /* [n_worlds, 2]: m, s */
+  const float* weights;   /* [n_worlds]: kernel weight */
+  const float* T;         /* [n_worlds]: dt = 1 / T */
+  const float* stats_R;   /* [n_worlds]: R of compute_stats; needed when any stats output is set */
+  const float* stats_T;   /* [n_worlds]: T of compute_stats */
+  float* final_cells;     /* [n_worlds, size^nb_dims] */
+  float* stats;           /* [n_worlds, steps, 12] (compute_stats order, C = 1) or NULL */
+  float* n_continue;      /* [n_worlds]: check_heuristics N, or NULL */
+  float* n_box;           /* [n_worlds]: N with the bounding-box stop (runner.py:24-25), or NULL */
+  float* centroid;        /* [n_worlds, steps, nb_dims]: absolute torus centroid, or NULL */
+} lgx_batch_class;
+
+typedef struct lgx_batch_job {
+  int n_classes; /* 1 .. LGX_BATCH_MAX_CLASSES */
+  int steps;
+  const lgx_batch_class* classes;
+  int order;      /* LGX_ORDER_* */
+  int grid;       /* persistent CTAs; 0 = one per SM */
+  int line_group; /* lanes per 3D line transform: 2 or 4; 0 = 4 */
+  const int* class_order; /* host array [n_classes], a permutation of 0..n_classes-1
+                             (LGX_ORDER_EXPLICIT only; read during the call) */
+} lgx_batch_job;
+
+/* Workspace for lgx_batch_run (depends on the classes, steps and grid):
+ * *bytes on LGX_OK; LGX_ERR_INVALID / LGX_ERR_UNSUPPORTED for a bad job. */
+LGX_API int lgx_batch_workspace_bytes(const lgx_batch_job* job, size_t* bytes);
+/* Run every world of every class for `steps` steps.  Returns LGX_ERR_INVALID /
+ * LGX_ERR_UNSUPPORTED for a bad job without launching anything. */
+LGX_API int lgx_batch_run(const lgx_batch_job* job, void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,603 @@
+// Uneven batch engine: worlds of different sizes and dimensions, radii and
+// growth parameters in one persistent launch fed by a device work queue.
+//
+// A 512-thread CTA per SM loops: it dequeues an item with an atomic counter
+// and processes it with the code for its class:
+//   * resident classes (2D 32^2, 64^2, 128^2): resident_item() -- 8, 4 or 1
+//     worlds per CTA, states in registers, spectra in shared memory;
+//   * big 2D (256^2): one world per CTA, packed-row spectrum in a per-CTA
+//     global (L2-resident) scratch, the resident engine's FFT passes;
+//   * big 3D (32^3, 64^3): one world per CTA, half spectrum [D][H][W/2+1] in
+//     the per-CTA scratch; x, y and z passes, the spectrum multiply fused into
+//     the z pass.  Lines of the y and z passes are transformed by groups of G
+//     lanes (G = 4 or 2, chosen per batch by the autotuner).
+// The host orders the queue (largest first by default) so long worlds start
+// early.
+//
+// This replaces leniax's vmap over identically-shaped worlds
+// (runner.py:167-168, experiments/readme.md:26-35) for heterogeneous batches;
+// every world follows core.update (core.py:13-49) and compute_stats
+// (statistics.py:36-126) as in the other engines.
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+
+#include "resident.cuh"
+
+namespace lgx {
+
+namespace {
+
+// twiddle tables of every size used here, 3 tables of N entries each
+constexpr int TW32 = 0, TW64 = TW32 + 3 * 32, TW128 = TW64 + 3 * 64, TW256 = TW128 + 3 * 128,
+              TW64G2 = TW256 + 3 * 256, TW32G2 = TW64G2 + 64, TW_END = TW32G2 + 32;
+
+constexpr int kBigRed = 16 * 16 + 16;  // floats: per-warp partials + shift
+
+template <int N, int G>
+constexpr size_t big_smem() {
+  return (size_t)(512 / G) * Geo<N, G>::SCR * sizeof(float2) + kBigRed * sizeof(float);
+}
+
+constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
+constexpr size_t kWorkBytes = cmax(
+    cmax(cmax(resident_work_bytes<128, 8>(), resident_work_bytes<64, 4>()), resident_work_bytes<32, 4>()),
+    cmax(cmax(big_smem<256, 8>(), cmax(big_smem<64, 4>(), big_smem<64, 2>())), cmax(big_smem<32, 4>(), big_smem<32, 2>())));
+constexpr size_t kMixedSmem = (size_t)TW_END * sizeof(float2) + kWorkBytes;
+static_assert(kMixedSmem <= 227 * 1024, "mixed kernel shared memory");
+
+template <int GF>
+__device__ __forceinline__ GrowthP big_growth(const BigArgs& a, int world) {
+  GrowthP g;
+  g.m = __ldg(a.gf + 2 * world);
+  g.s = __ldg(a.gf + 2 * world + 1);
+  g.id = a.gf_id;
+  g.a = GF == GF_FAST_GAUSSIAN ? 0.84932180028801904272f / g.s : (GF == GF_FAST_POLY4 ? 1.f / (9.f * g.s * g.s) : 0.f);
+  return g;
+}
+
+// acc layout == raw slots 0..13: M00, G00, CNT_POT, CNT_MASS, CNT_GROW,
+// MX[3], GX[3], MX2[3] (axes outermost first).  Block reduction, record of the
+// step's raw moments by warp 0 (lane i writes raw slot i), shift update.
+__device__ __forceinline__ void big_finish_step(const BigArgs& a, int world, int step, int nd, const int (&sizes)[3],
+                                                float (&acc)[14], bool border, float* red, int* shv) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < 14; ++i) acc[i] = warp_sum(acc[i]);
+  const bool anyb = __any_sync(0xffffffffu, border);
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < 14; ++i) red[wid * 16 + i] = acc[i];
+    red[wid * 16 + 14] = anyb ? 1.f : 0.f;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    float v = 0.f;
+    if (lane < 15)
+      for (int w = 0; w < 16; ++w) v += red[w * 16 + lane];
+    const int sh0 = shv[0], sh1 = shv[1], sh2 = shv[2];
+    const float m00 = __shfl_sync(0xffffffffu, v, RAW_M00);
+    const float mx0 = __shfl_sync(0xffffffffu, v, RAW_MX + 0);
+    const float mx1 = __shfl_sync(0xffffffffu, v, RAW_MX + 1);
+    const float mx2 = __shfl_sync(0xffffffffu, v, RAW_MX + 2);
+    float* rw = a.raw + ((size_t)world * a.steps + step) * raw_stride(1);
+    if (lane < RAW_BORDER) rw[lane] = v;
+    else if (lane == RAW_BORDER) rw[lane] = v > 0.f ? 1.f : 0.f;
+    else if (lane < RAW_CM) rw[lane] = (float)(lane == RAW_SHIFT ? sh0 : (lane == RAW_SHIFT + 1 ? sh1 : sh2));
+    else if (lane == RAW_CM) rw[lane] = m00;
+    __syncwarp();
+    if (lane == 0) {
+      const float den = m00 + kEps;
+      shv[0] = pmod(sh0 + (int)(mx0 / den), sizes[0]);
+      if (nd > 1) shv[1] = pmod(sh1 + (int)(mx1 / den), sizes[1]);
+      if (nd > 2) shv[2] = pmod(sh2 + (int)(mx2 / den), sizes[2]);
+    }
+  }
+  __syncthreads();
+}
+
+// ------------------------------------------------------------------ big 2D
+template <int N, int GF>
+__device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float2* tw, float2* work) {
+  constexpr int G = 8;
+  using GE = Geo<N, G>;
+  constexpr int P = GE::P, Q = GE::Q, NG = 512 / G, KP = N / 2 + 2;
+  const float2 *tw_std = tw, *tw_colf = tw + N, *tw_rowi = tw + 2 * N;
+  const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31;
+  const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
+  float2* scr = work + grp * GE::SCR;
+  float* red = reinterpret_cast<float*>(work + NG * GE::SCR);
+  int* shv = reinterpret_cast<int*>(red + 16 * 16);
+  float2* spec = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;  // [N/2][N]
+  const float2* kp = a.kp + (size_t)world * N * KP;
+  const float* c0 = a.cells0 + (size_t)world * N * N;
+  float* st = a.state + (size_t)world * N * N;
+  const GrowthP gq = big_growth<GF>(a, world);
+  const float wk = __ldg(a.w + world), wf = a.mean ? wk / wk : wk;
+  const float dt = 1.f / __ldg(a.T + world);
+  const int sizes[3] = {N, N, 1};
+  if (threadIdx.x == 0) shv[0] = shv[1] = shv[2] = 0;
+  __syncthreads();
+  for (int step = 0; step < a.steps; ++step) {
+    const float* src = step == 0 ? c0 : st;
+    for (int r = grp; r < N / 2; r += NG) {  // row pass
+      float2 v[P];
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) v[n2] = make_float2(src[(2 * r) * N + t + G * n2], src[(2 * r + 1) * N + t + G * n2]);
+      float2 u[Q][G];
+      fft_standard<GE, false, false>(v, u, scr, tw_std, t, gmask);
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) spec[r * N + t + G * q + P * k1] = u[q][k1];
+    }
+    __syncthreads();
+    for (int c = grp; c < N / 2; c += NG) {  // column pass
+      float2 v[Q][G];
+#pragma unroll
+      for (int jp = 0; jp < Q / 2; ++jp) {
+        const int m = t + G * jp;
+#pragma unroll
+        for (int n2 = 0; n2 < G; ++n2) {
+          const int r = m + (P / 2) * n2;
+          if (c != 0) {
+            const float2 z1 = spec[r * N + c], z2 = spec[r * N + N - c];
+            v[2 * jp][n2] = caddc(z1, z2);
+            const float2 d = csubc(z1, z2);
+            v[2 * jp + 1][n2] = make_float2(d.y, -d.x);
+          } else {
+            const float2 z1 = spec[r * N], z2 = spec[r * N + N / 2];
+            v[2 * jp][n2] = make_float2(z1.x, z2.x);
+            v[2 * jp + 1][n2] = make_float2(z1.y, z2.y);
+          }
+        }
+      }
+      float2 w[P];
+      fft_mirrored<GE, false, false>(v, w, scr, tw_colf, t, gmask);
+      if (c != 0) {
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) w[k1] = cmul(w[k1], __ldg(kp + (t + G * k1) * KP + c));
+      } else {
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) scr[t + G * k1] = w[k1];
+        __syncwarp(gmask);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+          const int ky = t + G * k1;
+          const float2 mir = scr[(N - ky) & (N - 1)];
+          w[k1] = cadd(cmul(w[k1], __ldg(kp + ky * KP)), cmul(conjf2(mir), __ldg(kp + ky * KP + N / 2)));
+        }
+        __syncwarp(gmask);
+      }
+      float2 u[Q][G];
+      fft_standard<GE, true, true>(w, u, scr, tw_std, t, gmask);
+#pragma unroll
+      for (int q = 0; q < Q; ++q) {
+        const int m = t + G * (q >> 1);
+        const int col = (c != 0) ? ((q & 1) ? N - c : c) : ((q & 1) ? N / 2 : 0);
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) spec[(m + (P / 2) * k1) * N + col] = u[q][k1];
+      }
+    }
+    __syncthreads();
+    float acc[14];
+#pragma unroll
+    for (int i = 0; i < 14; ++i) acc[i] = 0.f;
+    bool border = false;
+    const int sy = shv[0], sx = shv[1];
+    for (int r = grp; r < N / 2; r += NG) {  // row inverse, growth, update, moments
+      const float2* pr = spec + r * N;
+      float2 v[Q][G];
+#pragma unroll
+      for (int jp = 0; jp < Q / 2; ++jp) {
+        const int m = t + G * jp;
+        if (m != 0) {
+#pragma unroll
+          for (int n2 = 0; n2 < G; ++n2) {
+            const int kx = m + P * n2, kk = N - kx;
+            float2 zk, zkk;
+            if (n2 < G / 2) {
+              const float2 s1 = pr[kx], s2 = pr[kk];
+              zk = make_float2(s1.x - s2.y, s1.y + s2.x);
+              zkk = make_float2(s1.x + s2.y, s2.x - s1.y);
+            } else {
+              const float2 s1 = pr[kk], s2 = pr[kx];
+              zkk = make_float2(s1.x - s2.y, s1.y + s2.x);
+              zk = make_float2(s1.x + s2.y, s2.x - s1.y);
+            }
+            v[2 * jp][n2] = zk;
+            v[2 * jp + 1][G - 1 - n2] = zkk;
+          }
+        } else {
+          const float2 s0 = pr[0], sn = pr[N / 2];
+          v[2 * jp][0] = make_float2(s0.x, sn.x);
+          v[2 * jp][G / 2] = make_float2(s0.y, sn.y);
+#pragma unroll
+          for (int n2 = 1; n2 < G / 2; ++n2) {
+            const int kx = P * n2, kk = N - kx;
+            const float2 s1 = pr[kx], s2 = pr[kk];
+            v[2 * jp][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
+            v[2 * jp][G - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
+          }
+#pragma unroll
+          for (int n2 = 0; n2 < G / 2; ++n2) {
+            const int kx = P / 2 + P * n2, kk = N - kx;
+            const float2 s1 = pr[kx], s2 = pr[kk];
+            v[2 * jp + 1][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
+            v[2 * jp + 1][G - 1 - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
+          }
+        }
+      }
+      float2 w[P];
+      fft_mirrored<GE, true, true>(v, w, scr, tw_rowi, t, gmask);
+      const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);
+      const float cyb = (float)(((2 * r + 1 - sy) & (N - 1)) - N / 2);
+      float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f;
+#pragma unroll
+      for (int k1 = 0; k1 < P; ++k1) {
+        const int x = t + G * k1;
+        const float pa = w[k1].x, pb = w[k1].y;
+        const float sa = src[(2 * r) * N + x], sb = src[(2 * r + 1) * N + x];
+        const float fa = growth_cell<GF>(gq, pa) * wf, fb = growth_cell<GF>(gq, pb) * wf;
+        st[(2 * r) * N + x] = state_fn(a.state_fn, sa, fa, dt);
+        st[(2 * r + 1) * N + x] = state_fn(a.state_fn, sb, fb, dt);
+        const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
+        const float cx = (float)(((x - sx) & (N - 1)) - N / 2);
+        Sa += sa;
+        Sb += sb;
+        Ga += fpa;
+        Gb += fpb;
+        const float ss = sa + sb, gg = fpa + fpb;
+        acc[RAW_MX + 1] = fmaf(ss, cx, acc[RAW_MX + 1]);
+        acc[RAW_GX + 1] = fmaf(gg, cx, acc[RAW_GX + 1]);
+        acc[RAW_MX2 + 1] = fmaf(ss * cx, cx, acc[RAW_MX2 + 1]);
+        acc[RAW_CNT_POT] += (pa > kEps ? 1.f : 0.f) + (pb > kEps ? 1.f : 0.f);
+        const bool la = sa > kEps, lb = sb > kEps;
+        acc[RAW_CNT_MASS] += (la ? 1.f : 0.f) + (lb ? 1.f : 0.f);
+        acc[RAW_CNT_GROW] += (fpa > kEps ? 1.f : 0.f) + (fpb > kEps ? 1.f : 0.f);
+        border |= ((x == 0 || x == N - 1) && (la || lb)) || (r == 0 && la) || (r == N / 2 - 1 && lb);
+      }
+      acc[RAW_M00] += Sa + Sb;
+      acc[RAW_G00] += Ga + Gb;
+      acc[RAW_MX + 0] += cya * Sa + cyb * Sb;
+      acc[RAW_GX + 0] += cya * Ga + cyb * Gb;
+      acc[RAW_MX2 + 0] += cya * cya * Sa + cyb * cyb * Sb;
+    }
+    big_finish_step(a, world, step, 2, sizes, acc, border, red, shv);
+  }
+}
+
+// ------------------------------------------------------------------ big 3D
+// Half spectrum X[z][y][kx], kx in [0, N/2], in the per-CTA scratch.
+template <int N, int G, int GF>
+__device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float2* tw_std, float2* work) {
+  using GE = Geo<N, G>;
+  constexpr int P = GE::P, Q = GE::Q, NG = 512 / G, HW = N / 2 + 1;
+  constexpr size_t PLANE = (size_t)N * HW;
+  const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31;
+  const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
+  float2* scr = work + grp * GE::SCR;
+  float* red = reinterpret_cast<float*>(work + NG * GE::SCR);
+  int* shv = reinterpret_cast<int*>(red + 16 * 16);
+  float2* X = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;
+  const float2* kp = a.kp + (size_t)world * N * PLANE;  // [N][N][HW], scaled by 1/N^3
+  const float* c0 = a.cells0 + (size_t)world * N * N * N;
+  float* st = a.state + (size_t)world * N * N * N;
+  const GrowthP gq = big_growth<GF>(a, world);
+  const float wk = __ldg(a.w + world), wf = a.mean ? wk / wk : wk;
+  const float dt = 1.f / __ldg(a.T + world);
+  const int sizes[3] = {N, N, N};
+  if (threadIdx.x == 0) shv[0] = shv[1] = shv[2] = 0;
+  __syncthreads();
+  for (int step = 0; step < a.steps; ++step) {
+    const float* src = step == 0 ? c0 : st;
+    // x pass: row pairs (z, 2r, 2r+1) -> half spectrum rows
+    for (int p = grp; p < N * (N / 2); p += NG) {
+      const int z = p / (N / 2), r = p % (N / 2);
+      const float* ra = src + ((size_t)z * N + 2 * r) * N;
+      float2 v[P];
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) v[n2] = make_float2(ra[t + G * n2], ra[N + t + G * n2]);
+      float2 u[Q][G];
+      fft_standard<GE, false, false>(v, u, scr, tw_std, t, gmask);
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) scr[t + G * q + P * k1] = u[q][k1];
+      __syncwarp(gmask);
+      float2* xa = X + ((size_t)z * N + 2 * r) * HW;
+      for (int kx = t; kx <= N / 2; kx += G) {
+        const float2 zk = scr[kx], zm = scr[(N - kx) & (N - 1)];
+        const float2 A = caddc(zk, zm), D = csubc(zk, zm);  // 2 X[2r], 2i X[2r+1]
+        xa[kx] = make_float2(0.5f * A.x, 0.5f * A.y);
+        xa[HW + kx] = make_float2(0.5f * D.y, -0.5f * D.x);
+      }
+      __syncwarp(gmask);
+    }
+    __syncthreads();
+    // y pass forward: lines (z, kx)
+    for (int l = grp; l < N * HW; l += NG) {
+      float2* base = X + (size_t)(l / HW) * PLANE + (l % HW);
+      float2 v[P];
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) v[n2] = base[(size_t)(t + G * n2) * HW];
+      float2 u[Q][G];
+      fft_standard<GE, false, false>(v, u, scr, tw_std, t, gmask);
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) base[(size_t)(t + G * q + P * k1) * HW] = u[q][k1];
+    }
+    __syncthreads();
+    // z pass: forward, x prepared spectrum, inverse
+    for (int l = grp; l < N * HW; l += NG) {
+      float2* base = X + l;  // l = ky * HW + kx
+      const float2* kb = kp + l;
+      float2 v[P];
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) v[n2] = base[(size_t)(t + G * n2) * PLANE];
+      float2 u[Q][G];
+      fft_standard<GE, false, false>(v, u, scr, tw_std, t, gmask);
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) {
+          const int kz = t + G * q + P * k1;
+          u[q][k1] = cmul(u[q][k1], __ldg(kb + (size_t)kz * PLANE));
+        }
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) scr[t + G * q + P * k1] = u[q][k1];
+      __syncwarp(gmask);
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) v[n2] = scr[t + G * n2];
+      __syncwarp(gmask);
+      fft_standard<GE, true, false>(v, u, scr, tw_std, t, gmask);
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) base[(size_t)(t + G * q + P * k1) * PLANE] = u[q][k1];
+    }
+    __syncthreads();
+    // y pass inverse
+    for (int l = grp; l < N * HW; l += NG) {
+      float2* base = X + (size_t)(l / HW) * PLANE + (l % HW);
+      float2 v[P];
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) v[n2] = base[(size_t)(t + G * n2) * HW];
+      float2 u[Q][G];
+      fft_standard<GE, true, false>(v, u, scr, tw_std, t, gmask);
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) base[(size_t)(t + G * q + P * k1) * HW] = u[q][k1];
+    }
+    __syncthreads();
+    // x inverse, growth, update, moments
+    float acc[14];
+#pragma unroll
+    for (int i = 0; i < 14; ++i) acc[i] = 0.f;
+    bool border = false;
+    const int sz = shv[0], sy = shv[1], sx = shv[2];
+    for (int p = grp; p < N * (N / 2); p += NG) {
+      const int z = p / (N / 2), r = p % (N / 2);
+      const float2* xa = X + ((size_t)z * N + 2 * r) * HW;
+      float2 v[P];
+#pragma unroll
+      for (int n2 = 0; n2 < P; ++n2) {
+        const int n = t + G * n2;
+        if (n <= N / 2) {
+          const float2 A = xa[n], B = xa[HW + n];
+          v[n2] = make_float2(A.x - B.y, A.y + B.x);  // A + iB
+        } else {
+          const float2 A = xa[N - n], B = xa[HW + N - n];
+          v[n2] = make_float2(A.x + B.y, B.x - A.y);  // conj(A) + i conj(B)
+        }
+      }
+      float2 u[Q][G];
+      fft_standard<GE, true, false>(v, u, scr, tw_std, t, gmask);
+      const float cz = (float)(((z - sz) & (N - 1)) - N / 2);
+      const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);
+      const float cyb = (float)(((2 * r + 1 - sy) & (N - 1)) - N / 2);
+      const float* sra = src + ((size_t)z * N + 2 * r) * N;
+      float* dsa = st + ((size_t)z * N + 2 * r) * N;
+      float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f;
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) {
+          const int x = t + G * q + P * k1;
+          const float pa = u[q][k1].x, pb = u[q][k1].y;
+          const float sa = sra[x], sb = sra[N + x];
+          const float fa = growth_cell<GF>(gq, pa) * wf, fb = growth_cell<GF>(gq, pb) * wf;
+          dsa[x] = state_fn(a.state_fn, sa, fa, dt);
+          dsa[N + x] = state_fn(a.state_fn, sb, fb, dt);
+          const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
+          const float cx = (float)(((x - sx) & (N - 1)) - N / 2);
+          Sa += sa;
+          Sb += sb;
+          Ga += fpa;
+          Gb += fpb;
+          const float ss = sa + sb, gg = fpa + fpb;
+          acc[RAW_MX + 2] = fmaf(ss, cx, acc[RAW_MX + 2]);
+          acc[RAW_GX + 2] = fmaf(gg, cx, acc[RAW_GX + 2]);
+          acc[RAW_MX2 + 2] = fmaf(ss * cx, cx, acc[RAW_MX2 + 2]);
+          acc[RAW_CNT_POT] += (pa > kEps ? 1.f : 0.f) + (pb > kEps ? 1.f : 0.f);
+          const bool la = sa > kEps, lb = sb > kEps;
+          acc[RAW_CNT_MASS] += (la ? 1.f : 0.f) + (lb ? 1.f : 0.f);
+          acc[RAW_CNT_GROW] += (fpa > kEps ? 1.f : 0.f) + (fpb > kEps ? 1.f : 0.f);
+          border |= ((x == 0 || x == N - 1 || z == 0 || z == N - 1) && (la || lb)) || (r == 0 && la) ||
+                    (r == N / 2 - 1 && lb);
+        }
+      const float S = Sa + Sb, Gs = Ga + Gb;
+      acc[RAW_M00] += S;
+      acc[RAW_G00] += Gs;
+      acc[RAW_MX + 0] += cz * S;
+      acc[RAW_GX + 0] += cz * Gs;
+      acc[RAW_MX2 + 0] += cz * cz * S;
+      acc[RAW_MX + 1] += cya * Sa + cyb * Sb;
+      acc[RAW_GX + 1] += cya * Ga + cyb * Gb;
+      acc[RAW_MX2 + 1] += cya * cya * Sa + cyb * cyb * Sb;
+    }
+    big_finish_step(a, world, step, 3, sizes, acc, border, red, shv);
+  }
+}
+
+template <int N, int G, int GF>
+__device__ __noinline__ void resident_item_call(const ResidentArgs& a, int item, const float2* tw, float2* work) {
+  int loaded = -1;
+  resident_item<N, G, GF>(a, item, tw, work, loaded);
+}
+
+template <int GF>
+__device__ __forceinline__ void dispatch_gf(const BatchClassArgs& c, int item, float2* sm, float2* work) {
+  switch (c.kind) {
+    case BK_R32: resident_item_call<32, 4, GF>(c.r, item, sm + TW32, work); break;
+    case BK_R64: resident_item_call<64, 4, GF>(c.r, item, sm + TW64, work); break;
+    case BK_R128: resident_item_call<128, 8, GF>(c.r, item, sm + TW128, work); break;
+    case BK_B2D256: big2d_item<256, GF>(c.b, item, sm + TW256, work); break;
+    case BK_B3D32:
+      if (c.line_group == 2) big3d_item<32, 2, GF>(c.b, item, sm + TW32G2, work);
+      else big3d_item<32, 4, GF>(c.b, item, sm + TW32, work);
+      break;
+    case BK_B3D64:
+      if (c.line_group == 2) big3d_item<64, 2, GF>(c.b, item, sm + TW64G2, work);
+      else big3d_item<64, 4, GF>(c.b, item, sm + TW64, work);
+      break;
+  }
+}
+
+__global__ void __launch_bounds__(512, 1) mixed_kernel(MixedArgs ma) {
+  extern __shared__ __align__(16) float2 sm[];
+  init_twiddles<Geo<32, 4>>(sm + TW32, sm + TW32 + 32, sm + TW32 + 64, threadIdx.x, blockDim.x);
+  init_twiddles<Geo<64, 4>>(sm + TW64, sm + TW64 + 64, sm + TW64 + 128, threadIdx.x, blockDim.x);
+  init_twiddles<Geo<128, 8>>(sm + TW128, sm + TW128 + 128, sm + TW128 + 256, threadIdx.x, blockDim.x);
+  init_twiddles<Geo<256, 8>>(sm + TW256, sm + TW256 + 256, sm + TW256 + 512, threadIdx.x, blockDim.x);
+  // G = 2 line transforms use only the standard table
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * double(((i % 2) * (i / 2)) % 64) / 64.0, &s, &c);
+    sm[TW64G2 + i] = make_float2((float)c, (float)s);
+  }
+  for (int i = threadIdx.x; i < 32; i += blockDim.x) {
+    double s, c;
+    sincospi(-2.0 * double(((i % 2) * (i / 2)) % 32) / 32.0, &s, &c);
+    sm[TW32G2 + i] = make_float2((float)c, (float)s);
+  }
+  __syncthreads();
+  __shared__ BatchClassArgs s_cls[kMaxBatchClasses];
+  __shared__ int s_item;
+  {
+    const int* src = reinterpret_cast<const int*>(ma.cls);
+    int* dst = reinterpret_cast<int*>(s_cls);
+    const int n = ma.n_cls * (int)(sizeof(BatchClassArgs) / sizeof(int));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
+  float2* work = sm + TW_END;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(ma.head, 1);
+    __syncthreads();
+    const int it = s_item;
+    __syncthreads();
+    if (it >= ma.n_items) break;
+    const int2 w = ma.items[it];
+    const BatchClassArgs& c = s_cls[w.x];
+    if (c.gf_variant == GF_FAST_GAUSSIAN) dispatch_gf<GF_FAST_GAUSSIAN>(c, w.y, sm, work);
+    else if (c.gf_variant == GF_FAST_POLY4) dispatch_gf<GF_FAST_POLY4>(c, w.y, sm, work);
+    else dispatch_gf<GF_GENERIC>(c, w.y, sm, work);
+  }
+}
+
+template <int N>
+__global__ void prepare_3d_kernel(long n, const float2* __restrict__ kh, float2* __restrict__ kp) {
+  const long total = n * (long)N * N * (N / 2 + 1);
+  const float scale = 1.f / ((float)N * (float)N * (float)N);
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const float2 k = kh[i];
+    kp[i] = make_float2(k.x * scale, k.y * scale);
+  }
+}
+
+__global__ void batch_setup_kernel(BatchSetup s) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (blockIdx.x == 0) {
+    const int* src = reinterpret_cast<const int*>(s.cls);
+    int* dst = reinterpret_cast<int*>(s.cls_out);
+    const int n = s.n_cls * (int)(sizeof(BatchClassArgs) / sizeof(int));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+    if (threadIdx.x == 0) *s.head = 0;
+  }
+  for (int i = tid; i < s.n_items; i += gridDim.x * blockDim.x) {
+    int r = 0;
+    while (r + 1 < s.n_cls && s.first_item[r + 1] <= i) ++r;
+    s.items[i] = make_int2(s.cls_of_rank[r], i - s.first_item[r]);
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_batch_setup(const BatchSetup& s, cudaStream_t st) {
+  const int blocks = (int)std::min<long>((s.n_items + 255) / 256 + 1, 1024);
+  batch_setup_kernel<<<blocks, 256, 0, st>>>(s);
+  return cudaGetLastError();
+}
+
+size_t mixed_smem_bytes() { return kMixedSmem; }
+
+long batch_scratch_per_cta(int kind) {
+  switch (kind) {
+    case BK_B2D256: return 128L * 256;
+    case BK_B3D32: return 32L * 32 * 17;
+    case BK_B3D64: return 64L * 64 * 33;
+  }
+  return 0;
+}
+
+int batch_worlds_per_item(int kind) {
+  switch (kind) {
+    case BK_R32: return RCfg<32, 4>::WPC;
+    case BK_R64: return RCfg<64, 4>::WPC;
+    case BK_R128: return RCfg<128, 8>::WPC;
+  }
+  return 1;
+}
+
+int batch_kind_gf_variant(int gf_id) {
+  return gf_id == LGX_GF_GAUSSIAN ? GF_FAST_GAUSSIAN : (gf_id == LGX_GF_POLY_QUAD4 ? GF_FAST_POLY4 : GF_GENERIC);
+}
+
+cudaError_t launch_mixed(const MixedArgs& a, int grid, cudaStream_t st) {
+  // set once per device, before any stream capture of a launch (the first
+  // launch on a device happens uncaptured: UnevenBatch.capture warms up first)
+  static std::mutex mu;
+  static bool attr_set[64] = {false};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  {
+    std::lock_guard<std::mutex> lk(mu);
+    if (!attr_set[dev]) {
+      e = cudaFuncSetAttribute(mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMixedSmem);
+      if (e != cudaSuccess) return e;
+      attr_set[dev] = true;
+    }
+  }
+  mixed_kernel<<<grid, 512, kMixedSmem, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prepare_3d_spectrum(int N, long n, const float2* k_half, float2* kp, cudaStream_t st) {
+  const long total = n * (long)N * N * (N / 2 + 1);
+  const int blocks = (int)std::min<long>((total + 255) / 256, 8192);
+  switch (N) {
+    case 32: prepare_3d_kernel<32><<<blocks, 256, 0, st>>>(n, k_half, kp); break;
+    case 64: prepare_3d_kernel<64><<<blocks, 256, 0, st>>>(n, k_half, kp); break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace lgx

@@ -35,6 +35,15 @@ int cuda_fail(cudaError_t e, const char* where) {
   return fail(LGX_ERR_CUDA, "%s: %s", where, cudaGetErrorString(e));
 }
 
+}  // namespace
+
+int lgx::api_error(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+
+namespace {
+
 inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Bump allocator over a caller-owned workspace.

@@ -25,6 +25,9 @@ struct Model {
   long cells;   // D*H*W
 };
 
+// Record `msg` as the calling thread's lgx_last_error() and return `code`.
+int api_error(int code, const char* msg);
+
 // The model a plan was built from (capi.cu).
 const Model* plan_model(const lgx_plan* plan);
 
@@ -55,6 +58,58 @@ int resident_max_grid(int N);
 // Prepare the resident spectra: kp[s][ky][c] from the half spectrum.
 cudaError_t launch_prepare_resident_spectrum(int N, int n_sols, const float2* k_half, float2* kp,
                                              cudaStream_t st);
+
+// ---------------------------------------------------------------- uneven batch
+// One world per CTA for sizes beyond the resident slices: 2D 256^2 and 3D
+// 32^3 / 64^3.  Every world is its own solution (per-world spectrum and
+// parameters); raw moments are [n_worlds, steps, raw_stride(1)].
+struct BigArgs {
+  int n_worlds, steps;
+  int gf_id, state_fn, mean;
+  const float* cells0;   // [n_worlds, N^nd]
+  const float2* kp;      // 2D: [n_worlds, N, N/2+2] (resident layout); 3D: [n_worlds, N, N, N/2+1] / N^3
+  const float* gf;       // [n_worlds, 2]
+  const float* w;        // [n_worlds]
+  const float* T;        // [n_worlds]
+  float* state;          // [n_worlds, N^nd]: final cells (updated in place from step 1)
+  float* raw;            // [n_worlds, steps, raw_stride(1)]
+  float2* scratch;       // [grid, scratch_per_cta] spectrum scratch
+  long scratch_per_cta;  // float2 elements
+};
+enum BatchKind : int { BK_R32 = 0, BK_R64 = 1, BK_R128 = 2, BK_B2D256 = 3, BK_B3D32 = 4, BK_B3D64 = 5 };
+constexpr int kMaxBatchClasses = 8;
+struct BatchClassArgs {
+  int kind, gf_variant, line_group;  // line_group: 3D y/z line transform lanes (2 or 4)
+  ResidentArgs r;                    // resident kinds (n_init = 1)
+  BigArgs b;                         // big kinds
+};
+struct MixedArgs {
+  int n_items, n_cls;
+  const int2* items;           // [n_items] (class, item within class), processing order
+  int* head;                   // queue head counter, zeroed before the launch
+  const BatchClassArgs* cls;   // [n_cls] in device memory
+};
+// Spectrum scratch (float2 elements) one CTA needs for a big kind.
+long batch_scratch_per_cta(int kind);
+// Worlds processed per item of a kind.
+int batch_worlds_per_item(int kind);
+size_t mixed_smem_bytes();
+int batch_kind_gf_variant(int gf_id);
+cudaError_t launch_mixed(const MixedArgs& a, int grid, cudaStream_t st);
+// Work queue and class table of one mixed launch, written on the device so a
+// captured graph rebuilds them on every replay.
+struct BatchSetup {
+  BatchClassArgs cls[kMaxBatchClasses];
+  int n_cls, n_items;
+  int first_item[kMaxBatchClasses + 1];  // queue position of each rank's first item
+  int cls_of_rank[kMaxBatchClasses];     // class processed at each rank
+  BatchClassArgs* cls_out;
+  int2* items;
+  int* head;
+};
+cudaError_t launch_batch_setup(const BatchSetup& s, cudaStream_t st);
+// 3D prepared spectrum: the [n, N, N, N/2+1] half spectrum scaled by 1/N^3.
+cudaError_t launch_prepare_3d_spectrum(int N, long n, const float2* k_half, float2* kp, cudaStream_t st);
 
 // ---------------------------------------------------------------- streamed
 struct StreamedArgs;  // defined in streamed.cu
@@ -123,6 +178,8 @@ struct StatsArgs {
   int n_sols, n_init, steps, C, nb_dims;
   int world[3];
   float R, T;
+  const float* R_arr;  // per-solution R overriding R, or null
+  const float* T_arr;  // per-solution static T overriding T, or null
   const float* raw;
   float* stats;       // [Ns, steps, Ni, C + 11] or null
   float* n_continue;  // [Ns, Ni] or null

@@ -21,6 +21,8 @@ struct Ctx {
   int nd, C, steps, n_init;
   float R, dt;
   int world[3];
+  const float* R_arr;  // per-solution R (or null: R)
+  const float* T_arr;  // per-solution static T (or null: 1/dt)
 };
 
 // Per-axis triples are kept as named scalars and returned by value (no
@@ -90,7 +92,9 @@ __global__ void stats_kernel(Ctx c, int n_sols, const float* __restrict__ raw, f
   const int sol = (int)(i / ((long)c.n_init * c.steps));
   const int nd = c.nd;
   const float* r = raw_at(raw, c, sol, step, init);
-  const float R2 = c.R * c.R;
+  const float Rs = c.R_arr ? __ldg(c.R_arr + sol) : c.R;
+  const float dts = c.T_arr ? 1.f / __ldg(c.T_arr + sol) : c.dt;
+  const float R2 = Rs * Rs;
   const float m00 = r[RAW_M00], g00 = r[RAW_G00];
   const Tri zero = {0.f, 0.f, 0.f};
   const Tri cen = centroid(r, nd);
@@ -102,11 +106,11 @@ __global__ void stats_kernel(Ctx c, int n_sols, const float* __restrict__ raw, f
     pc = frac(c1);
     const Tri p1 = (step > 1) ? frac(centroid(raw_at(raw, c, sol, step - 2, init), nd)) : zero;
     const Tri d1 = sub(c1, p1);
-    prev_angle = angle_of(d1, norm(d1, nd), c.R);
+    prev_angle = angle_of(d1, norm(d1, nd), Rs);
   }
   const Tri delta = sub(cen, pc);
   const float dist_m = norm(delta, nd);
-  const float mass_angle = angle_of(delta, dist_m, c.R);
+  const float mass_angle = angle_of(delta, dist_m, Rs);
   // growth centroid distance and inertia (statistics.py:93-100)
   const float gden = g00 + kEps, mden = m00 * m00 + kEps;
   float gcd2, inertia;
@@ -148,9 +152,9 @@ __global__ void stats_kernel(Ctx c, int n_sols, const float* __restrict__ raw, f
   s[3] = growth;
   s[4] = growth_volume;
   s[5] = growth / (growth_volume + kEps);
-  s[6] = dist_m / c.R / c.dt;
-  s[7] = (md - 180.f) / c.dt;
-  s[8] = sqrtf(gcd2) / c.R;
+  s[6] = dist_m / Rs / dts;
+  s[7] = (md - 180.f) / dts;
+  s[8] = sqrtf(gcd2) / Rs;
   s[9] = inertia;
   s[10] = r[RAW_CNT_POT] / R2;
 }
@@ -160,7 +164,8 @@ __global__ void heuristics_kernel(Ctx c, int n_sols, float area, const float* __
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n_sols * c.n_init) return;
   const int sol = i / c.n_init, init = i % c.n_init;
-  const float R2 = c.R * c.R;
+  const float Rs = c.R_arr ? __ldg(c.R_arr + sol) : c.R;
+  const float R2 = Rs * Rs;
   float init_cm[kMaxChannels];
   const float* r0 = raw_at(raw, c, sol, 0, init);
   for (int ch = 0; ch < c.C && ch < kMaxChannels; ++ch) init_cm[ch] = r0[RAW_CM + ch] / R2;
@@ -205,6 +210,8 @@ cudaError_t launch_stats(const StatsArgs& a, cudaStream_t st) {
   c.n_init = a.n_init;
   c.R = a.R;
   c.dt = 1.f / a.T;
+  c.R_arr = a.R_arr;
+  c.T_arr = a.T_arr;
   for (int d = 0; d < 3; ++d) c.world[d] = a.world[d];
   if (a.steps <= 0) return cudaSuccess;
   if (a.stats || a.centroid) {

@@ -90,3 +90,43 @@ def test_update_fn_refuses_cpu_tensors():
     u = helpers.build_update_fn(K.shape, m)
     with pytest.raises(ValueError, match='CUDA'):
         u(None, torch.zeros(1, 1, 64, 64), K, m.get_gf_params(), m.get_kernels_weight_per_channel(), 0.1)
+
+
+def test_batch_rejects_bad_jobs_without_device_work():
+    from leniax_gb300 import batch as lbatch
+    lib = lbatch._bind(_lib.load())
+    buf = (ctypes.c_float * 16)()
+    addr = ctypes.addressof(buf)
+    arr = (lbatch.BatchClassC * 2)()
+    for c in arr:
+        c.nb_dims, c.size, c.n_worlds, c.gf_id, c.state_fn, c.mean = 2, 64, 3, 1, 0, 1
+        c.cells0 = c.k_half = c.gf_params = c.weights = c.T = c.final_cells = addr
+    job = lbatch.BatchJobC()
+    job.n_classes, job.steps, job.classes = 2, 4, arr
+    nbytes = ctypes.c_size_t(0)
+
+    def code():
+        return lib.lgx_batch_workspace_bytes(ctypes.byref(job), ctypes.byref(nbytes))
+
+    arr[1].size = 48  # not a supported side
+    assert code() == _lib.LGX_ERR_UNSUPPORTED and nbytes.value == 0
+    arr[1].nb_dims, arr[1].size = 3, 128  # 3D 128^3 is not supported
+    assert code() == _lib.LGX_ERR_UNSUPPORTED
+    arr[1].nb_dims, arr[1].size = 3, 32
+    arr[1].stats = addr  # statistics without stats_R / stats_T
+    assert code() == _lib.LGX_ERR_INVALID
+    arr[1].stats = None
+    arr[0].cells0 = None
+    assert code() == _lib.LGX_ERR_INVALID
+    arr[0].cells0 = addr
+    job.order = 2  # explicit order without class_order
+    assert code() == _lib.LGX_ERR_INVALID
+    order = (ctypes.c_int * 2)(1, 1)
+    job.class_order = order
+    assert code() == _lib.LGX_ERR_INVALID  # not a permutation
+    job.order, job.line_group = 0, 3
+    assert code() == _lib.LGX_ERR_INVALID
+    job.line_group, job.n_classes = 0, 9
+    assert code() == _lib.LGX_ERR_INVALID
+    job.n_classes = 2
+    assert lib.lgx_batch_run(ctypes.byref(job), None, 0, None) == _lib.LGX_ERR_WORKSPACE
