@@ -278,6 +278,8 @@ def run_ours(args, rank, world_size):
     plain_value = PLAIN_SAMPLE_WORLDS * P_CELLS * PLAIN_SAMPLE_STEPS / (p0.elapsed_time(p1) / 1e3)
 
     adjoint = measure_adjoint(dev)
+    multichannel = measure_multichannel(dev)
+    uneven = measure_uneven(dev)
 
     gpu_launches = args.steps * 4  # prepare spectrum, resident kernel, stats, heuristics per rollout
     out = {
@@ -313,6 +315,8 @@ def run_ours(args, rank, world_size):
             'speedup_batched_vs_plain': value / world_size / plain_value
         },
         'adjoint': adjoint,
+        'multichannel': multichannel,
+        'uneven': uneven,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
         'hbm_peak_gbs_measured': measured_peaks().get('hbm_gbs'),
@@ -370,6 +374,111 @@ def measure_adjoint(dev, worlds=64, steps=256, ckpt=16, reps=3):
             'cells0': bool(torch.isfinite(c0.grad).all()), 'm_s': bool(torch.isfinite(gf.grad).all()),
             'b': bool(torch.isfinite(b.grad).all())
         }
+    }
+
+
+def _timed(fn, stream, flush, reps):
+    """Median CUDA-event time (ms) of fn() over reps runs, L2 flushed before each."""
+    import torch
+    ts = []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        ts.append(a.elapsed_time(b))
+    return pystats.median(ts)
+
+
+def measure_multichannel(dev, worlds=256, size=256, C=3, per_channel=5, steps=512, reps=2):
+    """Multi-channel model on the streamed engine: 256 worlds of 256x256,
+    C=3 channels, K=15 kernels (5 per channel, seeded R in [10, 20], 1-3
+    rings, m in [0.1, 0.4], s in [0.01, 0.05], target weights normalised per
+    channel), dt=0.2, uniform[0,1) 64x64 central patches per channel, 512
+    steps with leniax statistics and both stop sets.  Streamed case roofline:
+    HBM bytes of the compulsory traffic (state in + out, half spectrum in:
+    8*C*P + 8*K*(P/2+1) bytes per world-step) over the rollout time."""
+    import torch
+    from leniax_gb300 import helpers, kernels, runner, statistics, workloads
+    R_world, T_mc = 20.0, 5.0
+    kp = workloads.multichannel_params(C, per_channel, seed=0, world_R=R_world)
+    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in kp], [size, size], C, R_world, True, dev)
+    upd = helpers.build_update_fn(K.shape, mp, 'v1', True)
+    stats_fn = statistics.ComputeStatsFn([size, size], R_world, T_mc)
+    cells = torch.from_numpy(workloads.multichannel_cells(worlds, C, size, 64, seed=0)[None]).to(dev)
+    gf, w, T = mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([T_mc])
+    nk = len(kp)
+    out = {}
+
+    def run(n_steps):
+        out['r'] = runner.run_scan_mem_optimized(None, cells, K[None], gf, w, T, n_steps, R_world, upd, stats_fn,
+                                                 engine='streamed', with_box=True)
+
+    run(4)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ms = _timed(lambda: run(steps), torch.cuda.current_stream(dev), flush, reps)
+    P = size * size
+    cu = worlds * C * P * steps
+    bytes_ws = 8 * C * P + 8 * nk * (P // 2 + 1)
+    achieved = bytes_ws * worlds * steps / (ms / 1e3) / 1e9
+    peak = measured_peaks().get('hbm_gbs')
+    sd = out['r'][0]
+    return {
+        'workload': f'multichannel-{worlds}x{size}x{size}-c{C}k{nk}-{steps}steps', 'engine': 'streamed',
+        'metric': METRIC, 'value': cu / (ms / 1e3), 'unit': METRIC, 'ms_per_rollout': ms,
+        'ms_per_euler_step': ms / steps, 'mean_N': float(sd['N'].float().mean()),
+        'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak if peak else None,
+                     'algorithmic_bytes_per_world_step': bytes_ws,
+                     'note': 'compulsory traffic over the whole step (4 kernels); peak = measured copy bandwidth'},
+        'l2': 'flushed between timed rollouts (256 MB write)',
+    }
+
+
+def measure_uneven(dev, steps=256, reps=3):
+    """Uneven search batch in one persistent launch, replayed from a CUDA
+    graph: 4096 C=K=1 worlds (2048 of 64x64, 1229 of 128x128, 614 of
+    256x256, 205 of 64x64x64), per-world R in [5, 26], m in [0.1, 0.35], s in
+    [0.01, 0.05], dt in {0.05, 0.1, 0.2}, uniform[0,1) central patches of side
+    size/3, 256 steps, statistics and both stop sets per world.  Settings from
+    the autotuner.  Beside it: the same classes launched one class after the
+    other (one shape per launch, as a shape-specialised vmap batches them)."""
+    import torch
+    from leniax_gb300 import autotune
+    from leniax_gb300 import batch as lbatch
+    from leniax_gb300 import workloads
+    classes = workloads.build_classes(device=dev)
+    t0 = time.perf_counter()
+    settings = autotune.tuned_settings(classes, steps)
+    tune_s = time.perf_counter() - t0
+    b = lbatch.UnevenBatch(classes, steps, **settings).capture()
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    b.run()
+    torch.cuda.synchronize()
+    ms = _timed(b.run, stream, flush, reps)
+    per_class = [lbatch.UnevenBatch([c], steps, line_group=settings.get('line_group', 4)).capture() for c in classes]
+    for pc in per_class:
+        pc.run()
+    torch.cuda.synchronize()
+
+    def seq():
+        for pc in per_class:
+            pc.run()
+
+    ms_seq = _timed(seq, stream, flush, max(1, reps - 1))
+    res = b.results()
+    n_alive = sum(float(r['stats']['N_box'].sum()) for r in res) / sum(c.n for c in classes)
+    return {
+        'workload': 'uneven-4096-worlds-64sq-128sq-256sq-64cube-256steps', 'metric': METRIC,
+        'value': b.cells_per_run / (ms / 1e3), 'unit': METRIC, 'ms_per_rollout': ms,
+        'classes': [{'world': list(c.world), 'worlds': c.n} for c in classes],
+        'settings': settings, 'autotune_seconds': tune_s, 'graph': True,
+        'one_class_per_launch': {'value': b.cells_per_run / (ms_seq / 1e3), 'ms_per_rollout': ms_seq},
+        'mean_stop_step_box_set': n_alive, 'l2': 'flushed between timed rollouts (256 MB write)',
     }
 
 

@@ -186,48 +186,8 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
     bool border = false;
     const int sy = shv[0], sx = shv[1];
     for (int r = grp; r < N / 2; r += NG) {  // row inverse, growth, update, moments
-      const float2* pr = spec + r * N;
       float2 v[Q][G];
-#pragma unroll
-      for (int jp = 0; jp < Q / 2; ++jp) {
-        const int m = t + G * jp;
-        if (m != 0) {
-#pragma unroll
-          for (int n2 = 0; n2 < G; ++n2) {
-            const int kx = m + P * n2, kk = N - kx;
-            float2 zk, zkk;
-            if (n2 < G / 2) {
-              const float2 s1 = pr[kx], s2 = pr[kk];
-              zk = make_float2(s1.x - s2.y, s1.y + s2.x);
-              zkk = make_float2(s1.x + s2.y, s2.x - s1.y);
-            } else {
-              const float2 s1 = pr[kk], s2 = pr[kx];
-              zkk = make_float2(s1.x - s2.y, s1.y + s2.x);
-              zk = make_float2(s1.x + s2.y, s2.x - s1.y);
-            }
-            v[2 * jp][n2] = zk;
-            v[2 * jp + 1][G - 1 - n2] = zkk;
-          }
-        } else {
-          const float2 s0 = pr[0], sn = pr[N / 2];
-          v[2 * jp][0] = make_float2(s0.x, sn.x);
-          v[2 * jp][G / 2] = make_float2(s0.y, sn.y);
-#pragma unroll
-          for (int n2 = 1; n2 < G / 2; ++n2) {
-            const int kx = P * n2, kk = N - kx;
-            const float2 s1 = pr[kx], s2 = pr[kk];
-            v[2 * jp][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
-            v[2 * jp][G - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
-          }
-#pragma unroll
-          for (int n2 = 0; n2 < G / 2; ++n2) {
-            const int kx = P / 2 + P * n2, kk = N - kx;
-            const float2 s1 = pr[kx], s2 = pr[kk];
-            v[2 * jp + 1][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
-            v[2 * jp + 1][G - 1 - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
-          }
-        }
-      }
+      unpack_row_pair<GE>(spec + r * N, v, t);
       float2 w[P];
       fft_mirrored<GE, true, true>(v, w, scr, tw_rowi, t, gmask);
       const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);

@@ -81,6 +81,38 @@ __device__ __forceinline__ float state_fn(int id, float s, float f, float dt) {
   return s + dt * f;
 }
 
+// Growth-function specialisations of the per-cell epilogue.
+constexpr int GF_GENERIC = 0, GF_FAST_GAUSSIAN = 1, GF_FAST_POLY4 = 2;
+
+__device__ __forceinline__ float fast_exp2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Per-world growth parameters.  The gaussian family uses
+// exp(-d^2/2) = 2^(-(d*sqrt(log2(e)/2))^2): the scale folds 1/s and that
+// constant, so a cell costs one subtract, two multiplies and one ex2.
+struct GrowthP {
+  float m, s, a;  // a: gaussian scale or 1/(9 s^2)
+  int id;
+};
+
+template <int GF>
+__device__ __forceinline__ float growth_cell(const GrowthP& g, float x) {
+  if constexpr (GF == GF_FAST_GAUSSIAN) {
+    const float d = (x - g.m) * g.a;
+    return fmaf(2.f, fast_exp2(-(d * d)), -1.f);
+  } else if constexpr (GF == GF_FAST_POLY4) {
+    const float d = x - g.m;
+    float o = fmaxf(0.f, fmaf(-(d * d), g.a, 1.f));
+    o = o * o;
+    return fmaf(2.f, o * o, -1.f);
+  } else {
+    return growth_fn(g.id, x, g.m, g.s);
+  }
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

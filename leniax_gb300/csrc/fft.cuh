@@ -270,4 +270,57 @@ __device__ __forceinline__ void fft_mirrored(float2 (&v)[GE::Q][GE::G], float2 (
   fft_reg<P, INV>(w);
 }
 
+// Row-inverse input of a packed row pair.  `pr` holds the N-point packed row r
+// of a real 2D transform after the column pass: slot k < N/2 carries
+// P[2r][k] and slot N - k carries P[2r+1][k] (P the half spectra of rows 2r
+// and 2r+1; slots 0 and N/2 carry the DC / Nyquist columns packed together).
+// Fills v[q][n2] = Z[n1 + P*n2] with n1 from the mirror set of lane t, where
+// Z = P[2r] + i P[2r+1] over the full row, ready for
+// fft_mirrored<GE, true, true>, whose output w[k1] is then
+// (row 2r, row 2r+1) at x = t + G*k1.
+template <class GE>
+__device__ __forceinline__ void unpack_row_pair(const float2* pr, float2 (&v)[GE::Q][GE::G], int t) {
+  constexpr int N = GE::N, G = GE::G, P = GE::P, Q = GE::Q;
+#pragma unroll
+  for (int jp = 0; jp < Q / 2; ++jp) {
+    const int m = t + G * jp;
+    if (m != 0) {
+#pragma unroll
+      for (int n2 = 0; n2 < G; ++n2) {
+        const int kx = m + P * n2, kk = N - kx;
+        float2 zk, zkk;
+        if (n2 < G / 2) {
+          const float2 s1 = pr[kx], s2 = pr[kk];
+          zk = make_float2(s1.x - s2.y, s1.y + s2.x);
+          zkk = make_float2(s1.x + s2.y, s2.x - s1.y);
+        } else {
+          const float2 s1 = pr[kk], s2 = pr[kx];
+          zkk = make_float2(s1.x - s2.y, s1.y + s2.x);
+          zk = make_float2(s1.x + s2.y, s2.x - s1.y);
+        }
+        v[2 * jp][n2] = zk;
+        v[2 * jp + 1][G - 1 - n2] = zkk;
+      }
+    } else {
+      const float2 s0 = pr[0], sn = pr[N / 2];
+      v[2 * jp][0] = make_float2(s0.x, sn.x);
+      v[2 * jp][G / 2] = make_float2(s0.y, sn.y);
+#pragma unroll
+      for (int n2 = 1; n2 < G / 2; ++n2) {
+        const int kx = P * n2, kk = N - kx;
+        const float2 s1 = pr[kx], s2 = pr[kk];
+        v[2 * jp][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
+        v[2 * jp][G - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
+      }
+#pragma unroll
+      for (int n2 = 0; n2 < G / 2; ++n2) {
+        const int kx = P / 2 + P * n2, kk = N - kx;
+        const float2 s1 = pr[kx], s2 = pr[kk];
+        v[2 * jp + 1][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
+        v[2 * jp + 1][G - 1 - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
+      }
+    }
+  }
+}
+
 }  // namespace lgx

@@ -36,38 +36,6 @@ __device__ __forceinline__ int swz(int r) {
   return G == 8 ? (((r >> 1) & 7) << 1) : 0;
 }
 
-// Growth-function specialisations of the per-cell epilogue.
-constexpr int GF_GENERIC = 0, GF_FAST_GAUSSIAN = 1, GF_FAST_POLY4 = 2;
-
-__device__ __forceinline__ float fast_exp2(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
-// Per-world growth parameters.  The gaussian family uses
-// exp(-d^2/2) = 2^(-(d*sqrt(log2(e)/2))^2): the scale folds 1/s and that
-// constant, so a cell costs one subtract, two multiplies and one ex2.
-struct GrowthP {
-  float m, s, a;  // a: gaussian scale or 1/(9 s^2)
-  int id;
-};
-
-template <int GF>
-__device__ __forceinline__ float growth_cell(const GrowthP& g, float x) {
-  if constexpr (GF == GF_FAST_GAUSSIAN) {
-    const float d = (x - g.m) * g.a;
-    return fmaf(2.f, fast_exp2(-(d * d)), -1.f);
-  } else if constexpr (GF == GF_FAST_POLY4) {
-    const float d = x - g.m;
-    float o = fmaxf(0.f, fmaf(-(d * d), g.a, 1.f));
-    o = o * o;
-    return fmaf(2.f, o * o, -1.f);
-  } else {
-    return growth_fn(g.id, x, g.m, g.s);
-  }
-}
-
 // One work item of the resident engine: WPC consecutive worlds, one per
 // (N/2)*G-thread slice of the 512-thread CTA.  `tw` holds the three N-entry
 // twiddle tables, `work` the slices' shared buffers (RCfg::SMEM - 3N float2).

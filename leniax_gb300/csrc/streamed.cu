@@ -25,7 +25,8 @@ namespace lgx {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = 256;     // row_fwd blocks
+constexpr int kColThreads = 128;  // col_conv blocks (register-heavy: several blocks per SM)
 
 struct KTab {  // per-plan kernel table, passed by value
   int C, K, max_k, mean, state_fn, dt_mode;
@@ -85,13 +86,13 @@ __global__ void __launch_bounds__(kThreads) row_fwd_kernel(int n_worlds, int C, 
 
 // ----------------------------------------------------------------- col_conv
 template <int N>
-__global__ void __launch_bounds__(kThreads) col_conv_kernel(int n_worlds, int n_init, KTab tab,
-                                                            const float2* __restrict__ spec,
-                                                            const float2* __restrict__ kp, long kp_sol_stride,
-                                                            float2* __restrict__ prod) {
+__global__ void __launch_bounds__(kColThreads) col_conv_kernel(int n_worlds, int n_init, KTab tab,
+                                                               const float2* __restrict__ spec,
+                                                               const float2* __restrict__ kp, long kp_sol_stride,
+                                                               float2* __restrict__ prod) {
   constexpr int G = SCfg<N>::G;
   using GE = Geo<N, G>;
-  constexpr int P = GE::P, Q = GE::Q, GPB = kThreads / G;
+  constexpr int P = GE::P, Q = GE::Q, GPB = kColThreads / G;
   constexpr int BPP = (N / 2 + GPB - 1) / GPB;
   constexpr int KPITCH = N / 2 + 2;
   extern __shared__ __align__(16) float2 sm[];
@@ -128,15 +129,13 @@ __global__ void __launch_bounds__(kThreads) col_conv_kernel(int n_worlds, int n_
   }
   float2 w0[P];
   fft_mirrored<GE, false, false>(v, w0, cs, sm + N, t, gmask);
-  float2 mir[P];
+  // the packed DC / Nyquist column (c == 0, one group per plane) keeps its
+  // spectrum in the block's mirror buffer: Q[ky] needs A[-ky] for every kernel
+  float2* mirror = scr + GPB * GE::SCR;
   if (c == 0) {
-    const int src_lane = (lane & ~(G - 1)) | ((G - t) & (G - 1));
 #pragma unroll
-    for (int k1 = 0; k1 < P; ++k1) {
-      float2 val = (t != 0) ? w0[P - 1 - k1] : w0[(P - k1) & (P - 1)];
-      mir[k1].x = __shfl_sync(gmask, val.x, src_lane);
-      mir[k1].y = __shfl_sync(gmask, val.y, src_lane);
-    }
+    for (int k1 = 0; k1 < P; ++k1) mirror[t + G * k1] = w0[k1];
+    __syncwarp(gmask);
   }
   for (int k = 0; k < tab.K; ++k) {
     if (tab.cin[k] != ch) continue;
@@ -149,8 +148,8 @@ __global__ void __launch_bounds__(kThreads) col_conv_kernel(int n_worlds, int n_
 #pragma unroll
       for (int k1 = 0; k1 < P; ++k1) {
         const int ky = t + G * k1;
-        float2 A = __ldg(kk + ky * KPITCH), B = __ldg(kk + ky * KPITCH + N / 2);
-        w[k1] = cadd(cmul(w0[k1], A), cmul(conjf2(mir[k1]), B));
+        const float2 A = __ldg(kk + ky * KPITCH), B = __ldg(kk + ky * KPITCH + N / 2);
+        w[k1] = cadd(cmul(w0[k1], A), cmul(conjf2(mirror[(N - ky) & (N - 1)]), B));
       }
     }
     float2 u[Q][G];
@@ -170,8 +169,13 @@ __global__ void __launch_bounds__(kThreads) col_conv_kernel(int n_worlds, int n_
 }
 
 // ------------------------------------------------------------------ row_inv
-// Block = GPB groups = GPB packed rows of one world.  Field accumulators for
-// the block's 2*GPB rows live in shared memory ([C][2*GPB][N] floats).
+// Block = GPB groups = GPB packed rows of one world.  Output channels are
+// processed one after the other; the weighted field of the current channel is
+// accumulated in registers (the row pair of a group: 2*P values per thread)
+// over the kernels that feed it.  A kernel feeding several channels is
+// inverse-transformed once per channel; its potential is counted (and
+// written) once, at the first channel it feeds; kernels that feed no channel
+// are transformed at the end for the potential count alone.
 template <int N>
 struct RowInvCfg {
   static constexpr int G = SCfg<N>::G;
@@ -180,166 +184,147 @@ struct RowInvCfg {
   static constexpr int BPW = (N / 2) / GPB;  // blocks per world
 };
 
-template <int N>
-__global__ void __launch_bounds__(128) row_inv_kernel(int n_worlds, int n_init, KTab tab, const float2* __restrict__ prod,
-                                                      const float* __restrict__ gfp, long gf_sol_stride,
-                                                      const float* __restrict__ wts, long w_sol_stride,
-                                                      const float* __restrict__ dtp, const float* __restrict__ state,
-                                                      float* __restrict__ state_out, float* __restrict__ field_out,
-                                                      float* __restrict__ pot_out, const int* __restrict__ shift,
-                                                      float* __restrict__ partial) {
+template <int N, int GF>
+__global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
+    int n_worlds, int n_init, KTab tab, const float2* __restrict__ prod, const float* __restrict__ gfp,
+    long gf_sol_stride, const float* __restrict__ wts, long w_sol_stride, const float* __restrict__ dtp,
+    const float* __restrict__ state, float* __restrict__ state_out, float* __restrict__ field_out,
+    float* __restrict__ pot_out, const int* __restrict__ shift, float* __restrict__ partial) {
   using RC = RowInvCfg<N>;
   constexpr int G = RC::G, GPB = RC::GPB, BPW = RC::BPW;
   using GE = Geo<N, G>;
   constexpr int P = GE::P, Q = GE::Q;
   constexpr int RAWS_MAX = RAW_CM + kMaxChannels;
+  constexpr int NWARPS = RC::T / 32;
   extern __shared__ __align__(16) float2 sm[];
-  float2* scr = init_tw<N>(sm);  // GPB * SCR
-  float* facc = reinterpret_cast<float*>(scr + GPB * GE::SCR);  // [C][2*GPB][N]
-  float* red = facc + tab.C * 2 * GPB * N;                      // [warps][RAWS_MAX]
+  float2* scr = init_tw<N>(sm);                                   // GPB * SCR
+  float* red = reinterpret_cast<float*>(scr + GPB * GE::SCR);  // [warps][RAWS_MAX]
+  __syncthreads();
   const int n = blockIdx.x / BPW;
   if (n >= n_worlds) return;
   const int sol = n / n_init;
   const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int r = (blockIdx.x % BPW) * GPB + grp;
   const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
-  const int C = tab.C;
-  for (int i = threadIdx.x; i < C * 2 * GPB * N; i += blockDim.x) facc[i] = 0.f;
-  __syncthreads();
+  const int C = tab.C, K = tab.K;
   float2* rs = scr + grp * GE::SCR;
   const float* gf = gfp + sol * gf_sol_stride;
   const float* wt = wts + sol * w_sol_stride;
-  float cpot = 0.f;
 
-  for (int k = 0; k < tab.K; ++k) {
-    const float2* pr = prod + (((size_t)n * tab.K + k) * (N / 2) + r) * N;
+  // inverse row transform of kernel k's product spectrum -> potentials of
+  // rows (2r, 2r+1) at x = t + G*k1; counts them, writes them if requested
+  auto potential = [&](int k, bool count, float2 (&w)[P], float& cpot) {
+    const float2* pr = prod + (((size_t)n * K + k) * (N / 2) + r) * N;
     float2 v[Q][G];
-#pragma unroll
-    for (int jp = 0; jp < Q / 2; ++jp) {
-      const int m = t + G * jp;
-      if (m != 0) {
-#pragma unroll
-        for (int n2 = 0; n2 < G; ++n2) {
-          const int kx = m + P * n2, kk = N - kx;
-          float2 zk, zkk;
-          if (n2 < G / 2) {
-            float2 s1 = pr[kx], s2 = pr[kk];
-            zk = make_float2(s1.x - s2.y, s1.y + s2.x);
-            zkk = make_float2(s1.x + s2.y, s2.x - s1.y);
-          } else {
-            float2 s1 = pr[kk], s2 = pr[kx];
-            zkk = make_float2(s1.x - s2.y, s1.y + s2.x);
-            zk = make_float2(s1.x + s2.y, s2.x - s1.y);
-          }
-          v[2 * jp][n2] = zk;
-          v[2 * jp + 1][G - 1 - n2] = zkk;
-        }
-      } else {
-        float2 s0 = pr[0], sn = pr[N / 2];
-        v[2 * jp][0] = make_float2(s0.x, sn.x);
-        v[2 * jp][G / 2] = make_float2(s0.y, sn.y);
-#pragma unroll
-        for (int n2 = 1; n2 < G / 2; ++n2) {
-          const int kx = P * n2, kk = N - kx;
-          float2 s1 = pr[kx], s2 = pr[kk];
-          v[2 * jp][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
-          v[2 * jp][G - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
-        }
-#pragma unroll
-        for (int n2 = 0; n2 < G / 2; ++n2) {
-          const int kx = P / 2 + P * n2, kk = N - kx;
-          float2 s1 = pr[kx], s2 = pr[kk];
-          v[2 * jp + 1][n2] = make_float2(s1.x - s2.y, s1.y + s2.x);
-          v[2 * jp + 1][G - 1 - n2] = make_float2(s1.x + s2.y, s2.x - s1.y);
-        }
-      }
-    }
-    float2 w[P];
+    unpack_row_pair<GE>(pr, v, t);
     fft_mirrored<GE, true, true>(v, w, rs, sm + 2 * N, t, gmask);
-    const float gm = __ldg(gf + 2 * k), gs = __ldg(gf + 2 * k + 1);
-    const int gid = tab.gf[k];
-    if (pot_out) {
-      float* po = pot_out + ((size_t)n * tab.K + k) * N * N;
+    if (count) {
 #pragma unroll
-      for (int k1 = 0; k1 < P; ++k1) {
-        po[(2 * r) * N + t + G * k1] = w[k1].x;
-        po[(2 * r + 1) * N + t + G * k1] = w[k1].y;
+      for (int k1 = 0; k1 < P; ++k1) cpot += (w[k1].x > kEps ? 1.f : 0.f) + (w[k1].y > kEps ? 1.f : 0.f);
+      if (pot_out) {
+        float* po = pot_out + ((size_t)n * K + k) * N * N;
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+          po[(2 * r) * N + t + G * k1] = w[k1].x;
+          po[(2 * r + 1) * N + t + G * k1] = w[k1].y;
+        }
       }
     }
-#pragma unroll
-    for (int k1 = 0; k1 < P; ++k1) {
-      float2 g = make_float2(growth_fn(gid, w[k1].x, gm, gs), growth_fn(gid, w[k1].y, gm, gs));
-      cpot += (w[k1].x > kEps ? 1.f : 0.f) + (w[k1].y > kEps ? 1.f : 0.f);
-      w[k1] = g;
-    }
-    for (int co = 0; co < C; ++co) {
-      const float wk = __ldg(wt + co * tab.K + k);
-      if (wk == 0.f) continue;
-      float* fa = facc + (co * 2 * GPB + 2 * grp) * N;
-#pragma unroll
-      for (int k1 = 0; k1 < P; ++k1) {
-        const int x = t + G * k1;
-        fa[x] = fmaf(wk, w[k1].x, fa[x]);
-        fa[N + x] = fmaf(wk, w[k1].y, fa[N + x]);
-      }
-    }
-  }
+  };
 
-  // field, state update, moments
   float dt;
   if (tab.dt_mode == 0) dt = __ldg(dtp);
   else if (tab.dt_mode == 1) dt = __ldg(dtp + n);
   else dt = 1.f / __ldg(dtp + sol);
   const int sy = shift[3 * n], sx = shift[3 * n + 1];
-  float m00 = 0.f, g00 = 0.f, cmass = 0.f, cgrow = 0.f, mxy = 0.f, mxx = 0.f, gxy = 0.f, gxx = 0.f, m2y = 0.f,
-        m2x = 0.f;
+  float cpot = 0.f, m00 = 0.f, g00 = 0.f, cmass = 0.f, cgrow = 0.f, mxy = 0.f, mxx = 0.f, gxy = 0.f, gxx = 0.f,
+        m2y = 0.f, m2x = 0.f;
   bool border = false;
-  float cm_part[kMaxChannels];
-#pragma unroll
-  for (int i = 0; i < kMaxChannels; ++i) cm_part[i] = 0.f;
+  const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);
+  const float cyb = (float)(((2 * r + 1 - sy) & (N - 1)) - N / 2);
+
   for (int co = 0; co < C; ++co) {
-    float wsum = 0.f;
-    for (int k = 0; k < tab.K; ++k) wsum += __ldg(wt + co * tab.K + k);
-    const float* fa = facc + (co * 2 * GPB + 2 * grp) * N;
-    const size_t base = ((size_t)n * C + co) * N * N;
-    float cms = 0.f;
+    float2 acc[P];
 #pragma unroll
-    for (int e = 0; e < 2; ++e) {
-      const int y = 2 * r + e;
-      const float cy = (float)(((y - sy) & (N - 1)) - N / 2);
-#pragma unroll 4
+    for (int k1 = 0; k1 < P; ++k1) acc[k1] = make_float2(0.f, 0.f);
+    float wsum = 0.f;
+    for (int k = 0; k < K; ++k) {
+      const float wk = __ldg(wt + co * K + k);
+      wsum += wk;
+      if (wk == 0.f) continue;  // uniform over the block
+      bool first = true;
+      for (int c2 = 0; c2 < co; ++c2) first = first && (__ldg(wt + c2 * K + k) == 0.f);
+      float2 w[P];
+      potential(k, first, w, cpot);
+      GrowthP g;
+      g.m = __ldg(gf + 2 * k);
+      g.s = __ldg(gf + 2 * k + 1);
+      g.id = tab.gf[k];
+      g.a = GF == GF_FAST_GAUSSIAN ? 0.84932180028801904272f / g.s
+                                   : (GF == GF_FAST_POLY4 ? 1.f / (9.f * (g.s * g.s)) : 0.f);
+#pragma unroll
       for (int k1 = 0; k1 < P; ++k1) {
-        const int x = t + G * k1;
-        float f = fa[e * N + x];
-        if (tab.mean) f = f / wsum;
-        const float s = __ldg(state + base + y * N + x);
-        state_out[base + y * N + x] = state_fn(tab.state_fn, s, f, dt);
-        if (field_out) field_out[base + y * N + x] = f;
-        const float fp = fmaxf(f, 0.f);
-        const float cx = (float)(((x - sx) & (N - 1)) - N / 2);
-        m00 += s;
-        cms += s;
-        g00 += fp;
-        cmass += s > kEps ? 1.f : 0.f;
-        cgrow += fp > kEps ? 1.f : 0.f;
-        mxy = fmaf(s, cy, mxy);
-        mxx = fmaf(s, cx, mxx);
-        gxy = fmaf(fp, cy, gxy);
-        gxx = fmaf(fp, cx, gxx);
-        m2y = fmaf(s * cy, cy, m2y);
-        m2x = fmaf(s * cx, cx, m2x);
-        if ((x == 0 || x == N - 1 || y == 0 || y == N - 1) && s > kEps) border = true;
+        acc[k1].x = fmaf(wk, growth_cell<GF>(g, w[k1].x), acc[k1].x);
+        acc[k1].y = fmaf(wk, growth_cell<GF>(g, w[k1].y), acc[k1].y);
       }
     }
-    if (co < kMaxChannels) cm_part[co] = cms;
+    // field (weighted_sum / weighted_mean, core.py:202-242), state update, moments
+    const size_t base = ((size_t)n * C + co) * N * N;
+    const float* sa_row = state + base + (size_t)(2 * r) * N;
+    float* da_row = state_out + base + (size_t)(2 * r) * N;
+    float* fa_row = field_out ? field_out + base + (size_t)(2 * r) * N : nullptr;
+    float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f;
+#pragma unroll
+    for (int k1 = 0; k1 < P; ++k1) {
+      const int x = t + G * k1;
+      float fa = acc[k1].x, fb = acc[k1].y;
+      if (tab.mean) {
+        fa = fa / wsum;
+        fb = fb / wsum;
+      }
+      const float sa = __ldg(sa_row + x), sb = __ldg(sa_row + N + x);
+      da_row[x] = state_fn(tab.state_fn, sa, fa, dt);
+      da_row[N + x] = state_fn(tab.state_fn, sb, fb, dt);
+      if (fa_row) {
+        fa_row[x] = fa;
+        fa_row[N + x] = fb;
+      }
+      const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
+      const float cx = (float)(((x - sx) & (N - 1)) - N / 2);
+      Sa += sa;
+      Sb += sb;
+      Ga += fpa;
+      Gb += fpb;
+      const float ss = sa + sb, gg = fpa + fpb;
+      mxx = fmaf(ss, cx, mxx);
+      gxx = fmaf(gg, cx, gxx);
+      m2x = fmaf(ss * cx, cx, m2x);
+      const bool la = sa > kEps, lb = sb > kEps;
+      cmass += (la ? 1.f : 0.f) + (lb ? 1.f : 0.f);
+      cgrow += (fpa > kEps ? 1.f : 0.f) + (fpb > kEps ? 1.f : 0.f);
+      border |= ((x == 0 || x == N - 1) && (la || lb)) || (r == 0 && la) || (r == N / 2 - 1 && lb);
+    }
+    m00 += Sa + Sb;
+    g00 += Ga + Gb;
+    mxy += cya * Sa + cyb * Sb;
+    gxy += cya * Ga + cyb * Gb;
+    m2y += cya * cya * Sa + cyb * cyb * Sb;
+    const float cms = warp_sum(Sa + Sb);
+    if (lane == 0) red[wid * RAWS_MAX + RAW_CM + co] = cms;
+  }
+  // kernels that feed no channel still count in potential_volume
+  for (int k = 0; k < K; ++k) {
+    bool unused = true;
+    for (int c2 = 0; c2 < C; ++c2) unused = unused && (__ldg(wt + c2 * K + k) == 0.f);
+    if (!unused) continue;
+    float2 w[P];
+    potential(k, true, w, cpot);
   }
   // block reduction: warp shuffles then shared memory
-  float acc[12] = {m00, g00, cpot, cmass, cgrow, mxy, mxx, gxy, gxx, m2y, m2x, 0.f};
-  const int nwarps = blockDim.x >> 5;
+  float acc[11] = {m00, g00, cpot, cmass, cgrow, mxy, mxx, gxy, gxx, m2y, m2x};
 #pragma unroll
   for (int i = 0; i < 11; ++i) acc[i] = warp_sum(acc[i]);
   const bool anyb = __any_sync(0xffffffffu, border);
-  for (int co = 0; co < C; ++co) cm_part[co] = warp_sum(cm_part[co]);
   if (lane == 0) {
     float* rd = red + wid * RAWS_MAX;
     rd[RAW_M00] = acc[0];
@@ -358,13 +343,12 @@ __global__ void __launch_bounds__(128) row_inv_kernel(int n_worlds, int n_init, 
     rd[RAW_MX2 + 2] = 0.f;
     rd[RAW_BORDER] = anyb ? 1.f : 0.f;
     rd[RAW_SHIFT + 0] = rd[RAW_SHIFT + 1] = rd[RAW_SHIFT + 2] = 0.f;
-    for (int co = 0; co < C; ++co) rd[RAW_CM + co] = cm_part[co];
   }
   __syncthreads();
   const int RAWS = raw_stride(C);
   if (threadIdx.x < RAWS) {
     float s = 0.f;
-    for (int w = 0; w < nwarps; ++w) s += red[w * RAWS_MAX + threadIdx.x];
+    for (int w = 0; w < NWARPS; ++w) s += red[w * RAWS_MAX + threadIdx.x];
     if (threadIdx.x == RAW_BORDER) s = s > 0.f ? 1.f : 0.f;
     partial[((size_t)n * BPW + (blockIdx.x % BPW)) * RAWS + threadIdx.x] = s;
   }
@@ -431,11 +415,23 @@ __global__ void prepare_streamed_kernel(long n_planes, const float2* __restrict_
 }
 
 template <int N>
-size_t row_inv_smem(int C) {
+size_t row_inv_smem() {
   using RC = RowInvCfg<N>;
   using GE = Geo<N, RC::G>;
   return (size_t)3 * N * sizeof(float2) + (size_t)RC::GPB * GE::SCR * sizeof(float2) +
-         (size_t)C * 2 * RC::GPB * N * sizeof(float) + (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float);
+         (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float);
+}
+
+template <int N, int GF>
+cudaError_t launch_row_inv(const StreamedStep& s, const KTab& tab, cudaStream_t st) {
+  using RC = RowInvCfg<N>;
+  const size_t sm_inv = row_inv_smem<N>();
+  cudaError_t e = cudaFuncSetAttribute(row_inv_kernel<N, GF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_inv);
+  if (e != cudaSuccess) return e;
+  row_inv_kernel<N, GF><<<(unsigned)((long)s.n_worlds * RC::BPW), RC::T, sm_inv, st>>>(
+      s.n_worlds, s.n_init, tab, s.prod, s.gf, s.gf_sol_stride, s.w, s.w_sol_stride, s.dt, s.state, s.state_out,
+      s.field_out, s.pot_out, s.shift, s.partial);
+  return cudaGetLastError();
 }
 
 template <int N>
@@ -458,22 +454,29 @@ cudaError_t step_n(const StreamedStep& s, cudaStream_t st) {
     tab.gf[k] = m.gf[k];
   }
   const size_t sm_fwd = (size_t)3 * N * sizeof(float2) + (size_t)GPB * GE::SCR * sizeof(float2);
+  constexpr int CGPB = kColThreads / G;
+  constexpr int CBPP = (N / 2 + CGPB - 1) / CGPB;
+  const size_t sm_col = (size_t)3 * N * sizeof(float2) + (size_t)CGPB * GE::SCR * sizeof(float2) +
+                        (size_t)N * sizeof(float2);  // + DC / Nyquist mirror
   cudaError_t e;
   e = cudaFuncSetAttribute(row_fwd_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_fwd);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(col_conv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_fwd);
+  e = cudaFuncSetAttribute(col_conv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_col);
   if (e != cudaSuccess) return e;
   const long planes = (long)s.n_worlds * m.C;
   row_fwd_kernel<N><<<(unsigned)(planes * BPP), kThreads, sm_fwd, st>>>(s.n_worlds, m.C, s.state, s.spec);
-  col_conv_kernel<N><<<(unsigned)(planes * BPP), kThreads, sm_fwd, st>>>(s.n_worlds, s.n_init, tab, s.spec, s.kp,
+  col_conv_kernel<N><<<(unsigned)(planes * CBPP), kColThreads, sm_col, st>>>(s.n_worlds, s.n_init, tab, s.spec, s.kp,
                                                                            s.kp_sol_stride, s.prod);
   using RC = RowInvCfg<N>;
-  const size_t sm_inv = row_inv_smem<N>(m.C);
-  e = cudaFuncSetAttribute(row_inv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_inv);
+  bool all_gauss = true, all_poly = true;
+  for (int k = 0; k < m.K; ++k) {
+    all_gauss = all_gauss && m.gf[k] == LGX_GF_GAUSSIAN;
+    all_poly = all_poly && m.gf[k] == LGX_GF_POLY_QUAD4;
+  }
+  if (all_gauss) e = launch_row_inv<N, GF_FAST_GAUSSIAN>(s, tab, st);
+  else if (all_poly) e = launch_row_inv<N, GF_FAST_POLY4>(s, tab, st);
+  else e = launch_row_inv<N, GF_GENERIC>(s, tab, st);
   if (e != cudaSuccess) return e;
-  row_inv_kernel<N><<<(unsigned)((long)s.n_worlds * RC::BPW), RC::T, sm_inv, st>>>(
-      s.n_worlds, s.n_init, tab, s.prod, s.gf, s.gf_sol_stride, s.w, s.w_sol_stride, s.dt, s.state, s.state_out,
-      s.field_out, s.pot_out, s.shift, s.partial);
   const int wpb = 8;
   reduce_kernel<<<(s.n_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.n_worlds, s.n_init, RC::BPW, m.C, N, N,
                                                                   s.partial, s.raw, s.raw_sol_stride,
@@ -487,15 +490,7 @@ bool streamed_supported(const Model& m) {
   if (m.nb_dims != 2 || m.H != m.W) return false;
   if (m.C > kMaxChannels || m.K > kMaxKernels) return false;
   if (!(m.H == 32 || m.H == 64 || m.H == 128 || m.H == 256)) return false;
-  // row_inv keeps C field planes of its rows in shared memory
-  size_t smem = 0;
-  switch (m.H) {
-    case 32: smem = row_inv_smem<32>(m.C); break;
-    case 64: smem = row_inv_smem<64>(m.C); break;
-    case 128: smem = row_inv_smem<128>(m.C); break;
-    case 256: smem = row_inv_smem<256>(m.C); break;
-  }
-  return smem <= 227 * 1024;
+  return true;
 }
 
 int streamed_blocks_per_world(const Model& m) {
