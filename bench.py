@@ -140,14 +140,11 @@ def measured_peaks():
         return {}
 
 
-def committed_traffic():
-    """DRAM bytes per launch of the resident kernel from the committed ncu
-    summary (profiles/), scaled to this workload, or None."""
-    try:
-        d = json.load(open(os.path.join(ROOT, 'profiles', 'resident_traffic.json')))
-        return d.get('dram_bytes_per_launch_full_workload')
-    except Exception:
-        return None
+# DRAM bytes (read + write) of one resident_kernel launch of this workload,
+# from the ncu full-set capture summarised in profiles/resident_kernel_search1024.md:
+# 134.4 MB read + 92.2 MB written for 2048 worlds x 16 steps; state traffic
+# scaled to 1024 worlds plus the raw moments (19 floats per world-step) of 1024 steps.
+RESIDENT_TRAFFIC_BYTES = 191.7e6
 
 
 def run_ours(args, rank, world_size):
@@ -305,7 +302,7 @@ def run_ours(args, rank, world_size):
         'e2e': {'value': e2e_value, 'unit': METRIC, 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
         'roofline': {
             'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s', 'frac': achieved / fp32_peak,
-            'traffic': committed_traffic(), 'kernel': 'resident_kernel<128,8>', 'kernel_ms': kern_ms,
+            'traffic': RESIDENT_TRAFFIC_BYTES, 'kernel': 'resident_kernel<128,8>', 'kernel_ms': kern_ms,
             'flops_per_launch': flops_launch,
             'peak_source': 'measured in-bench (FFMA probe kernel, burst); MEASURED_PEAKS.json has no FP32 entry'
         },
@@ -483,22 +480,50 @@ def measure_uneven(dev, steps=256, reps=3):
 
 
 def profile_case(args):
-    """One warm-up plus one timed rollout of a reduced batch (same per-step work
-    per world and launch shape as the benchmark), for ncu captures."""
+    """Small cases for ncu captures: one warm-up and one timed run of the
+    named workload, nothing else.
+      resident     : the search batch (--profile-worlds worlds x 128x128 x --profile-steps steps)
+      multichannel : the multi-channel model on the streamed engine
+                     (--profile-worlds worlds x 256x256, C=3, K=15, --profile-steps steps)
+      uneven256 / uneven3d : --profile-worlds worlds of 256x256 / 64x64x64 in one uneven-batch launch
+                     (--profile-steps steps)"""
     import torch
     from leniax_gb300 import helpers, kernels, runner, statistics
     dev = torch.device('cuda', 0)
-    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, dev)
-    upd = helpers.build_update_fn(K.shape, mp)
-    stats_fn = statistics.ComputeStatsFn([SIZE, SIZE], R, T_RATE)
-    cells = torch.from_numpy(make_inputs(args.profile_worlds, seed=1)).to(dev)
-    gf, w, Tt = mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([T_RATE])
-    for _ in range(2):
-        sd, fin = runner.run_scan_mem_optimized(None, cells, K[None], gf, w, Tt, args.profile_steps, R, upd, stats_fn,
-                                                with_box=True, with_centroid=True)
+    name, nw, ns = args.profile_case, args.profile_worlds, args.profile_steps
+    if name == 'resident':
+        K, mp = kernels.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, dev)
+        upd = helpers.build_update_fn(K.shape, mp)
+        stats_fn = statistics.ComputeStatsFn([SIZE, SIZE], R, T_RATE)
+        cells = torch.from_numpy(make_inputs(nw, seed=1)).to(dev)
+        gf, w, Tt = mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([T_RATE])
+        for _ in range(2):
+            sd, fin = runner.run_scan_mem_optimized(None, cells, K[None], gf, w, Tt, ns, R, upd, stats_fn,
+                                                    with_box=True, with_centroid=True)
+        info = {'mean_N_box': float(sd['N_box'].mean())}
+    elif name == 'multichannel':
+        from leniax_gb300 import workloads
+        C, size, Rw, Tm = 3, 256, 20.0, 5.0
+        kp = workloads.multichannel_params(C, 5, seed=0, world_R=Rw)
+        K, mp = kernels.get_kernels_and_mapping([dict(p) for p in kp], [size, size], C, Rw, True, dev)
+        upd = helpers.build_update_fn(K.shape, mp, 'v1', True)
+        stats_fn = statistics.ComputeStatsFn([size, size], Rw, Tm)
+        cells = torch.from_numpy(workloads.multichannel_cells(nw, C, size, 64, seed=0)[None]).to(dev)
+        gf, w, Tt = mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([Tm])
+        for _ in range(2):
+            sd, fin = runner.run_scan_mem_optimized(None, cells, K[None], gf, w, Tt, ns, Rw, upd, stats_fn,
+                                                    engine='streamed', with_box=True)
+        info = {'mean_N': float(sd['N'].float().mean())}
+    else:
+        from leniax_gb300 import batch as lbatch
+        from leniax_gb300 import workloads
+        world = (256, 256) if name == 'uneven256' else (64, 64, 64)
+        b = lbatch.UnevenBatch(workloads.build_classes(mix=[(world, nw)], device=dev), ns)
+        for _ in range(2):
+            b.run()
+        info = {'mean_N_box': float(b.results()[0]['stats']['N_box'].mean())}
     torch.cuda.synchronize()
-    print(json.dumps({'profile_case': f'{args.profile_worlds} worlds x {args.profile_steps} steps',
-                      'mean_N_box': float(sd['N_box'].mean())}))
+    print(json.dumps({'profile_case': name, 'worlds': nw, 'steps': ns, **info}))
 
 
 def run_reference(args):
@@ -521,9 +546,10 @@ def main():
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--profile-case', action='store_true',
+    ap.add_argument('--profile-case', nargs='?', const='resident', default=None,
+                    choices=['resident', 'multichannel', 'uneven256', 'uneven3d'],
                     help='profiling case for ncu: one warm-up and one rollout of --profile-worlds worlds x '
-                         '--profile-steps Euler steps, nothing else')
+                         '--profile-steps Euler steps of the named workload, nothing else')
     ap.add_argument('--profile-worlds', type=int, default=2048)
     ap.add_argument('--profile-steps', type=int, default=16)
     args = ap.parse_args()
