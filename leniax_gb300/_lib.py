@@ -35,7 +35,7 @@ NSTAT_SCALAR = 11
 EXPORTED = (
     'lgx_version', 'lgx_last_error', 'lgx_plan_create', 'lgx_plan_destroy', 'lgx_select_engine',
     'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update', 'lgx_fp32_probe',
-    'lgx_batch_workspace_bytes', 'lgx_batch_run'
+    'lgx_batch_workspace_bytes', 'lgx_batch_run', 'lgx_workspace_status'
 )
 
 
@@ -122,12 +122,22 @@ def load():
         lib.lgx_update.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.c_void_p] * 5 + [ctypes.c_int] + \
             [ctypes.c_void_p] * 3 + [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
         lib.lgx_update.restype = ctypes.c_int
+        lib.lgx_workspace_status.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+        lib.lgx_workspace_status.restype = ctypes.c_int
         lib.lgx_fp32_probe.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         lib.lgx_fp32_probe.restype = ctypes.c_longlong
         if lib.lgx_version() != 1:
             raise RuntimeError('leniax_gb300 engine ABI version mismatch')
         _lib = lib
         return lib
+
+
+def workspace_status(ws_ptr: int, stream_handle: int) -> int:
+    """Device status word of the last call that used this workspace (0 = ok);
+    synchronises the stream."""
+    out = ctypes.c_int(0)
+    check(load().lgx_workspace_status(ws_ptr, stream_handle, ctypes.byref(out)))
+    return out.value
 
 
 def check(code):

@@ -71,8 +71,12 @@ int select_engine(const Model& m, int requested) {
   return -1;
 }
 
+// Every lgx_run / lgx_update workspace starts with a 256-byte status block
+// (first int: device status word, see lgx_workspace_status).
+constexpr size_t kStatusBytes = 256;
+
 size_t resident_ws(const Model& m, int n_sols, int n_init, int steps) {
-  size_t b = 0;
+  size_t b = kStatusBytes;
   b += al256((size_t)n_sols * m.H * resident_kpitch(m.H) * sizeof(float2));
   b += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
   return b;
@@ -80,7 +84,7 @@ size_t resident_ws(const Model& m, int n_sols, int n_init, int steps) {
 
 size_t streamed_ws(const Model& m, int n_sols, int n_init, int steps, bool with_raw) {
   const int nw = n_sols * n_init;
-  size_t b = streamed_workspace_bytes(m, nw, n_sols);
+  size_t b = kStatusBytes + streamed_workspace_bytes(m, nw, n_sols);
   b += 2 * al256((size_t)nw * m.C * m.cells * sizeof(float));  // state ping-pong
   if (with_raw) b += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
   return b;
@@ -89,8 +93,9 @@ size_t streamed_ws(const Model& m, int n_sols, int n_init, int steps, bool with_
 struct StreamedBufs {
   float2 *spec, *prod, *kp;
   float* partial;
-  int* shift;
+  int *shift, *status;
   float *sa, *sb, *raw;
+  size_t used;  // bytes of the layout
 };
 
 StreamedBufs carve_streamed(const Model& m, int n_sols, int n_init, int steps, void* ws, size_t ws_bytes,
@@ -98,6 +103,7 @@ StreamedBufs carve_streamed(const Model& m, int n_sols, int n_init, int steps, v
   Carve cv(ws, ws_bytes);
   const int nw = n_sols * n_init;
   StreamedBufs b;
+  b.status = cv.take<int>(kStatusBytes / sizeof(int));
   b.spec = cv.take<float2>((size_t)nw * m.C * m.cells / 2);
   b.prod = cv.take<float2>((size_t)nw * m.K * m.cells / 2);
   b.kp = cv.take<float2>((size_t)n_sols * m.C * m.max_k * m.H * (m.W / 2 + 2));
@@ -106,6 +112,7 @@ StreamedBufs carve_streamed(const Model& m, int n_sols, int n_init, int steps, v
   b.sa = cv.take<float>((size_t)nw * m.C * m.cells);
   b.sb = cv.take<float>((size_t)nw * m.C * m.cells);
   b.raw = with_raw ? cv.take<float>((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C)) : nullptr;
+  b.used = cv.off;
   return b;
 }
 
@@ -215,9 +222,12 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     if (j->n_box) cudaMemsetAsync(j->n_box, 0, (size_t)nw * sizeof(float), st);
     return LGX_OK;
   }
+  ce = cudaMemsetAsync(ws, 0, sizeof(int), st);  // status word
+  if (ce != cudaSuccess) return cuda_fail(ce, "memset");
   float* raw = nullptr;
   if (e == LGX_ENGINE_RESIDENT) {
     Carve cv(ws, ws_bytes);
+    cv.take<int>(kStatusBytes / sizeof(int));
     float2* kp = cv.take<float2>((size_t)j->n_sols * m.H * resident_kpitch(m.H));
     raw = cv.take<float>((size_t)j->n_sols * j->steps * j->n_init * raw_stride(m.C));
     ce = launch_prepare_resident_spectrum(m.H, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
@@ -249,6 +259,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     if (j->main_events[1]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[1]), st);
   } else {
     StreamedBufs b = carve_streamed(m, j->n_sols, j->n_init, j->steps, ws, ws_bytes, true);
+    if (b.used > ws_bytes) return fail(LGX_ERR_WORKSPACE, "lgx_run: internal workspace layout exceeds its size query");
     raw = b.raw;
     ce = launch_prepare_streamed_spectrum(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), b.kp, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
@@ -290,6 +301,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
         ss.spec = b.spec;
         ss.prod = b.prod;
         ss.partial = b.partial;
+        ss.status = b.status;
         ce = launch_streamed_step(ss, st);
         if (ce != cudaSuccess) return cuda_fail(ce, "streamed step");
       } else {
@@ -311,6 +323,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
           ss.spec = b.spec;
           ss.prod = b.prod;
           ss.partial = b.partial;
+          ss.status = b.status;
           ce = launch_streamed_step(ss, st);
           if (ce != cudaSuccess) return cuda_fail(ce, "plain step");
         }
@@ -347,8 +360,8 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
 size_t lgx_update_workspace_bytes(const lgx_plan* plan, int n) {
   if (!plan || n < 1) return 0;
   const Model& m = plan->m;
-  if (resident_supported(m)) return resident_ws(m, 1, n, 1) + al256(sizeof(float));
-  if (streamed_supported(m)) return streamed_ws(m, 1, n, 1, false) + al256((size_t)n * sizeof(float));
+  // lgx_update runs one streamed step for every model (resident sizes included)
+  if (streamed_supported(m)) return streamed_ws(m, 1, n, 1, false);
   return 0;
 }
 
@@ -368,6 +381,9 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
   if (!streamed_supported(m) && !resident_supported(m)) return fail(LGX_ERR_UNSUPPORTED, "lgx_update: unsupported");
   if (streamed_supported(m)) {
     StreamedBufs b = carve_streamed(m, 1, n, 1, ws, ws_bytes, false);
+    if (b.used > ws_bytes) return fail(LGX_ERR_WORKSPACE, "lgx_update: internal workspace layout exceeds its size query");
+    ce = cudaMemsetAsync(b.status, 0, sizeof(int), st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "memset");
     ce = launch_prepare_streamed_spectrum(m, 1, reinterpret_cast<const float2*>(k_half), b.kp, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
     ce = cudaMemsetAsync(b.shift, 0, (size_t)n * 3 * sizeof(int), st);
@@ -395,12 +411,22 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
     ss.spec = b.spec;
     ss.prod = b.prod;
     ss.partial = b.partial;
+    ss.status = b.status;
     ce = launch_streamed_step(ss, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "update step");
     g_err.clear();
     return LGX_OK;
   }
   return fail(LGX_ERR_UNSUPPORTED, "lgx_update: unsupported world size");
+}
+
+int lgx_workspace_status(const void* ws, void* stream, int* status) {
+  if (!ws || !status) return fail(LGX_ERR_INVALID, "lgx_workspace_status: null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t ce = cudaMemcpyAsync(status, ws, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+  if (ce != cudaSuccess) return cuda_fail(ce, "lgx_workspace_status");
+  return LGX_OK;
 }
 
 }  // extern "C"

@@ -139,6 +139,7 @@ struct StreamedStep {
   float2* spec;            // workspace [n_worlds, C, H/2, W] packed row spectra
   float2* prod;            // workspace [n_worlds, K, H/2, W] packed product spectra
   float* partial;          // workspace per-block raw partials
+  int* status;             // device status word (0 = ok; set when a staged copy times out), or null
 };
 cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st);
 cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,

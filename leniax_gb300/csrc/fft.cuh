@@ -323,4 +323,51 @@ __device__ __forceinline__ void unpack_row_pair(const float2* pr, float2 (&v)[GE
   }
 }
 
+// Row-inverse input of a packed row pair stored in the pair-adjacent layout:
+// pair j (one 16-byte float4) holds (slot j, slot N - j) of the packed row,
+// pair 0 holds (slot 0, slot N/2).  Same result as unpack_row_pair on the
+// plain layout, with one 16-byte load per (slot k, slot N - k).
+template <class GE>
+__device__ __forceinline__ void unpack_row_pair_pa(const float2* pr, float2 (&v)[GE::Q][GE::G], int t) {
+  constexpr int N = GE::N, G = GE::G, P = GE::P, Q = GE::Q;
+  const float4* p4 = reinterpret_cast<const float4*>(pr);
+#pragma unroll
+  for (int jp = 0; jp < Q / 2; ++jp) {
+    const int m = t + G * jp;
+    if (m != 0) {
+#pragma unroll
+      for (int n2 = 0; n2 < G; ++n2) {
+        const int kx = m + P * n2;
+        // s1 = slot min(kx, N-kx), s2 = slot max(kx, N-kx)
+        const float4 q = p4[n2 < G / 2 ? kx : N - kx];
+        const float2 a = make_float2(q.x - q.w, q.y + q.z);  // s1 + i s2
+        const float2 b = make_float2(q.x + q.w, q.z - q.y);  // conj(s1) + i conj(s2)
+        if (n2 < G / 2) {
+          v[2 * jp][n2] = a;
+          v[2 * jp + 1][G - 1 - n2] = b;
+        } else {
+          v[2 * jp][n2] = b;
+          v[2 * jp + 1][G - 1 - n2] = a;
+        }
+      }
+    } else {
+      const float4 q0 = p4[0];  // (slot 0, slot N/2)
+      v[2 * jp][0] = make_float2(q0.x, q0.z);
+      v[2 * jp][G / 2] = make_float2(q0.y, q0.w);
+#pragma unroll
+      for (int n2 = 1; n2 < G / 2; ++n2) {
+        const float4 q = p4[P * n2];
+        v[2 * jp][n2] = make_float2(q.x - q.w, q.y + q.z);
+        v[2 * jp][G - n2] = make_float2(q.x + q.w, q.z - q.y);
+      }
+#pragma unroll
+      for (int n2 = 0; n2 < G / 2; ++n2) {
+        const float4 q = p4[P / 2 + P * n2];
+        v[2 * jp + 1][n2] = make_float2(q.x - q.w, q.y + q.z);
+        v[2 * jp + 1][G - 1 - n2] = make_float2(q.x + q.w, q.z - q.y);
+      }
+    }
+  }
+}
+
 }  // namespace lgx

@@ -2,31 +2,40 @@
 // worlds): the spectra of a step travel through HBM/L2 between four kernels.
 //
 //   row_fwd  : per (world, channel, packed row) N-point FFT of rows (2r, 2r+1)
-//              packed as one complex row -> spec[n][c][r][k]
-//   col_conv : per (world, channel, column pair) unpack + N-point FFT, then for
-//              every kernel reading that channel: x prepared spectrum, inverse
-//              FFT -> prod[n][k] (packed rows layout)
-//   row_inv  : per (world, packed-row block) inverse row FFTs of all kernels ->
-//              potential, growth, weighted field (core.py:163-242), state
-//              update (core.py:245-319), per-block raw statistics moments
+//              packed as one complex row -> spec[n][c][r][.] in the
+//              pair-adjacent layout (pa_pos below)
+//   col_conv : per (world, channel, block of column pairs) the block's column
+//              tile arrives by TMA (2D tensor copies, 128-byte swizzle); per
+//              pair: unpack + N-point FFT, then for every kernel reading that
+//              channel: x prepared spectrum, inverse FFT -> prod[n][k] (same
+//              layout, 16-byte pair stores)
+//   row_inv  : per (world, block of packed rows) the block's rows of every
+//              kernel's product plane arrive by bulk copies into a double
+//              buffer (the next kernel's rows land while this kernel's are
+//              transformed); inverse row FFTs -> potential, growth, weighted
+//              field in registers (core.py:163-242), state update
+//              (core.py:245-319), per-block raw statistics moments
 //   reduce   : per world: block moments -> raw moments of the step, carried
 //              torus shift update (statistics.py:117-119)
 //
 // This is leniax core.update with get_potential_fft (core.py:52-102), the
 // true-kernel selection (tc_indices, core.py:97-98) being the (c_in, slot)
 // table of the plan.
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "engine.h"
 #include "fft.cuh"
+#include "tma.cuh"
 
 namespace lgx {
 
 namespace {
 
-constexpr int kThreads = 256;     // row_fwd blocks
-constexpr int kColThreads = 128;  // col_conv blocks (register-heavy: several blocks per SM)
+constexpr int kThreads = 256;  // row_fwd blocks
 
 struct KTab {  // per-plan kernel table, passed by value
   int C, K, max_k, mean, state_fn, dt_mode;
@@ -51,6 +60,17 @@ __device__ __forceinline__ float2* init_tw(float2* sm) {
   using GE = Geo<N, SCfg<N>::G>;
   init_twiddles<GE>(sm, sm + N, sm + 2 * N, threadIdx.x, blockDim.x);
   return sm + 3 * N;
+}
+
+// Pair-adjacent layout of a packed-row spectrum Z[0..N-1]: pair j (16 bytes)
+// holds (Z[j], Z[N-j]) for 0 < j < N/2 and pair 0 holds (Z[0], Z[N/2]).  The
+// column pass reads and writes whole pairs, and its tiles start on 16-byte
+// boundaries, as TMA requires.  After the column pass, pair j of packed row r
+// holds (column j at row 2r, column j at row 2r+1); pair 0 the DC and Nyquist
+// columns packed as DC + i Nyquist.
+template <int N>
+__host__ __device__ __forceinline__ int pa_pos(int k) {
+  return k == 0 ? 0 : (k == N / 2 ? 1 : (k < N / 2 ? 2 * k : 2 * (N - k) + 1));
 }
 
 // ------------------------------------------------------------------ row_fwd
@@ -81,33 +101,73 @@ __global__ void __launch_bounds__(kThreads) row_fwd_kernel(int n_worlds, int C, 
 #pragma unroll
   for (int q = 0; q < Q; ++q)
 #pragma unroll
-    for (int k1 = 0; k1 < G; ++k1) dst[t + G * q + P * k1] = u[q][k1];
+    for (int k1 = 0; k1 < G; ++k1) dst[pa_pos<N>(t + G * q + P * k1)] = u[q][k1];
 }
 
 // ----------------------------------------------------------------- col_conv
 template <int N>
-__global__ void __launch_bounds__(kColThreads) col_conv_kernel(int n_worlds, int n_init, KTab tab,
-                                                               const float2* __restrict__ spec,
+struct ColCfg {
+  static constexpr int G = SCfg<N>::G;
+  static constexpr int T = ((N / 2) * G < 128) ? (N / 2) * G : 128;  // threads per block
+  static constexpr int GPB = T / G;                // column pairs per block (one per group)
+  static constexpr int BPP = (N / 2) / GPB;        // blocks per plane
+  static constexpr int BOXES = GPB / 8;            // TMA boxes: 8 pairs (128 bytes) x N/2 rows
+  static constexpr int BOX_BYTES = (N / 2) * 128;
+  static constexpr int TILE_BYTES = BOXES * BOX_BYTES;
+  static_assert(GPB % 8 == 0 && (N / 2) % GPB == 0, "column tile");
+};
+
+template <int N>
+constexpr size_t col_conv_smem() {
+  using CC = ColCfg<N>;
+  using GE = Geo<N, CC::G>;
+  // 1024 bytes of alignment slack for the swizzled tile, tile, twiddles,
+  // group scratch, DC/Nyquist mirror, mbarrier
+  return 1024 + (size_t)CC::TILE_BYTES + (size_t)3 * N * sizeof(float2) + (size_t)CC::GPB * GE::SCR * sizeof(float2) +
+         (size_t)N * sizeof(float2) + 16;
+}
+
+template <int N>
+__global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_constant__ CUtensorMap spec_map,
+                                                               int n_worlds, int n_init, KTab tab,
                                                                const float2* __restrict__ kp, long kp_sol_stride,
-                                                               float2* __restrict__ prod) {
-  constexpr int G = SCfg<N>::G;
+                                                               float2* __restrict__ prod, int* __restrict__ status) {
+  using CC = ColCfg<N>;
+  constexpr int G = CC::G, GPB = CC::GPB, BPP = CC::BPP;
   using GE = Geo<N, G>;
-  constexpr int P = GE::P, Q = GE::Q, GPB = kColThreads / G;
-  constexpr int BPP = (N / 2 + GPB - 1) / GPB;
+  constexpr int P = GE::P, Q = GE::Q;
   constexpr int KPITCH = N / 2 + 2;
-  extern __shared__ __align__(16) float2 sm[];
-  float2* scr = init_tw<N>(sm);
-  __syncthreads();
+  extern __shared__ __align__(16) unsigned char smraw[];
+  unsigned char* tile = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
+  float2* sm = reinterpret_cast<float2*>(tile + CC::TILE_BYTES);
+  float2* scr = sm + 3 * N;
+  float2* mirror = scr + GPB * GE::SCR;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(mirror + N);
   const int plane = blockIdx.x / BPP;  // n*C + c
   if (plane >= n_worlds * tab.C) return;
+  const int j0 = (blockIdx.x % BPP) * GPB;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    fence_proxy_async();
+    mbar_arrive_expect_tx(bar, CC::TILE_BYTES);
+    for (int b = 0; b < CC::BOXES; ++b)
+      tma_load_2d(tile + b * CC::BOX_BYTES, &spec_map, (j0 + 8 * b) * 4, plane * (N / 2), bar);
+  }
+  init_twiddles<GE>(sm, sm + N, sm + 2 * N, threadIdx.x, blockDim.x);
+  __syncthreads();
+  if (__syncthreads_or(!mbar_wait(bar, 0))) {  // the tile never landed: record, drain, leave
+    if (threadIdx.x == 0 && status) atomicExch(status, kStatusCopyTimeout);
+    mbar_wait(bar, 0);
+    return;
+  }
   const int n = plane / tab.C, ch = plane % tab.C;
   const int sol = n / n_init;
   const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31;
-  const int c = (blockIdx.x % BPP) * GPB + grp;
-  if (c >= N / 2) return;
+  const int j = j0 + grp;  // column pair (j, N-j); j == 0 carries (0, N/2)
   const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
   float2* cs = scr + grp * GE::SCR;
-  const float2* sp = spec + (size_t)plane * (N / 2) * N;
+  const unsigned char* tb = tile + (grp >> 3) * CC::BOX_BYTES;
+  const int chunk = grp & 7;
 
   float2 v[Q][G];
 #pragma unroll
@@ -116,23 +176,21 @@ __global__ void __launch_bounds__(kColThreads) col_conv_kernel(int n_worlds, int
 #pragma unroll
     for (int n2 = 0; n2 < G; ++n2) {
       const int r = m + (P / 2) * n2;
-      if (c != 0) {
-        float2 z1 = sp[r * N + c], z2 = sp[r * N + N - c];
-        v[2 * jp][n2] = make_float2(z1.x + z2.x, z1.y - z2.y);
-        v[2 * jp + 1][n2] = make_float2(z1.y + z2.y, z2.x - z1.x);
+      const float4 q = *reinterpret_cast<const float4*>(tb + swz128(r, chunk));
+      if (j != 0) {
+        v[2 * jp][n2] = make_float2(q.x + q.z, q.y - q.w);      // 2 X[2r][j]
+        v[2 * jp + 1][n2] = make_float2(q.y + q.w, q.z - q.x);  // 2 X[2r+1][j]
       } else {
-        float2 z1 = sp[r * N], z2 = sp[r * N + N / 2];
-        v[2 * jp][n2] = make_float2(z1.x, z2.x);
-        v[2 * jp + 1][n2] = make_float2(z1.y, z2.y);
+        v[2 * jp][n2] = make_float2(q.x, q.z);  // X[2r][0] + i X[2r][N/2]
+        v[2 * jp + 1][n2] = make_float2(q.y, q.w);
       }
     }
   }
   float2 w0[P];
   fft_mirrored<GE, false, false>(v, w0, cs, sm + N, t, gmask);
-  // the packed DC / Nyquist column (c == 0, one group per plane) keeps its
-  // spectrum in the block's mirror buffer: Q[ky] needs A[-ky] for every kernel
-  float2* mirror = scr + GPB * GE::SCR;
-  if (c == 0) {
+  // the packed DC / Nyquist column keeps its spectrum in the block's mirror
+  // buffer: Q[ky] needs A[-ky] for every kernel
+  if (j == 0) {
 #pragma unroll
     for (int k1 = 0; k1 < P; ++k1) mirror[t + G * k1] = w0[k1];
     __syncwarp(gmask);
@@ -141,9 +199,9 @@ __global__ void __launch_bounds__(kColThreads) col_conv_kernel(int n_worlds, int
     if (tab.cin[k] != ch) continue;
     const float2* kk = kp + sol * kp_sol_stride + ((size_t)(ch * tab.max_k + tab.slot[k]) * N) * KPITCH;
     float2 w[P];
-    if (c != 0) {
+    if (j != 0) {
 #pragma unroll
-      for (int k1 = 0; k1 < P; ++k1) w[k1] = cmul(w0[k1], __ldg(kk + (t + G * k1) * KPITCH + c));
+      for (int k1 = 0; k1 < P; ++k1) w[k1] = cmul(w0[k1], __ldg(kk + (t + G * k1) * KPITCH + j));
     } else {
 #pragma unroll
       for (int k1 = 0; k1 < P; ++k1) {
@@ -154,83 +212,123 @@ __global__ void __launch_bounds__(kColThreads) col_conv_kernel(int n_worlds, int
     }
     float2 u[Q][G];
     fft_standard<GE, true, true>(w, u, cs, sm, t, gmask);
-    float2* pd = prod + ((size_t)n * tab.K + k) * (N / 2) * N;
+    float4* pd4 = reinterpret_cast<float4*>(prod + ((size_t)n * tab.K + k) * (N / 2) * N);
 #pragma unroll
-    for (int q = 0; q < Q; ++q) {
-      const int m = t + G * (q >> 1);
+    for (int a = 0; a < Q / 2; ++a) {
+      const int m = t + G * a;
 #pragma unroll
       for (int k1 = 0; k1 < G; ++k1) {
         const int r = m + (P / 2) * k1;
-        const int col = (c != 0) ? ((q & 1) ? N - c : c) : ((q & 1) ? N / 2 : 0);
-        pd[r * N + col] = u[q][k1];
+        pd4[(size_t)r * (N / 2) + j] = make_float4(u[2 * a][k1].x, u[2 * a][k1].y, u[2 * a + 1][k1].x,
+                                                   u[2 * a + 1][k1].y);
       }
     }
   }
 }
 
 // ------------------------------------------------------------------ row_inv
-// Block = GPB groups = GPB packed rows of one world.  Output channels are
-// processed one after the other; the weighted field of the current channel is
-// accumulated in registers (the row pair of a group: 2*P values per thread)
-// over the kernels that feed it.  A kernel feeding several channels is
-// inverse-transformed once per channel; its potential is counted (and
-// written) once, at the first channel it feeds; kernels that feed no channel
-// are transformed at the end for the potential count alone.
+// Block = GPB groups = GPB packed rows of one world.  Work items are the
+// (output channel, kernel) pairs with a nonzero weight, channel by channel,
+// then the kernels that feed no channel (their potentials still count in
+// potential_volume).  Item i's GPB product rows are bulk-copied into buffer
+// i & 1 (row pitch N + G) while item i-1 is transformed; after unpacking its
+// row, a group reuses that row as its FFT exchange scratch.  The weighted
+// field of the current channel stays in registers (2*P values per thread); a
+// kernel feeding several channels is transformed once per channel, its
+// potential counted (and written) at the first.
 template <int N>
 struct RowInvCfg {
   static constexpr int G = SCfg<N>::G;
   static constexpr int T = ((N / 2) * G < 128) ? (N / 2) * G : 128;  // threads per block
   static constexpr int GPB = T / G;
   static constexpr int BPW = (N / 2) / GPB;  // blocks per world
+  static constexpr int ROWP = N + G;         // staged row pitch (float2) == Geo<N, G>::SCR
+  static constexpr int BUF = GPB * ROWP;     // float2 per buffer
 };
+
+// item word: bit 16 = count the potential, bits 8..15 = output channel + 1 (0: none), bits 0..7 = kernel
+__device__ __forceinline__ int item_k(int it) { return it & 255; }
+__device__ __forceinline__ int item_co(int it) { return ((it >> 8) & 255) - 1; }
+__device__ __forceinline__ bool item_count(int it) { return (it >> 16) & 1; }
+
+template <int N>
+size_t row_inv_smem(int C, int K) {
+  using RC = RowInvCfg<N>;
+  return (size_t)2 * RC::BUF * sizeof(float2) + (size_t)3 * N * sizeof(float2) +
+         (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float) + 16 * sizeof(uint64_t) +
+         (size_t)kMaxChannels * sizeof(float) + (size_t)(C * K + K + 1) * sizeof(int);
+}
 
 template <int N, int GF>
 __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     int n_worlds, int n_init, KTab tab, const float2* __restrict__ prod, const float* __restrict__ gfp,
     long gf_sol_stride, const float* __restrict__ wts, long w_sol_stride, const float* __restrict__ dtp,
     const float* __restrict__ state, float* __restrict__ state_out, float* __restrict__ field_out,
-    float* __restrict__ pot_out, const int* __restrict__ shift, float* __restrict__ partial) {
+    float* __restrict__ pot_out, const int* __restrict__ shift, float* __restrict__ partial, int* __restrict__ status) {
   using RC = RowInvCfg<N>;
-  constexpr int G = RC::G, GPB = RC::GPB, BPW = RC::BPW;
+  constexpr int G = RC::G, GPB = RC::GPB, BPW = RC::BPW, ROWP = RC::ROWP;
   using GE = Geo<N, G>;
   constexpr int P = GE::P, Q = GE::Q;
   constexpr int RAWS_MAX = RAW_CM + kMaxChannels;
   constexpr int NWARPS = RC::T / 32;
+  static_assert(ROWP == GE::SCR, "a staged row doubles as the group's FFT scratch");
   extern __shared__ __align__(16) float2 sm[];
-  float2* scr = init_tw<N>(sm);                                   // GPB * SCR
-  float* red = reinterpret_cast<float*>(scr + GPB * GE::SCR);  // [warps][RAWS_MAX]
-  __syncthreads();
+  float2* bufs = sm;                    // [2][GPB][ROWP]
+  float2* tw = bufs + 2 * RC::BUF;      // 3N twiddles
+  float* red = reinterpret_cast<float*>(tw + 3 * N);  // [warps][RAWS_MAX]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(red + NWARPS * RAWS_MAX);  // 2 (16 slots reserved)
+  float* wsum_s = reinterpret_cast<float*>(bars + 16);                    // [kMaxChannels]
+  int* items = reinterpret_cast<int*>(wsum_s + kMaxChannels);
+  __shared__ int s_nitems;
+
   const int n = blockIdx.x / BPW;
   if (n >= n_worlds) return;
   const int sol = n / n_init;
   const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int r = (blockIdx.x % BPW) * GPB + grp;
+  const int r0 = (blockIdx.x % BPW) * GPB;
+  const int r = r0 + grp;
   const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
   const int C = tab.C, K = tab.K;
-  float2* rs = scr + grp * GE::SCR;
   const float* gf = gfp + sol * gf_sol_stride;
   const float* wt = wts + sol * w_sol_stride;
 
-  // inverse row transform of kernel k's product spectrum -> potentials of
-  // rows (2r, 2r+1) at x = t + G*k1; counts them, writes them if requested
-  auto potential = [&](int k, bool count, float2 (&w)[P], float& cpot) {
-    const float2* pr = prod + (((size_t)n * K + k) * (N / 2) + r) * N;
-    float2 v[Q][G];
-    unpack_row_pair<GE>(pr, v, t);
-    fft_mirrored<GE, true, true>(v, w, rs, sm + 2 * N, t, gmask);
-    if (count) {
-#pragma unroll
-      for (int k1 = 0; k1 < P; ++k1) cpot += (w[k1].x > kEps ? 1.f : 0.f) + (w[k1].y > kEps ? 1.f : 0.f);
-      if (pot_out) {
-        float* po = pot_out + ((size_t)n * K + k) * N * N;
-#pragma unroll
-        for (int k1 = 0; k1 < P; ++k1) {
-          po[(2 * r) * N + t + G * k1] = w[k1].x;
-          po[(2 * r + 1) * N + t + G * k1] = w[k1].y;
-        }
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], 1);
+    mbar_init(&bars[1], 1);
+    fence_proxy_async();
+    // work items and per-channel weight sums
+    int ni = 0;
+    unsigned long long seen = 0ull;
+    for (int co = 0; co < C; ++co) {
+      float ws = 0.f;
+      for (int k = 0; k < K; ++k) {
+        const float w = __ldg(wt + co * K + k);
+        ws += w;
+        if (w == 0.f) continue;
+        const bool first = !((seen >> k) & 1ull);
+        seen |= 1ull << k;
+        items[ni++] = (first ? (1 << 16) : 0) | ((co + 1) << 8) | k;
       }
+      wsum_s[co] = ws;
     }
+    for (int k = 0; k < K; ++k)
+      if (!((seen >> k) & 1ull)) items[ni++] = (1 << 16) | k;
+    s_nitems = ni;
+  }
+  init_twiddles<GE>(tw, tw + N, tw + 2 * N, threadIdx.x, blockDim.x);
+  __syncthreads();
+  const int nit = s_nitems;
+
+  // warp 0 stages item i's GPB product rows into buffer i & 1
+  auto issue = [&](int i) {
+    const int b = i & 1;
+    const float2* src = prod + (((size_t)n * K + item_k(items[i])) * (N / 2) + r0) * N;
+    float2* dst = bufs + b * RC::BUF;
+    if (lane == 0) mbar_arrive_expect_tx(&bars[b], (unsigned)(GPB * N * sizeof(float2)));
+    __syncwarp();
+    for (int g = lane; g < GPB; g += 32) bulk_load(dst + g * ROWP, src + (size_t)g * N, N * sizeof(float2), &bars[b]);
   };
+  if (wid == 0 && nit > 0) issue(0);
 
   float dt;
   if (tab.dt_mode == 0) dt = __ldg(dtp);
@@ -242,20 +340,44 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   bool border = false;
   const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);
   const float cyb = (float)(((2 * r + 1 - sy) & (N - 1)) - N / 2);
+  float2 acc[P];
+  bool failed = false;
+  int failed_at = 0;
 
-  for (int co = 0; co < C; ++co) {
-    float2 acc[P];
+  // item i: wait for its rows, inverse row transform, count / write the
+  // potential, accumulate the weighted growth of channel co (co >= 0)
+  auto process = [&](int i) {
+    __syncthreads();  // every group is done with buffer (i + 1) & 1 (item i - 1)
+    if (wid == 0 && i + 1 < nit) {
+      fence_proxy_async();
+      issue(i + 1);
+    }
+    if (__syncthreads_or(!mbar_wait(&bars[i & 1], (i >> 1) & 1))) {
+      failed = true;
+      failed_at = i;
+      return;
+    }
+    const int it = items[i], k = item_k(it), co = item_co(it);
+    float2* row = bufs + (i & 1) * RC::BUF + grp * ROWP;
+    float2 v[Q][G];
+    unpack_row_pair_pa<GE>(row, v, t);
+    __syncwarp(gmask);
+    float2 w[P];
+    fft_mirrored<GE, true, true>(v, w, row, tw + 2 * N, t, gmask);
+    if (item_count(it)) {
 #pragma unroll
-    for (int k1 = 0; k1 < P; ++k1) acc[k1] = make_float2(0.f, 0.f);
-    float wsum = 0.f;
-    for (int k = 0; k < K; ++k) {
+      for (int k1 = 0; k1 < P; ++k1) cpot += (w[k1].x > kEps ? 1.f : 0.f) + (w[k1].y > kEps ? 1.f : 0.f);
+      if (pot_out) {
+        float* po = pot_out + ((size_t)n * K + k) * N * N;
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+          po[(2 * r) * N + t + G * k1] = w[k1].x;
+          po[(2 * r + 1) * N + t + G * k1] = w[k1].y;
+        }
+      }
+    }
+    if (co >= 0) {
       const float wk = __ldg(wt + co * K + k);
-      wsum += wk;
-      if (wk == 0.f) continue;  // uniform over the block
-      bool first = true;
-      for (int c2 = 0; c2 < co; ++c2) first = first && (__ldg(wt + c2 * K + k) == 0.f);
-      float2 w[P];
-      potential(k, first, w, cpot);
       GrowthP g;
       g.m = __ldg(gf + 2 * k);
       g.s = __ldg(gf + 2 * k + 1);
@@ -268,7 +390,16 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
         acc[k1].y = fmaf(wk, growth_cell<GF>(g, w[k1].y), acc[k1].y);
       }
     }
+  };
+
+  int i = 0;
+  for (int co = 0; co < C && !failed; ++co) {
+#pragma unroll
+    for (int k1 = 0; k1 < P; ++k1) acc[k1] = make_float2(0.f, 0.f);
+    while (!failed && i < nit && item_co(items[i]) == co) process(i++);
+    if (failed) break;
     // field (weighted_sum / weighted_mean, core.py:202-242), state update, moments
+    const float wsum = wsum_s[co];
     const size_t base = ((size_t)n * C + co) * N * N;
     const float* sa_row = state + base + (size_t)(2 * r) * N;
     float* da_row = state_out + base + (size_t)(2 * r) * N;
@@ -312,34 +443,36 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     const float cms = warp_sum(Sa + Sb);
     if (lane == 0) red[wid * RAWS_MAX + RAW_CM + co] = cms;
   }
-  // kernels that feed no channel still count in potential_volume
-  for (int k = 0; k < K; ++k) {
-    bool unused = true;
-    for (int c2 = 0; c2 < C; ++c2) unused = unused && (__ldg(wt + c2 * K + k) == 0.f);
-    if (!unused) continue;
-    float2 w[P];
-    potential(k, true, w, cpot);
+  while (!failed && i < nit) process(i++);  // kernels that feed no channel
+  if (failed) {
+    // a staged copy never landed: record it, give the copies in flight a
+    // bounded time to drain, leave without writing moments
+    if (threadIdx.x == 0 && status) atomicExch(status, kStatusCopyTimeout);
+    const int f = failed_at;
+    mbar_wait(&bars[f & 1], (f >> 1) & 1);
+    if (f + 1 < nit) mbar_wait(&bars[(f + 1) & 1], ((f + 1) >> 1) & 1);
+    return;
   }
   // block reduction: warp shuffles then shared memory
-  float acc[11] = {m00, g00, cpot, cmass, cgrow, mxy, mxx, gxy, gxx, m2y, m2x};
+  float accm[11] = {m00, g00, cpot, cmass, cgrow, mxy, mxx, gxy, gxx, m2y, m2x};
 #pragma unroll
-  for (int i = 0; i < 11; ++i) acc[i] = warp_sum(acc[i]);
+  for (int q = 0; q < 11; ++q) accm[q] = warp_sum(accm[q]);
   const bool anyb = __any_sync(0xffffffffu, border);
   if (lane == 0) {
     float* rd = red + wid * RAWS_MAX;
-    rd[RAW_M00] = acc[0];
-    rd[RAW_G00] = acc[1];
-    rd[RAW_CNT_POT] = acc[2];
-    rd[RAW_CNT_MASS] = acc[3];
-    rd[RAW_CNT_GROW] = acc[4];
-    rd[RAW_MX + 0] = acc[5];
-    rd[RAW_MX + 1] = acc[6];
+    rd[RAW_M00] = accm[0];
+    rd[RAW_G00] = accm[1];
+    rd[RAW_CNT_POT] = accm[2];
+    rd[RAW_CNT_MASS] = accm[3];
+    rd[RAW_CNT_GROW] = accm[4];
+    rd[RAW_MX + 0] = accm[5];
+    rd[RAW_MX + 1] = accm[6];
     rd[RAW_MX + 2] = 0.f;
-    rd[RAW_GX + 0] = acc[7];
-    rd[RAW_GX + 1] = acc[8];
+    rd[RAW_GX + 0] = accm[7];
+    rd[RAW_GX + 1] = accm[8];
     rd[RAW_GX + 2] = 0.f;
-    rd[RAW_MX2 + 0] = acc[9];
-    rd[RAW_MX2 + 1] = acc[10];
+    rd[RAW_MX2 + 0] = accm[9];
+    rd[RAW_MX2 + 1] = accm[10];
     rd[RAW_MX2 + 2] = 0.f;
     rd[RAW_BORDER] = anyb ? 1.f : 0.f;
     rd[RAW_SHIFT + 0] = rd[RAW_SHIFT + 1] = rd[RAW_SHIFT + 2] = 0.f;
@@ -347,10 +480,10 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   __syncthreads();
   const int RAWS = raw_stride(C);
   if (threadIdx.x < RAWS) {
-    float s = 0.f;
-    for (int w = 0; w < NWARPS; ++w) s += red[w * RAWS_MAX + threadIdx.x];
-    if (threadIdx.x == RAW_BORDER) s = s > 0.f ? 1.f : 0.f;
-    partial[((size_t)n * BPW + (blockIdx.x % BPW)) * RAWS + threadIdx.x] = s;
+    float sum = 0.f;
+    for (int w = 0; w < NWARPS; ++w) sum += red[w * RAWS_MAX + threadIdx.x];
+    if (threadIdx.x == RAW_BORDER) sum = sum > 0.f ? 1.f : 0.f;
+    partial[((size_t)n * BPW + (blockIdx.x % BPW)) * RAWS + threadIdx.x] = sum;
   }
 }
 
@@ -414,24 +547,46 @@ __global__ void prepare_streamed_kernel(long n_planes, const float2* __restrict_
   }
 }
 
-template <int N>
-size_t row_inv_smem() {
-  using RC = RowInvCfg<N>;
-  using GE = Geo<N, RC::G>;
-  return (size_t)3 * N * sizeof(float2) + (size_t)RC::GPB * GE::SCR * sizeof(float2) +
-         (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float);
-}
-
 template <int N, int GF>
 cudaError_t launch_row_inv(const StreamedStep& s, const KTab& tab, cudaStream_t st) {
   using RC = RowInvCfg<N>;
-  const size_t sm_inv = row_inv_smem<N>();
+  const size_t sm_inv = row_inv_smem<N>(tab.C, tab.K);
   cudaError_t e = cudaFuncSetAttribute(row_inv_kernel<N, GF>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_inv);
   if (e != cudaSuccess) return e;
   row_inv_kernel<N, GF><<<(unsigned)((long)s.n_worlds * RC::BPW), RC::T, sm_inv, st>>>(
       s.n_worlds, s.n_init, tab, s.prod, s.gf, s.gf_sol_stride, s.w, s.w_sol_stride, s.dt, s.state, s.state_out,
-      s.field_out, s.pot_out, s.shift, s.partial);
+      s.field_out, s.pot_out, s.shift, s.partial, s.status);
   return cudaGetLastError();
+}
+
+// cuTensorMapEncodeTiled, fetched once from the driver through the runtime.
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static std::once_flag once;
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+// Tensor map of the packed spectrum planes seen as rows of 2N floats:
+// boxes of 32 floats (8 column pairs, 128 bytes) x N/2 packed rows,
+// 128-byte swizzle.
+template <int N>
+bool encode_spec_map(CUtensorMap* map, const float2* spec, long planes) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)(2 * N), (cuuint64_t)(planes * (N / 2))};
+  const cuuint64_t strides[1] = {(cuuint64_t)(2 * N * sizeof(float))};
+  const cuuint32_t box[2] = {32, (cuuint32_t)(N / 2)};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2*>(spec), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 template <int N>
@@ -454,19 +609,19 @@ cudaError_t step_n(const StreamedStep& s, cudaStream_t st) {
     tab.gf[k] = m.gf[k];
   }
   const size_t sm_fwd = (size_t)3 * N * sizeof(float2) + (size_t)GPB * GE::SCR * sizeof(float2);
-  constexpr int CGPB = kColThreads / G;
-  constexpr int CBPP = (N / 2 + CGPB - 1) / CGPB;
-  const size_t sm_col = (size_t)3 * N * sizeof(float2) + (size_t)CGPB * GE::SCR * sizeof(float2) +
-                        (size_t)N * sizeof(float2);  // + DC / Nyquist mirror
+  using CC = ColCfg<N>;
+  constexpr size_t sm_col = col_conv_smem<N>();
   cudaError_t e;
   e = cudaFuncSetAttribute(row_fwd_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_fwd);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(col_conv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_col);
   if (e != cudaSuccess) return e;
   const long planes = (long)s.n_worlds * m.C;
+  alignas(64) CUtensorMap spec_map;
+  if (!encode_spec_map<N>(&spec_map, s.spec, planes)) return cudaErrorInvalidValue;
   row_fwd_kernel<N><<<(unsigned)(planes * BPP), kThreads, sm_fwd, st>>>(s.n_worlds, m.C, s.state, s.spec);
-  col_conv_kernel<N><<<(unsigned)(planes * CBPP), kColThreads, sm_col, st>>>(s.n_worlds, s.n_init, tab, s.spec, s.kp,
-                                                                           s.kp_sol_stride, s.prod);
+  col_conv_kernel<N><<<(unsigned)(planes * CC::BPP), CC::T, sm_col, st>>>(spec_map, s.n_worlds, s.n_init, tab, s.kp,
+                                                                          s.kp_sol_stride, s.prod, s.status);
   using RC = RowInvCfg<N>;
   bool all_gauss = true, all_poly = true;
   for (int k = 0; k < m.K; ++k) {

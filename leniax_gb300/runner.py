@@ -18,7 +18,8 @@ from . import statistics as lstat
 
 
 def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, gf_params, w, T, max_run_iter,
-             keep_intermediary: bool, engine: str, with_box: bool, with_centroid: bool = False):
+             keep_intermediary: bool, engine: str, with_box: bool, with_centroid: bool = False,
+             check_status: bool = False):
     """cells0 [Ns, Ni, C, *world], K [Ns, C, max_k, *world(-half)], gf [Ns, K, 2], w [Ns, C, K], T [Ns]."""
     m = update_fn.model
     _require_cuda('cells0', cells0)
@@ -74,12 +75,16 @@ def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, g
     job.engine = eng
     job.centroid = cen.data_ptr() if (cen is not None and steps) else None
     _lib.check(lib.lgx_run(m.plan.handle, job, ws.data_ptr(), ws.numel(), _stream_handle(dev)))
+    if check_status:
+        code = _lib.workspace_status(ws.data_ptr(), _stream_handle(dev))
+        if code != 0:
+            raise _lib.LgxError(_lib.LGX_ERR_TIMEOUT, f'device status {code}: a staged copy did not complete')
     return final, stats, ncont, nbox, traj, cen
 
 
 def run_scan(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
              update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, engine: str = 'auto',
-             with_box: bool = False, with_centroid: bool = False):
+             with_box: bool = False, with_centroid: bool = False, check_status: bool = False):
     """runner.py:119-164.
 
     cells0 ``[N_init, C, *world]``; K ``[1, C, max_k, *world]`` complex64;
@@ -94,7 +99,7 @@ def run_scan(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_r
     m = update_fn.model
     final, stats, ncont, nbox, traj, cen = _rollout(update_fn, compute_stats_fn, cells0.unsqueeze(0), K.reshape(
         (1, ) + tuple(K.shape[1:])), gf_params.unsqueeze(0), kernels_weight_per_channel.unsqueeze(0), T, max_run_iter,
-                                                    True, engine, with_box, with_centroid)
+                                                    True, engine, with_box, with_centroid, check_status)
     sd = split_stats(stats[0], m.C)
     sd['N'] = ncont[0]
     if nbox is not None:
@@ -107,7 +112,7 @@ def run_scan(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_r
 
 def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
                            update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, engine: str = 'auto',
-                           with_box: bool = False, with_centroid: bool = False):
+                           with_box: bool = False, with_centroid: bool = False, check_status: bool = False):
     """runner.py:167-215: all solutions x inits in one engine launch.
 
     cells0 ``[N_sols, N_init, C, *world]``; K ``[N_sols, 1, C, max_k, *world]``;
@@ -115,13 +120,15 @@ def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_cha
     Returns ``(stats, final_cells)``: ``stats[k]`` ``[N_sols, T, N_init]``
     (``channel_mass`` ``[N_sols, T, N_init, C]``), ``stats['N']``
     ``[N_sols, N_init]``; ``final_cells`` ``[N_sols, N_init, C, *world]``.
+    ``check_status=True`` synchronises after the launch and raises if the
+    engine's device status word reports a staged copy that never landed.
     """
     m = update_fn.model
     Ns = cells0.shape[0]
     Kr = K.reshape((Ns, ) + tuple(K.shape[2:])) if K.dim() == 3 + len(m.world) + 1 else K
     final, stats, ncont, nbox, _, cen = _rollout(update_fn, compute_stats_fn, cells0, Kr, gf_params,
                                                  kernels_weight_per_channel, T, max_run_iter, False, engine, with_box,
-                                                 with_centroid)
+                                                 with_centroid, check_status)
     sd = split_stats(stats, m.C)
     sd['N'] = ncont
     if nbox is not None:

@@ -230,3 +230,26 @@ def test_trajectory_outputs_match_oracle(cuda):
             atol = 8 / 13.**2 if k.endswith('volume') or k.endswith('density') else 1e-4
             assert np.allclose(a, b, rtol=1e-4, atol=atol), (engine, k, np.abs(a - b).max())
         assert np.abs(st['N'].cpu().numpy() - st_o['N']).max() == 0
+
+
+@pytest.mark.parametrize('size', [32, 64, 128, 256])
+def test_streamed_multichannel_status_word_and_engines_agree(cuda, size):
+    # the staged (TMA / bulk) copies of the streamed engine all land: the
+    # workspace status word stays 0, and the multi-channel rollout matches the
+    # FP32 oracle step for step
+    dev = torch.device('cuda')
+    C, steps, R = 2, 6, size / 8
+    kp = random_multichannel_params(C, 2, seed=size, R_range=(size / 16, size / 8), world_R=R)
+    K, mp, upd = engine_model(kp, [size, size], C, R, dev=dev)
+    cells = np.zeros((1, 3, C, size, size), np.float32)
+    rng = np.random.Generator(np.random.PCG64(size))
+    lo, p = size // 4, size // 2
+    cells[..., lo:lo + p, lo:lo + p] = rng.random((1, 3, C, p, p), dtype=np.float32)
+    stats_fn = statistics.ComputeStatsFn([size, size], R, 5)
+    sd, fin = runner.run_scan_mem_optimized(None, torch.from_numpy(cells).to(dev), K[None], mp.get_gf_params(dev)[None],
+                                            mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([5.]), steps, R,
+                                            upd, stats_fn, engine='streamed', check_status=True)
+    Ko, mpo, model = oracle_model(kp, [size, size], C, R)
+    st, fo = O.run_scan(cells[0], Ko, mpo['gf_params'], mpo['weights'], 5., steps, R, model, keep_intermediary=False)
+    assert np.abs(fin[0].cpu().numpy() - fo).max() <= 1e-4
+    np.testing.assert_array_equal(sd['N'][0].cpu().numpy(), st['N'])
