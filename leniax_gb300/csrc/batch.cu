@@ -40,9 +40,32 @@ constexpr size_t big_smem() {
 }
 
 constexpr size_t cmax(size_t a, size_t b) { return a > b ? a : b; }
-constexpr size_t kWorkBytes = cmax(
-    cmax(cmax(resident_work_bytes<128, 8>(), resident_work_bytes<64, 4>()), resident_work_bytes<32, 4>()),
-    cmax(cmax(big_smem<256, 8>(), cmax(big_smem<64, 4>(), big_smem<64, 2>())), cmax(big_smem<32, 4>(), big_smem<32, 2>())));
+
+template <int N, int LG>
+struct Big3D {
+  static constexpr int G = 4;
+  using GE = Geo<N, G>;
+  using GZ = Geo<N, LG>;
+  static constexpr int HW = N / 2 + 1;
+  static constexpr int NT = (N / 2) * G;  // threads per plane slice
+  static constexpr int SL = 512 / NT;     // planes in flight
+  static constexpr int PITCH = N + G;
+  static constexpr int BUF = (N / 2) * PITCH, CSCR = (N / 2) * GE::SCR;
+  static constexpr int PLANES = SL * (BUF + CSCR);
+  static constexpr int ZSCR = (512 / LG) * GZ::SCR;
+  static constexpr int REGION = PLANES > ZSCR ? PLANES : ZSCR;  // float2, phases A/C and B share it
+  static_assert(NT % 32 == 0 && 512 % NT == 0 && N % SL == 0, "plane slices");
+};
+
+template <int N, int LG>
+constexpr size_t big3d_smem() {
+  return (size_t)Big3D<N, LG>::REGION * sizeof(float2) + kBigRed * sizeof(float);
+}
+
+constexpr size_t kWorkBytes =
+    cmax(cmax(cmax(resident_work_bytes<128, 8>(), resident_work_bytes<64, 4>()), resident_work_bytes<32, 4>()),
+         cmax(big_smem<256, 8>(), cmax(cmax(big3d_smem<64, 4>(), big3d_smem<64, 2>()),
+                                       cmax(big3d_smem<32, 4>(), big3d_smem<32, 2>()))));
 constexpr size_t kMixedSmem = (size_t)TW_END * sizeof(float2) + kWorkBytes;
 static_assert(kMixedSmem <= 227 * 1024, "mixed kernel shared memory");
 
@@ -228,16 +251,35 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
 }
 
 // ------------------------------------------------------------------ big 3D
-// Half spectrum X[z][y][kx], kx in [0, N/2], in the per-CTA scratch.
-template <int N, int G, int GF>
-__device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float2* tw_std, float2* work) {
-  using GE = Geo<N, G>;
-  constexpr int P = GE::P, Q = GE::Q, NG = 512 / G, HW = N / 2 + 1;
+// One N^3 world per CTA.  Per step:
+//   A. planes forward: the CTA is cut into SL slices of (N/2)*4 threads; each
+//      slice takes one z plane at a time through the resident engine's row
+//      and column passes in shared memory (row pairs packed as one complex
+//      row, column pairs unpacked) and writes the plane's true half spectrum
+//      X[z][ky][kx], kx in [0, N/2], to the per-CTA scratch (the packed
+//      DC / Nyquist column is split with its ky mirror);
+//   B. z pass over the scratch: lines (ky, kx) on groups of LG lanes, forward
+//      FFT, x prepared spectrum (scaled 1/N^3), inverse FFT;
+//   C. planes inverse: column inverse (DC and Nyquist columns re-packed as
+//      DC + i Nyquist), row inverse -> potential, growth, update, moments.
+template <int N, int LG, int GF>
+__device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float2* tw4, const float2* twz,
+                                        float2* work) {
+  using B3 = Big3D<N, LG>;
+  using GE = typename B3::GE;
+  using GZ = typename B3::GZ;
+  constexpr int G = B3::G, P = GE::P, Q = GE::Q, HW = B3::HW, NT = B3::NT, SL = B3::SL, PITCH = B3::PITCH;
+  constexpr int PZ = GZ::P, QZ = GZ::Q, NGZ = 512 / LG;
   constexpr size_t PLANE = (size_t)N * HW;
-  const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31;
+  const float2 *tw_std = tw4, *tw_colf = tw4 + N, *tw_rowi = tw4 + 2 * N;
+  const int sub = threadIdx.x / NT, tid = threadIdx.x % NT;
+  const int grp = tid / G, t = tid % G, lane = threadIdx.x & 31;
   const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
-  float2* scr = work + grp * GE::SCR;
-  float* red = reinterpret_cast<float*>(work + NG * GE::SCR);
+  const int bar_id = 1 + sub;
+  float2* buf = work + sub * (B3::BUF + B3::CSCR);
+  float2* cs = buf + B3::BUF + grp * GE::SCR;
+  float2* rowbuf = buf + grp * PITCH;
+  float* red = reinterpret_cast<float*>(work + B3::REGION);
   int* shv = reinterpret_cast<int*>(red + 16 * 16);
   float2* X = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;
   const float2* kp = a.kp + (size_t)world * N * PLANE;  // [N][N][HW], scaled by 1/N^3
@@ -247,128 +289,158 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
   const float wk = __ldg(a.w + world), wf = a.mean ? wk / wk : wk;
   const float dt = 1.f / __ldg(a.T + world);
   const int sizes[3] = {N, N, N};
+  const int c = grp;  // column pair of the column passes: (c, N-c); c == 0 carries (0, N/2)
+  const int c1 = c != 0 ? c : 0, c2 = c != 0 ? N - c : N / 2;
   if (threadIdx.x == 0) shv[0] = shv[1] = shv[2] = 0;
   __syncthreads();
   for (int step = 0; step < a.steps; ++step) {
     const float* src = step == 0 ? c0 : st;
-    // x pass: row pairs (z, 2r, 2r+1) -> half spectrum rows
-    for (int p = grp; p < N * (N / 2); p += NG) {
-      const int z = p / (N / 2), r = p % (N / 2);
-      const float* ra = src + ((size_t)z * N + 2 * r) * N;
-      float2 v[P];
+    // ---------------------------------------------------------- A. planes forward
+    for (int zb = 0; zb < N; zb += SL) {
+      const int z = zb + sub;
+      {
+        const float* pl = src + (size_t)z * N * N;
+        float2 v[P];
 #pragma unroll
-      for (int n2 = 0; n2 < P; ++n2) v[n2] = make_float2(ra[t + G * n2], ra[N + t + G * n2]);
-      float2 u[Q][G];
-      fft_standard<GE, false, false>(v, u, scr, tw_std, t, gmask);
+        for (int n2 = 0; n2 < P; ++n2)
+          v[n2] = make_float2(pl[(2 * grp) * N + t + G * n2], pl[(2 * grp + 1) * N + t + G * n2]);
+        float2 u[Q][G];
+        fft_standard<GE, false, false>(v, u, rowbuf, tw_std, t, gmask);
 #pragma unroll
-      for (int q = 0; q < Q; ++q)
+        for (int q = 0; q < Q; ++q)
 #pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) scr[t + G * q + P * k1] = u[q][k1];
-      __syncwarp(gmask);
-      float2* xa = X + ((size_t)z * N + 2 * r) * HW;
-      for (int kx = t; kx <= N / 2; kx += G) {
-        const float2 zk = scr[kx], zm = scr[(N - kx) & (N - 1)];
-        const float2 A = caddc(zk, zm), D = csubc(zk, zm);  // 2 X[2r], 2i X[2r+1]
-        xa[kx] = make_float2(0.5f * A.x, 0.5f * A.y);
-        xa[HW + kx] = make_float2(0.5f * D.y, -0.5f * D.x);
+          for (int k1 = 0; k1 < G; ++k1) rowbuf[t + G * q + P * k1] = u[q][k1];
       }
-      __syncwarp(gmask);
-    }
-    __syncthreads();
-    // y pass forward: lines (z, kx)
-    for (int l = grp; l < N * HW; l += NG) {
-      float2* base = X + (size_t)(l / HW) * PLANE + (l % HW);
-      float2 v[P];
+      named_bar(bar_id, NT);
+      {
+        float2 v[Q][G];
 #pragma unroll
-      for (int n2 = 0; n2 < P; ++n2) v[n2] = base[(size_t)(t + G * n2) * HW];
-      float2 u[Q][G];
-      fft_standard<GE, false, false>(v, u, scr, tw_std, t, gmask);
+        for (int jp = 0; jp < Q / 2; ++jp) {
+          const int m = t + G * jp;
 #pragma unroll
-      for (int q = 0; q < Q; ++q)
-#pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) base[(size_t)(t + G * q + P * k1) * HW] = u[q][k1];
-    }
-    __syncthreads();
-    // z pass: forward, x prepared spectrum, inverse
-    for (int l = grp; l < N * HW; l += NG) {
-      float2* base = X + l;  // l = ky * HW + kx
-      const float2* kb = kp + l;
-      float2 v[P];
-#pragma unroll
-      for (int n2 = 0; n2 < P; ++n2) v[n2] = base[(size_t)(t + G * n2) * PLANE];
-      float2 u[Q][G];
-      fft_standard<GE, false, false>(v, u, scr, tw_std, t, gmask);
-#pragma unroll
-      for (int q = 0; q < Q; ++q)
-#pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) {
-          const int kz = t + G * q + P * k1;
-          u[q][k1] = cmul(u[q][k1], __ldg(kb + (size_t)kz * PLANE));
+          for (int n2 = 0; n2 < G; ++n2) {
+            const int rr = m + (P / 2) * n2;
+            const float2 z1 = buf[rr * PITCH + c1], z2 = buf[rr * PITCH + c2];
+            if (c != 0) {
+              v[2 * jp][n2] = caddc(z1, z2);  // 2 X[2rr][c]
+              const float2 d = csubc(z1, z2);  // 2i X[2rr+1][c]
+              v[2 * jp + 1][n2] = make_float2(d.y, -d.x);
+            } else {
+              v[2 * jp][n2] = make_float2(z1.x, z2.x);
+              v[2 * jp + 1][n2] = make_float2(z1.y, z2.y);
+            }
+          }
         }
+        float2 w[P];
+        fft_mirrored<GE, false, false>(v, w, cs, tw_colf, t, gmask);  // w[k1]: ky = t + G*k1
+        float2* xz = X + (size_t)z * PLANE;
+        if (c != 0) {
 #pragma unroll
-      for (int q = 0; q < Q; ++q)
+          for (int k1 = 0; k1 < P; ++k1) xz[(t + G * k1) * HW + c] = make_float2(0.5f * w[k1].x, 0.5f * w[k1].y);
+        } else {
+          // w = X0 + i XN (x-DC and x-Nyquist columns); X0[ky] = (w[ky] + conj w[-ky]) / 2,
+          // XN[ky] = -i (w[ky] - conj w[-ky]) / 2
 #pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) scr[t + G * q + P * k1] = u[q][k1];
-      __syncwarp(gmask);
+          for (int k1 = 0; k1 < P; ++k1) cs[t + G * k1] = w[k1];
+          __syncwarp(gmask);
 #pragma unroll
-      for (int n2 = 0; n2 < P; ++n2) v[n2] = scr[t + G * n2];
-      __syncwarp(gmask);
-      fft_standard<GE, true, false>(v, u, scr, tw_std, t, gmask);
-#pragma unroll
-      for (int q = 0; q < Q; ++q)
-#pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) base[(size_t)(t + G * q + P * k1) * PLANE] = u[q][k1];
+          for (int k1 = 0; k1 < P; ++k1) {
+            const int ky = t + G * k1;
+            const float2 mr = cs[(N - ky) & (N - 1)];
+            xz[ky * HW] = make_float2(0.5f * (w[k1].x + mr.x), 0.5f * (w[k1].y - mr.y));
+            xz[ky * HW + N / 2] = make_float2(0.5f * (w[k1].y + mr.y), -0.5f * (w[k1].x - mr.x));
+          }
+          __syncwarp(gmask);
+        }
+      }
+      named_bar(bar_id, NT);
     }
     __syncthreads();
-    // y pass inverse
-    for (int l = grp; l < N * HW; l += NG) {
-      float2* base = X + (size_t)(l / HW) * PLANE + (l % HW);
-      float2 v[P];
+    // ---------------------------------------------------------- B. z pass
+    {
+      const int zg = threadIdx.x / LG, zt = threadIdx.x % LG;
+      const unsigned zmask = ((1u << LG) - 1u) << (lane & ~(LG - 1));
+      float2* zs = work + zg * GZ::SCR;
+      for (int l = zg; l < N * HW; l += NGZ) {
+        float2* base = X + l;  // l = ky * HW + kx
+        const float2* kb = kp + l;
+        float2 v[PZ];
 #pragma unroll
-      for (int n2 = 0; n2 < P; ++n2) v[n2] = base[(size_t)(t + G * n2) * HW];
-      float2 u[Q][G];
-      fft_standard<GE, true, false>(v, u, scr, tw_std, t, gmask);
+        for (int n2 = 0; n2 < PZ; ++n2) v[n2] = base[(size_t)(zt + LG * n2) * PLANE];
+        float2 u[QZ][LG];
+        fft_standard<GZ, false, false>(v, u, zs, twz, zt, zmask);
 #pragma unroll
-      for (int q = 0; q < Q; ++q)
+        for (int q = 0; q < QZ; ++q)
 #pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) base[(size_t)(t + G * q + P * k1) * HW] = u[q][k1];
+          for (int k1 = 0; k1 < LG; ++k1) {
+            const int kz = zt + LG * q + PZ * k1;
+            u[q][k1] = cmul(u[q][k1], __ldg(kb + (size_t)kz * PLANE));
+          }
+#pragma unroll
+        for (int q = 0; q < QZ; ++q)
+#pragma unroll
+          for (int k1 = 0; k1 < LG; ++k1) zs[zt + LG * q + PZ * k1] = u[q][k1];
+        __syncwarp(zmask);
+#pragma unroll
+        for (int n2 = 0; n2 < PZ; ++n2) v[n2] = zs[zt + LG * n2];
+        __syncwarp(zmask);
+        fft_standard<GZ, true, false>(v, u, zs, twz, zt, zmask);
+#pragma unroll
+        for (int q = 0; q < QZ; ++q)
+#pragma unroll
+          for (int k1 = 0; k1 < LG; ++k1) base[(size_t)(zt + LG * q + PZ * k1) * PLANE] = u[q][k1];
+      }
     }
     __syncthreads();
-    // x inverse, growth, update, moments
+    // ---------------------------------------------------------- C. planes inverse
     float acc[14];
 #pragma unroll
     for (int i = 0; i < 14; ++i) acc[i] = 0.f;
     bool border = false;
     const int sz = shv[0], sy = shv[1], sx = shv[2];
-    for (int p = grp; p < N * (N / 2); p += NG) {
-      const int z = p / (N / 2), r = p % (N / 2);
-      const float2* xa = X + ((size_t)z * N + 2 * r) * HW;
-      float2 v[P];
+    for (int zb = 0; zb < N; zb += SL) {
+      const int z = zb + sub;
+      {
+        const float2* xz = X + (size_t)z * PLANE;
+        float2 w[P];
 #pragma unroll
-      for (int n2 = 0; n2 < P; ++n2) {
-        const int n = t + G * n2;
-        if (n <= N / 2) {
-          const float2 A = xa[n], B = xa[HW + n];
-          v[n2] = make_float2(A.x - B.y, A.y + B.x);  // A + iB
-        } else {
-          const float2 A = xa[N - n], B = xa[HW + N - n];
-          v[n2] = make_float2(A.x + B.y, B.x - A.y);  // conj(A) + i conj(B)
+        for (int k1 = 0; k1 < P; ++k1) {
+          const int ky = t + G * k1;
+          if (c != 0) {
+            w[k1] = xz[ky * HW + c];
+          } else {
+            const float2 a0 = xz[ky * HW], an = xz[ky * HW + N / 2];
+            w[k1] = make_float2(a0.x - an.y, a0.y + an.x);  // DC + i Nyquist
+          }
+        }
+        float2 u[Q][G];
+        fft_standard<GE, true, true>(w, u, cs, tw_std, t, gmask);
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+          const int m = t + G * (q >> 1);
+          const int col = (q & 1) ? c2 : c1;
+#pragma unroll
+          for (int k1 = 0; k1 < G; ++k1) buf[(m + (P / 2) * k1) * PITCH + col] = u[q][k1];
         }
       }
-      float2 u[Q][G];
-      fft_standard<GE, true, false>(v, u, scr, tw_std, t, gmask);
-      const float cz = (float)(((z - sz) & (N - 1)) - N / 2);
-      const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);
-      const float cyb = (float)(((2 * r + 1 - sy) & (N - 1)) - N / 2);
-      const float* sra = src + ((size_t)z * N + 2 * r) * N;
-      float* dsa = st + ((size_t)z * N + 2 * r) * N;
-      float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f;
+      named_bar(bar_id, NT);
+      {
+        const int r = grp;
+        float2 v[Q][G];
+        unpack_row_pair<GE>(rowbuf, v, t);
+        __syncwarp(gmask);
+        float2 w[P];
+        fft_mirrored<GE, true, true>(v, w, rowbuf, tw_rowi, t, gmask);  // w[k1]: x = t + G*k1
+        const float cz = (float)(((z - sz) & (N - 1)) - N / 2);
+        const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);
+        const float cyb = (float)(((2 * r + 1 - sy) & (N - 1)) - N / 2);
+        const float* sra = src + ((size_t)z * N + 2 * r) * N;
+        float* dsa = st + ((size_t)z * N + 2 * r) * N;
+        float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f;
 #pragma unroll
-      for (int q = 0; q < Q; ++q)
-#pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) {
-          const int x = t + G * q + P * k1;
-          const float pa = u[q][k1].x, pb = u[q][k1].y;
+        for (int k1 = 0; k1 < P; ++k1) {
+          const int x = t + G * k1;
+          const float pa = w[k1].x, pb = w[k1].y;
           const float sa = sra[x], sb = sra[N + x];
           const float fa = growth_cell<GF>(gq, pa) * wf, fb = growth_cell<GF>(gq, pb) * wf;
           dsa[x] = state_fn(a.state_fn, sa, fa, dt);
@@ -390,15 +462,17 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
           border |= ((x == 0 || x == N - 1 || z == 0 || z == N - 1) && (la || lb)) || (r == 0 && la) ||
                     (r == N / 2 - 1 && lb);
         }
-      const float S = Sa + Sb, Gs = Ga + Gb;
-      acc[RAW_M00] += S;
-      acc[RAW_G00] += Gs;
-      acc[RAW_MX + 0] += cz * S;
-      acc[RAW_GX + 0] += cz * Gs;
-      acc[RAW_MX2 + 0] += cz * cz * S;
-      acc[RAW_MX + 1] += cya * Sa + cyb * Sb;
-      acc[RAW_GX + 1] += cya * Ga + cyb * Gb;
-      acc[RAW_MX2 + 1] += cya * cya * Sa + cyb * cyb * Sb;
+        const float S = Sa + Sb, Gs = Ga + Gb;
+        acc[RAW_M00] += S;
+        acc[RAW_G00] += Gs;
+        acc[RAW_MX + 0] += cz * S;
+        acc[RAW_GX + 0] += cz * Gs;
+        acc[RAW_MX2 + 0] += cz * cz * S;
+        acc[RAW_MX + 1] += cya * Sa + cyb * Sb;
+        acc[RAW_GX + 1] += cya * Ga + cyb * Gb;
+        acc[RAW_MX2 + 1] += cya * cya * Sa + cyb * cyb * Sb;
+      }
+      named_bar(bar_id, NT);
     }
     big_finish_step(a, world, step, 3, sizes, acc, border, red, shv);
   }
@@ -418,12 +492,12 @@ __device__ __forceinline__ void dispatch_gf(const BatchClassArgs& c, int item, f
     case BK_R128: resident_item_call<128, 8, GF>(c.r, item, sm + TW128, work); break;
     case BK_B2D256: big2d_item<256, GF>(c.b, item, sm + TW256, work); break;
     case BK_B3D32:
-      if (c.line_group == 2) big3d_item<32, 2, GF>(c.b, item, sm + TW32G2, work);
-      else big3d_item<32, 4, GF>(c.b, item, sm + TW32, work);
+      if (c.line_group == 2) big3d_item<32, 2, GF>(c.b, item, sm + TW32, sm + TW32G2, work);
+      else big3d_item<32, 4, GF>(c.b, item, sm + TW32, sm + TW32, work);
       break;
     case BK_B3D64:
-      if (c.line_group == 2) big3d_item<64, 2, GF>(c.b, item, sm + TW64G2, work);
-      else big3d_item<64, 4, GF>(c.b, item, sm + TW64, work);
+      if (c.line_group == 2) big3d_item<64, 2, GF>(c.b, item, sm + TW64, sm + TW64G2, work);
+      else big3d_item<64, 4, GF>(c.b, item, sm + TW64, sm + TW64, work);
       break;
   }
 }
