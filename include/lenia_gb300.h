@@ -260,6 +260,42 @@ LGX_API int lgx_run_noalloc(const lgx_plan* plan, const lgx_rollout* job, void* 
 LGX_API const char* lgx_noalloc_last_error(void);
 
 /* ---------------------------------------------------------------------------
+ * Ring kernels built on the device, a batch at a time: leniax's circle_2d
+ * (kernels.py:176-212) with the kernel_functions registry, placed and
+ * fftshifted as get_kernels_and_mapping does (kernels.py:66-158), each with its
+ * own R, r, ring weights and kernel-function parameters; optionally their
+ * Hermitian half spectra.  r R is formed in double precision and rounded to
+ * float, as leniax forms it from Python floats.
+ * ------------------------------------------------------------------------- */
+#define LGX_KF_POLY_QUAD 0
+#define LGX_KF_GAUSS_BUMP 1
+#define LGX_KF_STEP 2
+#define LGX_KF_GAUSS 3
+#define LGX_KF_THRESHOLD 4
+#define LGX_KF_STAIRCASE 5
+#define LGX_KF_TRIANGLE 6
+
+typedef struct lgx_ring_batch {
+  int nb_dims;  /* 2 or 3 */
+  int size;     /* world side: 2D 32..256, 3D 32/64 */
+  int n;        /* kernels */
+  int kf_id;    /* LGX_KF_* */
+  int nb_max;   /* row length of b */
+  const float* R;         /* [n] world radius */
+  const float* r;         /* [n] relative kernel radius (k_params[0]) */
+  const float* b;         /* [n, nb_max] ring weights (k_params[1], zero-padded) */
+  const int* nb;          /* [n] ring counts, 1..nb_max */
+  const float* kf_params; /* [n, 2] kernel-function parameters (the second only for staircase / triangle) */
+  float* kernel_out;      /* [n, size^nb_dims] normalised, fftshifted real kernels */
+  float* k_half;          /* [n, size^(nb_dims-1), size/2+1] complex64 half spectra, or NULL */
+  int* status;            /* device int, set to 1 if a kernel box (2 ceil(r R) cells) exceeds the
+                             world or a ring count is out of range (that kernel is left zero) */
+} lgx_ring_batch;
+
+LGX_API int lgx_ring_kernels_workspace_bytes(const lgx_ring_batch* job, size_t* bytes);
+LGX_API int lgx_ring_kernels(const lgx_ring_batch* job, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Uneven batch: thousands of worlds of different sizes, dimensions, kernels,
  * growth parameters and time steps in ONE persistent launch.  Replaces
  * leniax's vmap over identically shaped worlds (leniax/runner.py:167-215,

@@ -35,7 +35,8 @@ NSTAT_SCALAR = 11
 EXPORTED = (
     'lgx_version', 'lgx_last_error', 'lgx_plan_create', 'lgx_plan_destroy', 'lgx_select_engine',
     'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update', 'lgx_fp32_probe',
-    'lgx_batch_workspace_bytes', 'lgx_batch_run', 'lgx_workspace_status'
+    'lgx_batch_workspace_bytes', 'lgx_batch_run', 'lgx_workspace_status', 'lgx_ring_kernels_workspace_bytes',
+    'lgx_ring_kernels'
 )
 
 

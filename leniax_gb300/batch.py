@@ -93,19 +93,18 @@ class WorldClass:
 
 def world_spectra(world: Sequence[int], R: Sequence[float], kernel_params: Dict, device=None) -> torch.Tensor:
     """Per-world kernel spectra ``[n, *world[:-1], W//2+1]`` complex64 for
-    one ring-kernel recipe at per-world radii ``R`` (leniax builds one kernel
-    per R, kernels.py:66-158; worlds sharing an R share its spectrum)."""
-    world = [int(w) for w in world]
-    R = [float(r) for r in R]
-    uniq = sorted(set(R))
-    index = {r: i for i, r in enumerate(uniq)}
-    specs = []
-    for r in uniq:
-        K, _ = lkernels.get_kernels_and_mapping([dict(kernel_params)], world, 1, r, True, device)
-        specs.append(K[0, 0, 0, ..., :world[-1] // 2 + 1])
-    stack = torch.stack(specs)
-    idx = torch.tensor([index[r] for r in R], device=stack.device)
-    return stack.index_select(0, idx).contiguous()
+    one ring-kernel recipe (a leniax kernels_params entry: ``k_params`` [r,
+    b], ``kf_slug``, ``kf_params``) at per-world radii ``R``, built on the GPU
+    by :func:`leniax_gb300.kernels.ring_kernels` (kernels.py:66-212 per
+    world)."""
+    kp = kernel_params
+    if kp.get('k_slug', 'circle_2d') != 'circle_2d':
+        raise ValueError('world_spectra builds circle_2d ring kernels only')
+    r, b = kp['k_params'][0], kp['k_params'][1]
+    n = len(R)
+    _, K = lkernels.ring_kernels(world, list(R), [r] * n, [list(b)] * n, kp['kf_slug'], list(kp['kf_params']),
+                                 spectrum=True, device=device)
+    return K
 
 
 def _half(K: torch.Tensor, world) -> torch.Tensor:

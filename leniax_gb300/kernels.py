@@ -194,3 +194,87 @@ def get_kernels_and_mapping(kernels_params: List[Dict], world_size: Sequence[int
     K = np.fft.fftshift(K, axes=axes)
     K = np.fft.fftn(K.astype(np.complex64), axes=axes).astype(np.complex64)
     return torch.from_numpy(np.ascontiguousarray(K)).to(device), mapping
+
+
+# ---------------------------------------------------------------- device builder
+KF_IDS = {'poly_quad': 0, 'gauss_bump': 1, 'step': 2, 'gauss': 3, 'threshold': 4, 'staircase': 5, 'triangle': 6}
+
+
+class RingBatchC:
+    """ctypes mirror of ``lgx_ring_batch`` (built lazily with the library)."""
+    _cls = None
+
+    @classmethod
+    def get(cls):
+        if cls._cls is None:
+            import ctypes
+
+            class _C(ctypes.Structure):
+                _fields_ = [('nb_dims', ctypes.c_int), ('size', ctypes.c_int), ('n', ctypes.c_int),
+                            ('kf_id', ctypes.c_int), ('nb_max', ctypes.c_int), ('R', ctypes.c_void_p),
+                            ('r', ctypes.c_void_p), ('b', ctypes.c_void_p), ('nb', ctypes.c_void_p),
+                            ('kf_params', ctypes.c_void_p), ('kernel_out', ctypes.c_void_p),
+                            ('k_half', ctypes.c_void_p), ('status', ctypes.c_void_p)]
+
+            cls._cls = _C
+        return cls._cls
+
+
+def ring_kernels(world: Sequence[int], R, r, b, kf_slug: str, kf_params, spectrum: bool = True, device=None):
+    """Ring kernels of ``circle_2d`` (kernels.py:176-212) built on the GPU for
+    a batch of worlds, each with its own radius ``R[i]``, relative radius
+    ``r[i]``, ring weights ``b[i]`` (list) and kernel-function parameters
+    ``kf_params[i]``; placed and fftshifted on the world grid as
+    ``get_kernels_and_mapping`` does.  Returns ``(kernels [n, *world] float32,
+    K_half [n, *world[:-1], W//2+1] complex64 or None)``.  2D worlds of side
+    32..256, 3D worlds of side 32 or 64."""
+    import ctypes
+    from . import _lib
+    world = [int(w) for w in world]
+    n = len(R)
+    if device is None:
+        device = torch.device('cuda', torch.cuda.current_device())
+    if kf_slug not in KF_IDS:
+        raise ValueError(f'unknown kernel function slug {kf_slug!r}')
+    if len(set(world)) != 1:
+        raise ValueError(f'world {world} must be square / cubic')
+    rr = [float(x) for x in (r if hasattr(r, '__len__') else [r] * n)]
+    bl = [list(map(float, x)) for x in b]
+    if len(bl) == 1 and n > 1:
+        bl = bl * n
+    nb_max = max(len(x) for x in bl)
+    bm = np.zeros((n, nb_max), np.float32)
+    for i, x in enumerate(bl):
+        bm[i, :len(x)] = x
+    kfp = np.zeros((n, 2), np.float32)
+    kf_rows = kf_params if (len(kf_params) == n and hasattr(kf_params[0], '__len__')) else [kf_params] * n
+    for i, x in enumerate(kf_rows):
+        x = list(x)
+        kfp[i, :len(x)] = x
+    t = lambda a, dt=torch.float32: torch.as_tensor(np.asarray(a), dtype=dt).to(device)
+    Rt, rt, bt = t(np.asarray(R, np.float32)), t(np.asarray(rr, np.float32)), t(bm)
+    nbt, kft = t(np.array([len(x) for x in bl], np.int32), torch.int32), t(kfp)
+    out = torch.empty([n] + world, dtype=torch.float32, device=device)
+    kh = torch.empty([n] + world[:-1] + [world[-1] // 2 + 1], dtype=torch.complex64, device=device) if spectrum else None
+    status = torch.zeros(1, dtype=torch.int32, device=device)
+    job = RingBatchC.get()()
+    job.nb_dims, job.size, job.n, job.kf_id, job.nb_max = len(world), world[0], n, KF_IDS[kf_slug], nb_max
+    job.R, job.r, job.b, job.nb, job.kf_params = (x.data_ptr() for x in (Rt, rt, bt, nbt, kft))
+    job.kernel_out = out.data_ptr()
+    job.k_half = kh.data_ptr() if kh is not None else None
+    job.status = status.data_ptr()
+    lib = _lib.load()
+    if not getattr(lib, '_lgx_ring_bound', False):
+        lib.lgx_ring_kernels_workspace_bytes.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]
+        lib.lgx_ring_kernels_workspace_bytes.restype = ctypes.c_int
+        lib.lgx_ring_kernels.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        lib.lgx_ring_kernels.restype = ctypes.c_int
+        lib._lgx_ring_bound = True
+    nbytes = ctypes.c_size_t(0)
+    _lib.check(lib.lgx_ring_kernels_workspace_bytes(ctypes.byref(job), ctypes.byref(nbytes)))
+    ws = torch.empty(max(int(nbytes.value), 256), dtype=torch.uint8, device=device)
+    _lib.check(lib.lgx_ring_kernels(ctypes.byref(job), ws.data_ptr(), ws.numel(),
+                                    torch.cuda.current_stream(device).cuda_stream))
+    if int(status.item()) != 0:
+        raise ValueError('a kernel box (2*ceil(r*R) cells) exceeds the world, or a ring list is empty')
+    return out, kh
