@@ -296,6 +296,31 @@ LGX_API int lgx_ring_kernels_workspace_bytes(const lgx_ring_batch* job, size_t* 
 LGX_API int lgx_ring_kernels(const lgx_ring_batch* job, void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------------------------
+ * Initial states generated on the device (leniax initializations.py:10-116 and
+ * perlin.py:16-71; make_array_compressible, loader.py:16-30): nb_init states
+ * per world from the world's 64-bit seed.  Random numbers: a counter-based
+ * SplitMix64 hash of (seed, stream, index), not JAX's threefry stream.
+ * ------------------------------------------------------------------------- */
+#define LGX_INIT_RANDOM_UNIFORM 0 /* uniform [0, maxval_i), maxval = linspace(0.4, 1, nb_init) */
+#define LGX_INIT_PERLIN 1         /* Perlin noise normalised per state, scaled from gf m */
+#define LGX_INIT_CROPPED_PERLIN 2 /* the 2 ceil(R) square at [24, 24 + 2 ceil(R)) on a zero 128 x 128 world */
+
+typedef struct lgx_init_job {
+  int kind;          /* LGX_INIT_* */
+  int n_worlds;
+  int nb_init;       /* states per world */
+  int H, W;          /* 2D world */
+  float R;           /* kernel radius of the Perlin periods (world_params R) */
+  int compressible;  /* 1: round to the NB_CHARS^2 - 1 grid of make_array_compressible */
+  const uint64_t* seeds; /* [n_worlds] device */
+  const float* gf_m;     /* [n_worlds] device: m of the first kernel (Perlin kinds) */
+  float* out;            /* [n_worlds, nb_init, H, W] */
+} lgx_init_job;
+
+LGX_API int lgx_init_cells_workspace_bytes(const lgx_init_job* job, size_t* bytes);
+LGX_API int lgx_init_cells(const lgx_init_job* job, void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
  * Uneven batch: thousands of worlds of different sizes, dimensions, kernels,
  * growth parameters and time steps in ONE persistent launch.  Replaces
  * leniax's vmap over identically shaped worlds (leniax/runner.py:167-215,

@@ -1,0 +1,94 @@
+"""QD evaluation glue and device initial states on the GPU."""
+import numpy as np
+import pytest
+import torch
+
+from leniax_gb300 import helpers, initializations, kernels, qd, runner, statistics
+from leniax_gb300.constant import NB_CHARS
+
+pytestmark = pytest.mark.gpu
+
+
+def qd_config(init_slug='perlin', steps=48, nb_init_search=4):
+    return {
+        'world_params': {'nb_channels': 1, 'R': 13, 'T': 10.0},
+        'render_params': {'world_size': [128, 128]},
+        'run_params': {'max_run_iter': steps, 'nb_init_search': nb_init_search, 'seed': 1},
+        'algo': {'init_slug': init_slug},
+        'kernels_params': [{
+            'k_slug': 'circle_2d', 'k_params': [1.0, [1.0]], 'kf_slug': 'gauss_bump', 'kf_params': [4.0],
+            'gf_slug': 'gaussian', 'gf_params': [0.15, 0.015], 'h': 1.0, 'c_in': 0, 'c_out': 0
+        }],
+        'genotype': [{'key': 'kernels_params.0.gf_params.0', 'domain': [0.1, 0.3], 'type': 'float'},
+                     {'key': 'kernels_params.0.gf_params.1', 'domain': [0.01, 0.05], 'type': 'float'}],
+        'phenotype': ['behaviours.mass', 'behaviours.mass_volume'],
+    }
+
+
+@pytest.mark.parametrize('kind', ['random_uniform', 'perlin', 'cropped_perlin'])
+def test_initial_states(cuda, kind):
+    nb_init, R = 6, 13
+    a = initializations.generate(kind, [11, 12], nb_init, [128, 128], R, [0.15, 0.2]).cpu().numpy()
+    b = initializations.generate(kind, [11, 12], nb_init, [128, 128], R, [0.15, 0.2]).cpu().numpy()
+    c = initializations.generate(kind, [13, 12], nb_init, [128, 128], R, [0.15, 0.2]).cpu().numpy()
+    assert a.shape == (2, nb_init, 128, 128)
+    np.testing.assert_array_equal(a, b)  # same seed, same states
+    assert not np.array_equal(a[0], c[0]) and np.array_equal(a[1], c[1])
+    q = a * (NB_CHARS**2 - 1)
+    assert np.abs(q - np.round(q)).max() < 1e-2  # on the make_array_compressible grid
+    if kind == 'random_uniform':
+        maxv = np.linspace(0.4, 1., nb_init)
+        for i in range(nb_init):
+            assert a[0, i].min() >= 0 and a[0, i].max() <= maxv[i] + 1e-4 and a[0, i].max() > 0.9 * maxv[i]
+            assert abs(a[0, i].mean() - maxv[i] / 2) < 0.01
+    else:
+        for w, m in enumerate([0.15, 0.2]):
+            for i in range(nb_init):
+                scale = m + i / nb_init * (min(1., 3 * m) - m)
+                x = a[w, i]
+                if kind == 'perlin':
+                    assert abs(x.min()) < 1e-4 and abs(x.max() - scale) < 1e-3
+                    assert x.std() > 0.05 * scale  # a noise field, not a constant
+                else:
+                    crop, pad = 2 * R, (128 - 2 * R) // 2
+                    inner = x[pad:pad + crop, pad:pad + crop]
+                    assert np.all(x[:pad] == 0) and np.all(x[pad + crop:] == 0) and inner.max() > 0
+
+
+def test_dynamic_args_device_kernels_match_host_path(cuda):
+    cfg = qd_config()
+    inds = [qd.LeniaIndividual(cfg, 5 + i, [0.2 + 0.3 * i, 0.4]) for i in range(3)]
+    _, (cells0, K, gf, w, T) = qd.get_dynamic_args(cfg, inds)
+    assert tuple(cells0.shape) == (3, 4, 1, 128, 128)
+    assert tuple(K.shape) == (3, 1, 1, 1, 128, 128) and K.dtype == torch.complex64
+    assert tuple(gf.shape) == (3, 1, 2) and tuple(w.shape) == (3, 1, 1) and tuple(T.shape) == (3, )
+    for i, ind in enumerate(inds):
+        c = ind.get_config()
+        Kh, mp = kernels.get_kernels_and_mapping([dict(p) for p in c['kernels_params']], [128, 128], 1, 13, True)
+        assert (K[i, 0] - Kh[0]).abs().max().item() <= 2e-5 * Kh.abs().max().item()
+        np.testing.assert_allclose(gf[i].cpu().numpy(), mp.get_gf_params().cpu().numpy())
+    # genes reached the growth parameters
+    assert abs(gf[1, 0, 0].item() - (0.1 + 0.2 * 0.5)) < 1e-6
+
+
+def test_eval_fn_fitness_is_max_stop_count(cuda):
+    cfg = qd_config(steps=48)
+    inds = [qd.LeniaIndividual(cfg, 21 + i, [0.1 + 0.2 * i, 0.3 + 0.1 * i]) for i in range(4)]
+    ev = qd.build_eval_lenia_config_mem_optimized_fn(cfg)
+    out = ev(inds)
+    # the same rollout through the runner
+    _, args = qd.get_dynamic_args(cfg, inds, full_spectrum=False)
+    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in cfg['kernels_params']], [128, 128], 1, 13, True)
+    upd = helpers.build_update_fn(K.shape, mp)
+    stats, _ = runner.run_scan_mem_optimized(None, *args, 48, 13, upd,
+                                             statistics.build_compute_stats_fn(cfg['world_params'],
+                                                                               cfg['render_params']))
+    N = stats['N'].cpu().numpy()
+    for i, ind in enumerate(out):
+        assert ind.fitness == N[i].max()
+        assert ind.qd_config['algo']['best_init_idxs'] == [int(j) for j in np.nonzero(N[i] == N[i].max())[0]]
+        assert len(ind.features) == 2
+        b = int(np.argmax(N[i]))
+        ns = max(int(ind.fitness), 128)
+        m = stats['mass'][i, ns - 128:ns, b].double().mean().item() if ns - 128 < 48 else float('nan')
+        assert (np.isnan(m) and np.isnan(ind.features[0])) or abs(ind.features[0] - m) < 1e-9
