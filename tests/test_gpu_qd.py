@@ -92,3 +92,13 @@ def test_eval_fn_fitness_is_max_stop_count(cuda):
         ns = max(int(ind.fitness), 128)
         m = stats['mass'][i, ns - 128:ns, b].double().mean().item() if ns - 128 < 48 else float('nan')
         assert (np.isnan(m) and np.isnan(ind.features[0])) or abs(ind.features[0] - m) < 1e-9
+
+
+def test_codec_batch_on_device_states(cuda):
+    from leniax_gb300 import loader
+    x = initializations.generate('perlin', [3, 4, 5], 2, [64, 64], 5, [0.2] * 3, compressible=False)
+    on_dev = loader.compress_batch(x.reshape(6, 1, 64, 64))
+    on_host = loader.compress_batch(x.reshape(6, 1, 64, 64).cpu())
+    assert on_dev == on_host
+    back = loader.decompress_array(on_dev[4], device=x.device)
+    assert torch.equal(back, loader.make_array_compressible(x.reshape(6, 1, 64, 64)[4]))
