@@ -46,7 +46,9 @@ namespace {
 
 inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Bump allocator over a caller-owned workspace.
+// Bump allocator over a caller-owned workspace.  `fits()` tells whether the
+// layout carved so far stays inside the caller's bytes; every entry point
+// checks it before launching anything.
 struct Carve {
   char* base;
   size_t off = 0, cap;
@@ -57,6 +59,7 @@ struct Carve {
     off = al256(off + count * sizeof(T));
     return p;
   }
+  bool fits() const { return off <= cap; }
 };
 
 bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
@@ -230,6 +233,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     cv.take<int>(kStatusBytes / sizeof(int));
     float2* kp = cv.take<float2>((size_t)j->n_sols * m.H * resident_kpitch(m.H));
     raw = cv.take<float>((size_t)j->n_sols * j->steps * j->n_init * raw_stride(m.C));
+    if (!cv.fits()) return fail(LGX_ERR_WORKSPACE, "lgx_run: internal workspace layout exceeds its size query");
     ce = launch_prepare_resident_spectrum(m.H, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
     ResidentArgs a;
@@ -302,6 +306,9 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
         ss.prod = b.prod;
         ss.partial = b.partial;
         ss.status = b.status;
+        // the row inverse of step s writes the row spectra step s + 1 starts from
+        ss.spec_ready = s > 0;
+        ss.emit_spec = s + 1 < j->steps;
         ce = launch_streamed_step(ss, st);
         if (ce != cudaSuccess) return cuda_fail(ce, "streamed step");
       } else {
@@ -324,6 +331,8 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
           ss.prod = b.prod;
           ss.partial = b.partial;
           ss.status = b.status;
+          ss.spec_ready = false;  // one world per launch: the spectrum buffer is shared by all worlds
+          ss.emit_spec = false;
           ce = launch_streamed_step(ss, st);
           if (ce != cudaSuccess) return cuda_fail(ce, "plain step");
         }
@@ -412,6 +421,8 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
     ss.prod = b.prod;
     ss.partial = b.partial;
     ss.status = b.status;
+    ss.spec_ready = false;
+    ss.emit_spec = false;
     ce = launch_streamed_step(ss, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "update step");
     g_err.clear();
@@ -486,6 +497,7 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   a.spec = cv.take<float2>(nw * cells);
   a.prod = cv.take<float2>(nw * cells / 2);
   a.partial = cv.take<float>(nw * 64 * 3);
+  if (!cv.fits()) return fail(LGX_ERR_WORKSPACE, "lgx_adjoint: internal workspace layout exceeds its size query");
   cudaError_t ce = launch_prepare_streamed_spectrum(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
   if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
   a.n_sols = j->n_sols;

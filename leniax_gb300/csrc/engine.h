@@ -140,6 +140,8 @@ struct StreamedStep {
   float2* prod;            // workspace [n_worlds, K, H/2, W] packed product spectra
   float* partial;          // workspace per-block raw partials
   int* status;             // device status word (0 = ok; set when a staged copy times out), or null
+  bool spec_ready;         // spec already holds the row spectra of `state` (written by the previous step)
+  bool emit_spec;          // write the row spectra of `state_out` into spec for the next step
 };
 cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st);
 cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,

@@ -256,7 +256,8 @@ size_t row_inv_smem(int C, int K) {
   using RC = RowInvCfg<N>;
   return (size_t)2 * RC::BUF * sizeof(float2) + (size_t)3 * N * sizeof(float2) +
          (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float) + 16 * sizeof(uint64_t) +
-         (size_t)kMaxChannels * sizeof(float) + (size_t)(C * K + K + 1) * sizeof(int);
+         (size_t)RC::GPB * RC::ROWP * sizeof(float2) + (size_t)kMaxChannels * sizeof(float) +
+         (size_t)(C * K + K + 1) * sizeof(int);
 }
 
 template <int N, int GF>
@@ -264,7 +265,8 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     int n_worlds, int n_init, KTab tab, const float2* __restrict__ prod, const float* __restrict__ gfp,
     long gf_sol_stride, const float* __restrict__ wts, long w_sol_stride, const float* __restrict__ dtp,
     const float* __restrict__ state, float* __restrict__ state_out, float* __restrict__ field_out,
-    float* __restrict__ pot_out, const int* __restrict__ shift, float* __restrict__ partial, int* __restrict__ status) {
+    float* __restrict__ pot_out, const int* __restrict__ shift, float* __restrict__ partial, int* __restrict__ status,
+    float2* __restrict__ spec_next) {
   using RC = RowInvCfg<N>;
   constexpr int G = RC::G, GPB = RC::GPB, BPW = RC::BPW, ROWP = RC::ROWP;
   using GE = Geo<N, G>;
@@ -277,7 +279,8 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   float2* tw = bufs + 2 * RC::BUF;      // 3N twiddles
   float* red = reinterpret_cast<float*>(tw + 3 * N);  // [warps][RAWS_MAX]
   uint64_t* bars = reinterpret_cast<uint64_t*>(red + NWARPS * RAWS_MAX);  // 2 (16 slots reserved)
-  float* wsum_s = reinterpret_cast<float*>(bars + 16);                    // [kMaxChannels]
+  float2* fscr = reinterpret_cast<float2*>(bars + 16);                    // [GPB][ROWP] next-step row FFT scratch
+  float* wsum_s = reinterpret_cast<float*>(fscr + GPB * ROWP);            // [kMaxChannels]
   int* items = reinterpret_cast<int*>(wsum_s + kMaxChannels);
   __shared__ int s_nitems;
 
@@ -405,6 +408,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     float* da_row = state_out + base + (size_t)(2 * r) * N;
     float* fa_row = field_out ? field_out + base + (size_t)(2 * r) * N : nullptr;
     float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f;
+    float2 nsv[P];  // the new rows (2r, 2r+1) at x = t + G*k1: the next step's row-FFT input comb
 #pragma unroll
     for (int k1 = 0; k1 < P; ++k1) {
       const int x = t + G * k1;
@@ -414,8 +418,9 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
         fb = fb / wsum;
       }
       const float sa = __ldg(sa_row + x), sb = __ldg(sa_row + N + x);
-      da_row[x] = state_fn(tab.state_fn, sa, fa, dt);
-      da_row[N + x] = state_fn(tab.state_fn, sb, fb, dt);
+      nsv[k1] = make_float2(state_fn(tab.state_fn, sa, fa, dt), state_fn(tab.state_fn, sb, fb, dt));
+      da_row[x] = nsv[k1].x;
+      da_row[N + x] = nsv[k1].y;
       if (fa_row) {
         fa_row[x] = fa;
         fa_row[N + x] = fb;
@@ -442,6 +447,16 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     m2y += cya * cya * Sa + cyb * cyb * Sb;
     const float cms = warp_sum(Sa + Sb);
     if (lane == 0) red[wid * RAWS_MAX + RAW_CM + co] = cms;
+    if (spec_next) {
+      // the next step's row pass, fused: FFT of the packed new rows -> its spectrum plane
+      float2 u[Q][G];
+      fft_standard<GE, false, false>(nsv, u, fscr + grp * ROWP, tw, t, gmask);
+      float2* dst = spec_next + (((size_t)n * C + co) * (N / 2) + r) * N;
+#pragma unroll
+      for (int q = 0; q < Q; ++q)
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) dst[pa_pos<N>(t + G * q + P * k1)] = u[q][k1];
+    }
   }
   while (!failed && i < nit) process(i++);  // kernels that feed no channel
   if (failed) {
@@ -555,7 +570,7 @@ cudaError_t launch_row_inv(const StreamedStep& s, const KTab& tab, cudaStream_t 
   if (e != cudaSuccess) return e;
   row_inv_kernel<N, GF><<<(unsigned)((long)s.n_worlds * RC::BPW), RC::T, sm_inv, st>>>(
       s.n_worlds, s.n_init, tab, s.prod, s.gf, s.gf_sol_stride, s.w, s.w_sol_stride, s.dt, s.state, s.state_out,
-      s.field_out, s.pot_out, s.shift, s.partial, s.status);
+      s.field_out, s.pot_out, s.shift, s.partial, s.status, s.emit_spec ? s.spec : nullptr);
   return cudaGetLastError();
 }
 
@@ -619,7 +634,8 @@ cudaError_t step_n(const StreamedStep& s, cudaStream_t st) {
   const long planes = (long)s.n_worlds * m.C;
   alignas(64) CUtensorMap spec_map;
   if (!encode_spec_map<N>(&spec_map, s.spec, planes)) return cudaErrorInvalidValue;
-  row_fwd_kernel<N><<<(unsigned)(planes * BPP), kThreads, sm_fwd, st>>>(s.n_worlds, m.C, s.state, s.spec);
+  if (!s.spec_ready)  // otherwise the previous step's row inverse already wrote this step's row spectra
+    row_fwd_kernel<N><<<(unsigned)(planes * BPP), kThreads, sm_fwd, st>>>(s.n_worlds, m.C, s.state, s.spec);
   col_conv_kernel<N><<<(unsigned)(planes * CC::BPP), CC::T, sm_col, st>>>(spec_map, s.n_worlds, s.n_init, tab, s.kp,
                                                                           s.kp_sol_stride, s.prod, s.status);
   using RC = RowInvCfg<N>;
