@@ -486,7 +486,9 @@ def profile_case(args):
       multichannel : the multi-channel model on the streamed engine
                      (--profile-worlds worlds x 256x256, C=3, K=15, --profile-steps steps)
       uneven256 / uneven3d : --profile-worlds worlds of 256x256 / 64x64x64 in one uneven-batch launch
-                     (--profile-steps steps)"""
+                     (--profile-steps steps)
+      adjoint      : the differentiation workload (forward + backward) on --profile-worlds worlds of
+                     128x128 over --profile-steps steps, checkpoints every 16"""
     import torch
     from leniax_gb300 import helpers, kernels, runner, statistics
     dev = torch.device('cuda', 0)
@@ -514,6 +516,9 @@ def profile_case(args):
             sd, fin = runner.run_scan_mem_optimized(None, cells, K[None], gf, w, Tt, ns, Rw, upd, stats_fn,
                                                     engine='streamed', with_box=True)
         info = {'mean_N': float(sd['N'].float().mean())}
+    elif name == 'adjoint':
+        r = measure_adjoint(dev, worlds=nw, steps=ns, reps=1)
+        info = {'fwd_bwd_world_steps_per_s': r['value']}
     else:
         from leniax_gb300 import batch as lbatch
         from leniax_gb300 import workloads
@@ -547,7 +552,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--profile-case', nargs='?', const='resident', default=None,
-                    choices=['resident', 'multichannel', 'uneven256', 'uneven3d'],
+                    choices=['resident', 'multichannel', 'uneven256', 'uneven3d', 'adjoint'],
                     help='profiling case for ncu: one warm-up and one rollout of --profile-worlds worlds x '
                          '--profile-steps Euler steps of the named workload, nothing else')
     ap.add_argument('--profile-worlds', type=int, default=2048)

@@ -14,8 +14,9 @@
 //            spectrum of a times conj(K^))
 //   dL/dm, dL/ds, dL/dw  += sums of dt * mu * df/dparam
 //   dL/dK  += a (*)^T s  (accumulated as spectrum(a) * conj(spectrum(s)))
-// Kernels of one adjoint step: adj_point -> row_fwd (a and s planes) ->
-// col_adj -> row_inv_adj -> param reduction.  The same packed real-FFT
+// Kernels of one adjoint step: adj_rows (pointwise adjoint + row FFTs of the
+// a and s planes) -> col_adj -> row_inv_add; the parameter partials are
+// reduced once per segment.  The same packed real-FFT
 // passes as the streamed engine are used (rows paired as one complex row,
 // columns 0 and N/2 packed together).
 #include <algorithm>
@@ -87,57 +88,6 @@ __device__ __forceinline__ void growth_and_grads(int id, float u, float m, float
   }
 }
 
-// ------------------------------------------------------------- adj_point
-// One thread per cell.  Writes lambda_out = direct term, the a and s planes
-// for the FFT passes, and per-block partial sums of dL/dm, dL/ds, dL/dw.
-__global__ void adj_point_kernel(AdjParams p, int cells, const float* __restrict__ lam_in,
-                                 const float* __restrict__ s_t, const float* __restrict__ u_t,
-                                 float* __restrict__ lam_out, float* __restrict__ as_planes,
-                                 float* __restrict__ partial) {
-  const int world = blockIdx.y;
-  const int sol = world / p.n_init;
-  const float m = __ldg(p.gf + 2 * sol), sg = __ldg(p.gf + 2 * sol + 1);
-  const float wk = __ldg(p.w + sol), dt = 1.f / __ldg(p.T + sol);
-  const float wf = p.mean ? wk / wk : wk;
-  float am = 0.f, as = 0.f, aw = 0.f;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < cells; i += gridDim.x * blockDim.x) {
-    const size_t off = (size_t)world * cells + i;
-    const float lam = lam_in[off], s = s_t[off], u = u_t[off];
-    float g, gu, gm, gs;
-    growth_and_grads(p.gf_id, u, m, sg, g, gu, gm, gs);
-    const float f = g * wf;
-    float mu = lam;
-    if (p.state_fn == LGX_STATE_V1 && p.clip_mask) {
-      const float n = s + dt * f;
-      mu = (n > 0.f && n < 1.f) ? lam : 0.f;
-    }
-    const float direct = p.state_fn == LGX_STATE_V2 ? mu * (1.f - dt) : mu;
-    const float dfl = dt * mu;  // dL/df
-    lam_out[off] = direct;
-    as_planes[(size_t)world * 2 * cells + i] = dfl * wf * gu;  // a = dL/du
-    as_planes[(size_t)world * 2 * cells + cells + i] = s;
-    am += dfl * wf * gm;
-    as += dfl * wf * gs;
-    aw += p.mean ? 0.f : dfl * g;  // weighted_sum: f = w g; weighted_mean with one kernel: f = g
-  }
-  am = warp_sum(am);
-  as = warp_sum(as);
-  aw = warp_sum(aw);
-  __shared__ float red[3][32];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) {
-    red[0][wid] = am;
-    red[1][wid] = as;
-    red[2][wid] = aw;
-  }
-  __syncthreads();
-  if (threadIdx.x < 3) {
-    float v = 0.f;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
-    partial[((size_t)world * gridDim.x + blockIdx.x) * 3 + threadIdx.x] = v;
-  }
-}
-
 // per solution: grad_gf[s] += (dm, ds), grad_w[s] += dw over its inits and blocks
 __global__ void adj_param_reduce_kernel(int n_sols, int n_init, int blocks, const float* __restrict__ partial,
                                         float* __restrict__ grad_gf, float* __restrict__ grad_w) {
@@ -193,6 +143,94 @@ __global__ void __launch_bounds__(kT) adj_row_fwd_kernel(int planes, const float
   for (int q = 0; q < Q; ++q)
 #pragma unroll
     for (int k1 = 0; k1 < G; ++k1) dst[t + G * q + P * k1] = u[q][k1];
+}
+
+// ------------------------------------------------------------- adj_rows
+// Pointwise adjoint fused with the row FFTs: per (world, packed row pair) the
+// direct term lambda_next, a = dL/du and the row spectra of a (plane 2n) and
+// s (plane 2n+1); per-block partial sums of dL/dm, dL/ds, dL/dw accumulate
+// over the segment's steps in pacc (one slot per block, reduced once per
+// segment).
+template <int N>
+__global__ void __launch_bounds__(kT) adj_rows_kernel(AdjParams p, const float* __restrict__ lam_in,
+                                                      const float* __restrict__ s_t, const float* __restrict__ u_t,
+                                                      float* __restrict__ lam_next, float2* __restrict__ spec,
+                                                      float* __restrict__ pacc) {
+  constexpr int G = ACfg<N>::G;
+  using GE = Geo<N, G>;
+  constexpr int P = GE::P, Q = GE::Q, GPB = kT / G, BPP = (N / 2 + GPB - 1) / GPB;
+  extern __shared__ __align__(16) float2 sm[];
+  float2* scr = twiddles<N>(sm);
+  __shared__ float red[3][kT / 32];
+  __syncthreads();
+  const int n = blockIdx.x / BPP;
+  if (n >= p.n_worlds) return;  // whole blocks
+  const int sol = n / p.n_init;
+  const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int r = (blockIdx.x % BPP) * GPB + grp;
+  const bool active = r < N / 2;  // idle groups (small N) still reach the block barrier
+  const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
+  float am = 0.f, as = 0.f, aw = 0.f;
+  if (active) {
+    const float m = __ldg(p.gf + 2 * sol), sg = __ldg(p.gf + 2 * sol + 1);
+    const float wk = __ldg(p.w + sol), dt = 1.f / __ldg(p.T + sol);
+    const float wf = p.mean ? wk / wk : wk;
+    const size_t base = (size_t)n * N * N + (size_t)(2 * r) * N;
+    float2 va[P], vs[P];
+#pragma unroll
+    for (int n2 = 0; n2 < P; ++n2) {
+      float ae[2], se[2];
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const size_t off = base + (size_t)e * N + t + G * n2;
+        const float lam = lam_in[off], sv = __ldg(s_t + off), u = __ldg(u_t + off);
+        float g, gu, gm, gs;
+        growth_and_grads(p.gf_id, u, m, sg, g, gu, gm, gs);
+        float mu = lam;
+        if (p.state_fn == LGX_STATE_V1 && p.clip_mask) {
+          const float nn = sv + dt * (g * wf);
+          mu = (nn > 0.f && nn < 1.f) ? lam : 0.f;
+        }
+        lam_next[off] = p.state_fn == LGX_STATE_V2 ? mu * (1.f - dt) : mu;
+        const float dfl = dt * mu;  // dL/df
+        ae[e] = dfl * wf * gu;      // a = dL/du
+        se[e] = sv;
+        am += dfl * wf * gm;
+        as += dfl * wf * gs;
+        aw += p.mean ? 0.f : dfl * g;  // weighted_sum: f = w g; weighted_mean with one kernel: f = g
+      }
+      va[n2] = make_float2(ae[0], ae[1]);
+      vs[n2] = make_float2(se[0], se[1]);
+    }
+    float2 u[Q][G];
+    float2* rs = scr + grp * GE::SCR;
+    fft_standard<GE, false, false>(va, u, rs, sm, t, gmask);
+    float2* da = spec + ((size_t)(2 * n) * (N / 2) + r) * N;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int k1 = 0; k1 < G; ++k1) da[t + G * q + P * k1] = u[q][k1];
+    fft_standard<GE, false, false>(vs, u, rs, sm, t, gmask);
+    float2* ds = spec + ((size_t)(2 * n + 1) * (N / 2) + r) * N;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+#pragma unroll
+      for (int k1 = 0; k1 < G; ++k1) ds[t + G * q + P * k1] = u[q][k1];
+  }
+  am = warp_sum(am);
+  as = warp_sum(as);
+  aw = warp_sum(aw);
+  if (lane == 0) {
+    red[0][wid] = am;
+    red[1][wid] = as;
+    red[2][wid] = aw;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    float v = 0.f;
+    for (int w = 0; w < kT / 32; ++w) v += red[threadIdx.x][w];
+    pacc[((size_t)n * BPP + blockIdx.x % BPP) * 3 + threadIdx.x] += v;
+  }
 }
 
 // Load column pair c of a packed-row spectrum plane and run the forward column
@@ -478,12 +516,10 @@ cudaError_t adjoint_n(const AdjointSegment& j, cudaStream_t st) {
   constexpr int G = ACfg<N>::G, GPB = kT / G, BPP = (N / 2 + GPB - 1) / GPB;
   const size_t smem = pass_smem<N>();
   cudaError_t e;
-  if ((e = allow_smem(adj_row_fwd_kernel<N>, smem)) != cudaSuccess) return e;
   if ((e = allow_smem(col_adj_kernel<N>, smem)) != cudaSuccess) return e;
   if ((e = allow_smem(row_inv_add_kernel<N>, smem)) != cudaSuccess) return e;
   const int nw = j.n_sols * j.n_init;
   const int cells = N * N;
-  const int pblocks = std::max(1, std::min(64, cells / 256));
   AdjParams p;
   p.n_worlds = nw;
   p.n_init = j.n_init;
@@ -494,21 +530,22 @@ cudaError_t adjoint_n(const AdjointSegment& j, cudaStream_t st) {
   p.gf = j.gf_params;
   p.w = j.weights;
   p.T = j.T;
+  if ((e = allow_smem(adj_rows_kernel<N>, smem)) != cudaSuccess) return e;
   const long kp_sol = (long)N * (N / 2 + 2);
+  // per-block parameter partials accumulate over the segment, reduced once
+  if ((e = cudaMemsetAsync(j.partial, 0, (size_t)nw * BPP * 3 * sizeof(float), st)) != cudaSuccess) return e;
   // lambda ping-pong: step t reads lam_cur, writes lam_next
   const float* lam_cur = j.lambda_in;
   for (int s = j.steps - 1; s >= 0; --s) {
     float* lam_next = (s == 0) ? j.lambda_out : ((s & 1) ? j.lam_a : j.lam_b);
     const float* st_s = j.traj_cells + (size_t)s * nw * cells;
     const float* st_u = j.traj_potential + (size_t)s * nw * cells;
-    adj_point_kernel<<<dim3(pblocks, nw), 256, 0, st>>>(p, cells, lam_cur, st_s, st_u, lam_next, j.as_planes,
-                                                       j.partial);
-    adj_param_reduce_kernel<<<j.n_sols, 256, 0, st>>>(j.n_sols, j.n_init, pblocks, j.partial, j.grad_gf, j.grad_w);
-    adj_row_fwd_kernel<N><<<(unsigned)(2 * nw * BPP), kT, smem, st>>>(2 * nw, j.as_planes, j.spec);
+    adj_rows_kernel<N><<<(unsigned)(nw * BPP), kT, smem, st>>>(p, lam_cur, st_s, st_u, lam_next, j.spec, j.partial);
     col_adj_kernel<N><<<(unsigned)(nw * BPP), kT, smem, st>>>(nw, j.n_init, j.spec, j.kp, kp_sol, j.gk, j.prod);
     row_inv_add_kernel<N><<<(unsigned)(nw * BPP), kT, smem, st>>>(nw, j.prod, lam_next, 1.f, 1);
     lam_cur = lam_next;
   }
+  adj_param_reduce_kernel<<<j.n_sols, 256, 0, st>>>(j.n_sols, j.n_init, BPP, j.partial, j.grad_gf, j.grad_w);
   return cudaGetLastError();
 }
 

@@ -455,7 +455,6 @@ size_t adjoint_ws(const Model& m, int n_sols, int n_init) {
   size_t b = 0;
   b += al256((size_t)n_sols * m.H * (m.W / 2 + 2) * sizeof(float2));  // kp
   b += 2 * al256(nw * cells * sizeof(float));                         // lam_a, lam_b
-  b += al256(nw * 2 * cells * sizeof(float));                         // as planes
   b += al256(nw * cells * sizeof(float2));                            // spec (2 planes x N/2 x N)
   b += al256(nw * cells / 2 * sizeof(float2));                        // prod
   b += al256(nw * 64 * 3 * sizeof(float));                            // partial
@@ -493,7 +492,6 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   float2* kp = cv.take<float2>((size_t)j->n_sols * m.H * (m.W / 2 + 2));
   a.lam_a = cv.take<float>(nw * cells);
   a.lam_b = cv.take<float>(nw * cells);
-  a.as_planes = cv.take<float>(nw * 2 * cells);
   a.spec = cv.take<float2>(nw * cells);
   a.prod = cv.take<float2>(nw * cells / 2);
   a.partial = cv.take<float>(nw * 64 * 3);

@@ -160,10 +160,9 @@ struct AdjointSegment {
   const float* lambda_in;       // [nw, N, N]
   float* lambda_out;            // [nw, N, N]
   float *lam_a, *lam_b;         // [nw, N, N] ping-pong
-  float* as_planes;             // [nw, 2, N, N]
   float2* spec;                 // [nw, 2, N/2, N]
   float2* prod;                 // [nw, N/2, N]
-  float* partial;               // [nw, 64, 3]
+  float* partial;               // [nw, 64, 3] per-block parameter partials
   float2* gk;                   // [nw, N/2, N] kernel-gradient accumulator (column domain)
   float* grad_gf;               // [Ns, 2]   +=
   float* grad_w;                // [Ns]      +=
