@@ -4,10 +4,10 @@
 //                      (statistics.py:36-126).  The carried centroid / angle of
 //                      step t only depend on the moments of steps t-1 and t-2,
 //                      so every step is evaluated independently.
-//  heuristics_kernel : one thread per (sol, init): the sequential scan of
-//                      check_heuristics (statistics.py:134-205) -> N, and the
-//                      box stop set (mass < 1e-3, mass > 0.9 * area, a live
-//                      cell on the outer layer) -> N_box.
+//  heuristics_kernel : one warp per (sol, init): check_heuristics
+//                      (statistics.py:134-205) -> N, and the box stop set
+//                      (mass < 1e-3, mass > 0.9 * area, a live cell on the
+//                      outer layer) -> N_box, 32 steps per round.
 #include "common.cuh"
 #include "engine.h"
 
@@ -159,45 +159,84 @@ __global__ void stats_kernel(Ctx c, int n_sols, const float* __restrict__ raw, f
   s[10] = r[RAW_CNT_POT] / R2;
 }
 
+// One warp per (sol, init), 32 steps per round.  The scan of
+// statistics.py:134-205 is rewritten in closed form so the lanes of a round
+// work independently: the monotone and mass-volume counters at step t equal
+// t - b + 1 with b the last reset step at or before t (a sign change, resp.
+// mass_volume <= 10; step 0 counts as a reset), found with a warp max-scan
+// carried across rounds; should_continue is the product of the conditions,
+// so N is the first step whose condition fails (steps if none), found with a
+// ballot.  The box stop set is the same first-failure search.  Results equal
+// the sequential scan's (same per-step arithmetic).
+__device__ __forceinline__ int warp_max_scan(int v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v = max(v, u);
+  }
+  return v;
+}
+
 __global__ void heuristics_kernel(Ctx c, int n_sols, float area, const float* __restrict__ raw,
                                   float* __restrict__ n_cont, float* __restrict__ n_box) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_sols * c.n_init) return;
+  const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (i >= n_sols * c.n_init) return;  // whole warps
   const int sol = i / c.n_init, init = i % c.n_init;
   const float Rs = c.R_arr ? __ldg(c.R_arr + sol) : c.R;
   const float R2 = Rs * Rs;
-  float init_cm[kMaxChannels];
   const float* r0 = raw_at(raw, c, sol, 0, init);
-  for (int ch = 0; ch < c.C && ch < kMaxChannels; ++ch) init_cm[ch] = r0[RAW_CM + ch] / R2;
-  float should = 1.f, N = 0.f, prev_mass = r0[RAW_M00] / R2, prev_sign = 0.f;
-  int c_mono = 0, c_vol = 0;
-  float box = 1.f, NB = 0.f;
-  for (int t = 0; t < c.steps; ++t) {
-    const float* r = raw_at(raw, c, sol, t, init);
+  const int T = c.steps;
+  int N = T, NB = T;
+  bool foundN = false, foundB = false;
+  float prev_mass = r0[RAW_M00] / R2, prev_sign = 0.f;  // carried into each round's lane 0
+  int carry_bm = 0, carry_bv = 0;                        // last reset steps so far
+  for (int t0 = 0; t0 < T && !(foundN && foundB); t0 += 32) {
+    const int t = t0 + lane;
+    const bool valid = t < T;
+    const float* r = raw_at(raw, c, sol, valid ? t : T - 1, init);
     bool cond = true;
     for (int ch = 0; ch < c.C && ch < kMaxChannels; ++ch) {
       const float cm = r[RAW_CM + ch] / R2;
-      cond = cond && (cm >= kEps) && (cm <= 3.f * init_cm[ch]);  // statistics.py:224-251
+      const float cm0 = r0[RAW_CM + ch] / R2;
+      cond = cond && (cm >= kEps) && (cm <= 3.f * cm0);  // statistics.py:224-251
     }
     const float mass = r[RAW_M00] / R2;
-    const float d = mass - prev_mass;
+    float pm = __shfl_up_sync(0xffffffffu, mass, 1);
+    if (lane == 0) pm = prev_mass;
+    const float d = mass - pm;
     const float sign = d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f);
-    c_mono = c_mono * (sign == prev_sign ? 1 : 0) + 1;  // statistics.py:287-306
-    cond = cond && (c_mono <= 128);
+    float ps = __shfl_up_sync(0xffffffffu, sign, 1);
+    if (lane == 0) ps = prev_sign;
+    // monotone counter (statistics.py:287-306): resets where the sign changes
+    const int bm = max(warp_max_scan((t == 0 || sign != ps) ? t : -1, lane), carry_bm);
+    const int c_mono = t - bm + 1;
+    // mass-volume counter (statistics.py:317-333): resets where mass_volume <= 10
     const float mv = r[RAW_CNT_MASS] / R2;
-    c_vol = c_vol * (mv > 10.f ? 1 : 0) + 1;  // statistics.py:317-333
-    cond = cond && (c_vol <= 128);
-    should = should * (cond ? 1.f : 0.f);
-    N += should;
-    prev_mass = mass;
-    prev_sign = sign;
+    const int bv = max(warp_max_scan((t == 0 || !(mv > 10.f)) ? t : -1, lane), carry_bv);
+    const int c_vol = t - bv + 1;
+    cond = cond && (c_mono <= 128) && (c_vol <= 128);
+    const unsigned failN = __ballot_sync(0xffffffffu, valid && !cond);
+    if (!foundN && failN) {
+      N = t0 + __ffs(failN) - 1;
+      foundN = true;
+    }
     const float raw_mass = r[RAW_M00];
     const bool bc = raw_mass >= 1e-3f && raw_mass <= 0.9f * area && r[RAW_BORDER] == 0.f;
-    box = box * (bc ? 1.f : 0.f);
-    NB += box;
+    const unsigned failB = __ballot_sync(0xffffffffu, valid && !bc);
+    if (!foundB && failB) {
+      NB = t0 + __ffs(failB) - 1;
+      foundB = true;
+    }
+    prev_mass = __shfl_sync(0xffffffffu, mass, 31);
+    prev_sign = __shfl_sync(0xffffffffu, sign, 31);
+    carry_bm = __shfl_sync(0xffffffffu, bm, 31);
+    carry_bv = __shfl_sync(0xffffffffu, bv, 31);
   }
-  if (n_cont) n_cont[i] = N;
-  if (n_box) n_box[i] = NB;
+  if (lane == 0) {
+    if (n_cont) n_cont[i] = (float)N;
+    if (n_box) n_box[i] = (float)NB;
+  }
 }
 
 }  // namespace
@@ -221,8 +260,8 @@ cudaError_t launch_stats(const StatsArgs& a, cudaStream_t st) {
   if (a.n_continue || a.n_box) {
     float area = (float)a.C;
     for (int d = 0; d < a.nb_dims; ++d) area *= (float)a.world[d];
-    const int n = a.n_sols * a.n_init;
-    heuristics_kernel<<<(n + 127) / 128, 128, 0, st>>>(c, a.n_sols, area, a.raw, a.n_continue, a.n_box);
+    const int n = a.n_sols * a.n_init;  // one warp each
+    heuristics_kernel<<<(n + 7) / 8, 256, 0, st>>>(c, a.n_sols, area, a.raw, a.n_continue, a.n_box);
   }
   return cudaGetLastError();
 }

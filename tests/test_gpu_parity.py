@@ -253,3 +253,29 @@ def test_streamed_multichannel_status_word_and_engines_agree(cuda, size):
     st, fo = O.run_scan(cells[0], Ko, mpo['gf_params'], mpo['weights'], 5., steps, R, model, keep_intermediary=False)
     assert np.abs(fin[0].cpu().numpy() - fo).max() <= 1e-4
     np.testing.assert_array_equal(sd['N'][0].cpu().numpy(), st['N'])
+
+
+def test_stop_count_equals_sequential_scan_of_engine_stats(cuda):
+    # N from the warp-parallel heuristics kernel must equal leniax's sequential
+    # check_heuristics scan (restated in the oracle) over the engine's own
+    # statistics, for long rollouts where the monotone and mass-volume
+    # counters can run past 128
+    dev = torch.device('cuda')
+    size, R, steps = 64, 10, 400
+    cells = np.stack([patch_init(6, size, 24, seed=40 + s, scale_range=(0.3, 1.0)) for s in range(3)])
+    Ks, gfs, ws = [], [], []
+    upd = None
+    for s, (m, sg) in enumerate([(0.15, 0.02), (0.12, 0.03), (0.2, 0.04)]):
+        K, mp, u = engine_model(bump_kernel_params(m=m, s=sg), [size, size], 1, R, dev=dev)
+        upd = upd or u
+        Ks.append(K)
+        gfs.append(mp.get_gf_params(dev))
+        ws.append(mp.get_kernels_weight_per_channel(dev))
+    stats_fn = statistics.ComputeStatsFn([size, size], R, 10)
+    sd, _ = runner.run_scan_mem_optimized(None, torch.from_numpy(cells).to(dev), torch.stack(Ks), torch.stack(gfs),
+                                          torch.stack(ws), torch.tensor([10., 10., 10.]), steps, R, upd, stats_fn)
+    for s in range(3):
+        st = {k: v[s].cpu().numpy() for k, v in sd.items() if k != 'N'}
+        st['channel_mass'] = st['channel_mass']  # [T, Ni, C]
+        cont = O.check_heuristics(st)
+        np.testing.assert_array_equal(sd['N'][s].cpu().numpy(), cont.sum(axis=0))
