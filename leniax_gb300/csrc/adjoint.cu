@@ -582,6 +582,12 @@ bool adjoint_supported(const Model& m) {
 
 bool spectrum_supported(int H, int W) { return H == W && (H == 32 || H == 64 || H == 128 || H == 256); }
 
+cudaError_t launch_param_reduce(int n_sols, int n_init, int blocks, const float* partial, float* grad_gf,
+                                float* grad_w, cudaStream_t st) {
+  adj_param_reduce_kernel<<<n_sols, 256, 0, st>>>(n_sols, n_init, blocks, partial, grad_gf, grad_w);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_adjoint_segment(int N, const AdjointSegment& j, cudaStream_t st) {
   switch (N) {
     case 32: return adjoint_n<32>(j, st);

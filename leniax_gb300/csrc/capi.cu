@@ -516,8 +516,34 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   a.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
   a.grad_gf = j->grad_gf;
   a.grad_w = j->grad_weights;
-  ce = launch_adjoint_segment(m.H, a, st);
-  if (ce != cudaSuccess) return cuda_fail(ce, "adjoint segment");
+  if (adjoint_resident_supported(m)) {
+    // resident sizes: one persistent launch for the whole segment
+    AdjResArgs r;
+    r.n_worlds = (int)nw;
+    r.n_init = j->n_init;
+    r.steps = j->steps;
+    r.gf_id = a.gf_id;
+    r.state_fn = a.state_fn;
+    r.mean = a.mean;
+    r.clip_mask = a.clip_mask;
+    r.gf = j->gf_params;
+    r.w = j->weights;
+    r.T = j->T;
+    r.kp = kp;
+    r.traj_cells = j->traj_cells;
+    r.traj_pot = j->traj_potential;
+    r.lambda_in = j->lambda_in;
+    r.lambda_out = j->lambda_out;
+    r.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
+    r.pacc = a.partial;
+    ce = cudaMemsetAsync(a.partial, 0, nw * 3 * sizeof(float), st);
+    if (ce == cudaSuccess) ce = launch_adjoint_resident(m.H, r, st);
+    if (ce == cudaSuccess) ce = launch_param_reduce(j->n_sols, j->n_init, 1, a.partial, j->grad_gf, j->grad_weights, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "resident adjoint segment");
+  } else {
+    ce = launch_adjoint_segment(m.H, a, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "adjoint segment");
+  }
   g_err.clear();
   return LGX_OK;
 }

@@ -167,6 +167,27 @@ struct AdjointSegment {
   float* grad_gf;               // [Ns, 2]   +=
   float* grad_w;                // [Ns]      +=
 };
+// Resident adjoint (adjoint_resident.cu): one launch per segment for the
+// resident sizes, lambda in registers across the segment's steps.
+struct AdjResArgs {
+  int n_worlds, n_init, steps;
+  int gf_id, state_fn, mean, clip_mask;
+  const float* gf;              // [Ns, 2]
+  const float* w;               // [Ns]
+  const float* T;               // [Ns]
+  const float2* kp;             // [Ns, N, N/2+2] prepared spectra
+  const float* traj_cells;      // [steps, nw, N, N]
+  const float* traj_pot;        // [steps, nw, N, N]
+  const float* lambda_in;       // [nw, N, N]
+  float* lambda_out;            // [nw, N, N]
+  float2* gk;                   // [nw, N/2, N] kernel-gradient accumulator (+=)
+  float* pacc;                  // [nw, 3] parameter partials (+=)
+};
+bool adjoint_resident_supported(const Model& m);
+cudaError_t launch_adjoint_resident(int N, const AdjResArgs& a, cudaStream_t st);
+// per solution: grad_gf += partial sums 0..1, grad_w += partial sum 2 over its inits and blocks
+cudaError_t launch_param_reduce(int n_sols, int n_init, int blocks, const float* partial, float* grad_gf,
+                                float* grad_w, cudaStream_t st);
 bool adjoint_supported(const Model& m);
 bool spectrum_supported(int H, int W);
 cudaError_t launch_adjoint_segment(int N, const AdjointSegment& j, cudaStream_t st);
