@@ -1,5 +1,6 @@
 // Streamed Lenia step for any channel/kernel topology (2D, square power-of-two
-// worlds): the spectra of a step travel through HBM/L2 between four kernels.
+// worlds of side 32..512): the spectra of a step travel through HBM/L2
+// between its kernels.
 //
 //   row_fwd  : per (world, channel, packed row) N-point FFT of rows (2r, 2r+1)
 //              packed as one complex row -> spec[n][c][r][.] in the
@@ -54,6 +55,8 @@ template <>
 struct SCfg<128> { static constexpr int G = 8; };
 template <>
 struct SCfg<256> { static constexpr int G = 8; };
+template <>
+struct SCfg<512> { static constexpr int G = 16; };
 
 template <int N>
 __device__ __forceinline__ float2* init_tw(float2* sm) {
@@ -660,7 +663,7 @@ cudaError_t step_n(const StreamedStep& s, cudaStream_t st) {
 bool streamed_supported(const Model& m) {
   if (m.nb_dims != 2 || m.H != m.W) return false;
   if (m.C > kMaxChannels || m.K > kMaxKernels) return false;
-  if (!(m.H == 32 || m.H == 64 || m.H == 128 || m.H == 256)) return false;
+  if (!(m.H == 32 || m.H == 64 || m.H == 128 || m.H == 256 || m.H == 512)) return false;
   return true;
 }
 
@@ -670,6 +673,7 @@ int streamed_blocks_per_world(const Model& m) {
     case 64: return RowInvCfg<64>::BPW;
     case 128: return RowInvCfg<128>::BPW;
     case 256: return RowInvCfg<256>::BPW;
+    case 512: return RowInvCfg<512>::BPW;
   }
   return 1;
 }
@@ -692,6 +696,7 @@ cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st) {
     case 64: return step_n<64>(s, st);
     case 128: return step_n<128>(s, st);
     case 256: return step_n<256>(s, st);
+    case 512: return step_n<512>(s, st);
   }
   return cudaErrorInvalidValue;
 }
@@ -707,6 +712,7 @@ cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const f
     case 64: prepare_streamed_kernel<64><<<blocks, threads, 0, st>>>(planes, k_half, kp); break;
     case 128: prepare_streamed_kernel<128><<<blocks, threads, 0, st>>>(planes, k_half, kp); break;
     case 256: prepare_streamed_kernel<256><<<blocks, threads, 0, st>>>(planes, k_half, kp); break;
+    case 512: prepare_streamed_kernel<512><<<blocks, threads, 0, st>>>(planes, k_half, kp); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

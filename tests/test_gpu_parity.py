@@ -36,7 +36,7 @@ def single_step_case(kparams, world, C, R, cells, T, state_slug='v1', average=Tr
     return (s.cpu().numpy(), f.cpu().numpy(), p.cpu().numpy()), (s_o, f_o, p_o)
 
 
-@pytest.mark.parametrize('size', [32, 64, 128, 256])
+@pytest.mark.parametrize('size', [32, 64, 128, 256, 512])
 def test_update_single_step_bump_gaussian(cuda, size):
     R = 13 if size >= 64 else 6
     cells = patch_init(3, size, min(40, size // 2), seed=size)
@@ -232,7 +232,7 @@ def test_trajectory_outputs_match_oracle(cuda):
         assert np.abs(st['N'].cpu().numpy() - st_o['N']).max() == 0
 
 
-@pytest.mark.parametrize('size', [32, 64, 128, 256])
+@pytest.mark.parametrize('size', [32, 64, 128, 256, 512])
 def test_streamed_multichannel_status_word_and_engines_agree(cuda, size):
     # the staged (TMA / bulk) copies of the streamed engine all land: the
     # workspace status word stays 0, and the multi-channel rollout matches the
