@@ -69,6 +69,8 @@ extern "C" {
 #define LGX_ENGINE_RESIDENT 1 /* one world per CTA slice, state in registers across steps */
 #define LGX_ENGINE_STREAMED 2 /* multi-pass, spectra through HBM/L2, any C/K             */
 #define LGX_ENGINE_PLAIN 3    /* one world per launch, one step per launch (reference)  */
+#define LGX_ENGINE_CTA 4      /* one world per CTA, persistent over a work queue: 3D
+                                 worlds of side 32 / 64 (C = K = 1); no trajectories   */
 
 /* number of scalar statistics besides the C channel masses */
 #define LGX_NSTAT_SCALAR 11

@@ -29,7 +29,7 @@ GF_IDS = {
     'identity': 6,
 }
 STATE_IDS = {'v1': 0, 'v2': 1, 'simple': 2}
-ENGINES = {'auto': 0, 'resident': 1, 'streamed': 2, 'plain': 3}
+ENGINES = {'auto': 0, 'resident': 1, 'streamed': 2, 'plain': 3, 'cta': 4}
 NSTAT_SCALAR = 11
 
 EXPORTED = (

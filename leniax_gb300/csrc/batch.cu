@@ -70,10 +70,10 @@ constexpr size_t kMixedSmem = (size_t)TW_END * sizeof(float2) + kWorkBytes;
 static_assert(kMixedSmem <= 227 * 1024, "mixed kernel shared memory");
 
 template <int GF>
-__device__ __forceinline__ GrowthP big_growth(const BigArgs& a, int world) {
+__device__ __forceinline__ GrowthP big_growth(const BigArgs& a, int sol) {
   GrowthP g;
-  g.m = __ldg(a.gf + 2 * world);
-  g.s = __ldg(a.gf + 2 * world + 1);
+  g.m = __ldg(a.gf + 2 * sol);
+  g.s = __ldg(a.gf + 2 * sol + 1);
   g.id = a.gf_id;
   g.a = GF == GF_FAST_GAUSSIAN ? 0.84932180028801904272f / g.s : (GF == GF_FAST_POLY4 ? 1.f / (9.f * g.s * g.s) : 0.f);
   return g;
@@ -103,7 +103,8 @@ __device__ __forceinline__ void big_finish_step(const BigArgs& a, int world, int
     const float mx0 = __shfl_sync(0xffffffffu, v, RAW_MX + 0);
     const float mx1 = __shfl_sync(0xffffffffu, v, RAW_MX + 1);
     const float mx2 = __shfl_sync(0xffffffffu, v, RAW_MX + 2);
-    float* rw = a.raw + ((size_t)world * a.steps + step) * raw_stride(1);
+    const int sol = world / a.n_init, init = world - sol * a.n_init;
+    float* rw = a.raw + (((size_t)sol * a.steps + step) * a.n_init + init) * raw_stride(1);
     if (lane < RAW_BORDER) rw[lane] = v;
     else if (lane == RAW_BORDER) rw[lane] = v > 0.f ? 1.f : 0.f;
     else if (lane < RAW_CM) rw[lane] = (float)(lane == RAW_SHIFT ? sh0 : (lane == RAW_SHIFT + 1 ? sh1 : sh2));
@@ -132,12 +133,13 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
   float* red = reinterpret_cast<float*>(work + NG * GE::SCR);
   int* shv = reinterpret_cast<int*>(red + 16 * 16);
   float2* spec = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;  // [N/2][N]
-  const float2* kp = a.kp + (size_t)world * N * KP;
+  const int sol = world / a.n_init;
+  const float2* kp = a.kp + (size_t)sol * N * KP;
   const float* c0 = a.cells0 + (size_t)world * N * N;
   float* st = a.state + (size_t)world * N * N;
-  const GrowthP gq = big_growth<GF>(a, world);
-  const float wk = __ldg(a.w + world), wf = a.mean ? wk / wk : wk;
-  const float dt = 1.f / __ldg(a.T + world);
+  const GrowthP gq = big_growth<GF>(a, sol);
+  const float wk = __ldg(a.w + sol), wf = a.mean ? wk / wk : wk;
+  const float dt = 1.f / __ldg(a.T + sol);
   const int sizes[3] = {N, N, 1};
   if (threadIdx.x == 0) shv[0] = shv[1] = shv[2] = 0;
   __syncthreads();
@@ -282,12 +284,13 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
   float* red = reinterpret_cast<float*>(work + B3::REGION);
   int* shv = reinterpret_cast<int*>(red + 16 * 16);
   float2* X = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;
-  const float2* kp = a.kp + (size_t)world * N * PLANE;  // [N][N][HW], scaled by 1/N^3
+  const int sol = world / a.n_init;
+  const float2* kp = a.kp + (size_t)sol * N * PLANE;  // [N][N][HW], scaled by 1/N^3
   const float* c0 = a.cells0 + (size_t)world * N * N * N;
   float* st = a.state + (size_t)world * N * N * N;
-  const GrowthP gq = big_growth<GF>(a, world);
-  const float wk = __ldg(a.w + world), wf = a.mean ? wk / wk : wk;
-  const float dt = 1.f / __ldg(a.T + world);
+  const GrowthP gq = big_growth<GF>(a, sol);
+  const float wk = __ldg(a.w + sol), wf = a.mean ? wk / wk : wk;
+  const float dt = 1.f / __ldg(a.T + sol);
   const int sizes[3] = {N, N, N};
   const int c = grp;  // column pair of the column passes: (c, N-c); c == 0 carries (0, N/2)
   const int c1 = c != 0 ? c : 0, c2 = c != 0 ? N - c : N / 2;

@@ -163,6 +163,50 @@ Layout layout_of(const lgx_batch_job* j) {
 
 }  // namespace
 
+namespace lgx {
+
+size_t big_rollout_setup_bytes(int n_worlds) {
+  return al256(sizeof(BatchClassArgs) * kMaxBatchClasses) + al256(sizeof(int2) * std::max(n_worlds, 1)) + 256;
+}
+
+long big_kind_scratch(int nb_dims, int size) {
+  const int kind = kind_of(nb_dims, size);
+  return kind >= 0 && is_big(kind) ? batch_scratch_per_cta(kind) : 0;
+}
+
+cudaError_t launch_big_rollout(int nb_dims, int size, const BigArgs& b, int gf_id, int grid, void* setup_ws,
+                               cudaStream_t st) {
+  const int kind = kind_of(nb_dims, size);
+  if (kind < 0 || !is_big(kind)) return cudaErrorInvalidValue;
+  BatchSetup su;
+  std::memset(&su, 0, sizeof(su));
+  su.cls[0].kind = kind;
+  su.cls[0].gf_variant = batch_kind_gf_variant(gf_id);
+  su.cls[0].line_group = 4;
+  su.cls[0].b = b;
+  su.n_cls = 1;
+  su.n_items = b.n_worlds;
+  su.cls_of_rank[0] = 0;
+  su.first_item[0] = 0;
+  for (int r = 1; r <= kMaxBatchClasses; ++r) su.first_item[r] = b.n_worlds;
+  char* base = static_cast<char*>(setup_ws);
+  su.cls_out = reinterpret_cast<BatchClassArgs*>(base);
+  su.items = reinterpret_cast<int2*>(base + al256(sizeof(BatchClassArgs) * kMaxBatchClasses));
+  su.head = reinterpret_cast<int*>(base + al256(sizeof(BatchClassArgs) * kMaxBatchClasses) +
+                                   al256(sizeof(int2) * std::max(b.n_worlds, 1)));
+  cudaError_t e = launch_batch_setup(su, st);
+  if (e != cudaSuccess) return e;
+  MixedArgs ma;
+  ma.n_items = b.n_worlds;
+  ma.n_cls = 1;
+  ma.items = su.items;
+  ma.head = su.head;
+  ma.cls = su.cls_out;
+  return launch_mixed(ma, grid, st);
+}
+
+}  // namespace lgx
+
 extern "C" {
 
 int lgx_batch_workspace_bytes(const lgx_batch_job* j, size_t* bytes) {
@@ -217,6 +261,7 @@ int lgx_batch_run(const lgx_batch_job* j, void* ws, size_t ws_bytes, void* strea
     if (is_big(kind)) {
       BigArgs& b = a.b;
       b.n_worlds = c.n_worlds;
+      b.n_init = 1;
       b.steps = j->steps;
       b.gf_id = c.gf_id;
       b.state_fn = c.state_fn;

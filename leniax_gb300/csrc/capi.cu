@@ -64,14 +64,29 @@ struct Carve {
 
 bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
 
+// 3D worlds of side 32 / 64 with one channel and one kernel: one world per CTA
+// (the plane-fused items of the mixed kernel).
+bool cta_supported(const Model& m) {
+  return m.nb_dims == 3 && m.C == 1 && m.K == 1 && m.D == m.H && m.H == m.W && (m.H == 32 || m.H == 64);
+}
+
 int select_engine(const Model& m, int requested) {
   if (requested == LGX_ENGINE_RESIDENT) return resident_supported(m) ? LGX_ENGINE_RESIDENT : -1;
   if (requested == LGX_ENGINE_STREAMED) return streamed_supported(m) ? LGX_ENGINE_STREAMED : -1;
   if (requested == LGX_ENGINE_PLAIN) return streamed_supported(m) ? LGX_ENGINE_PLAIN : -1;
+  if (requested == LGX_ENGINE_CTA) return cta_supported(m) ? LGX_ENGINE_CTA : -1;
   if (requested != LGX_ENGINE_AUTO) return -1;
   if (resident_supported(m)) return LGX_ENGINE_RESIDENT;
   if (streamed_supported(m)) return LGX_ENGINE_STREAMED;
+  if (cta_supported(m)) return LGX_ENGINE_CTA;
   return -1;
+}
+
+int sm_count_now() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  return sms > 0 ? sms : 1;
 }
 
 // Every lgx_run / lgx_update workspace starts with a 256-byte status block
@@ -83,6 +98,34 @@ size_t resident_ws(const Model& m, int n_sols, int n_init, int steps) {
   b += al256((size_t)n_sols * m.H * resident_kpitch(m.H) * sizeof(float2));
   b += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
   return b;
+}
+
+// CTA engine layout: status, prepared spectra [Ns, N, N, N/2+1], raw moments,
+// class table + queue, state [nw, N^3] (when the caller wants no final cells),
+// per-CTA spectrum scratch.
+struct CtaLayout {
+  size_t kp, raw, setup, state, scratch, end;
+  int grid;
+};
+
+CtaLayout cta_layout(const Model& m, int n_sols, int n_init, int steps) {
+  CtaLayout L;
+  const int nw = n_sols * n_init;
+  const size_t N = (size_t)m.H;
+  size_t off = kStatusBytes;
+  L.kp = off;
+  off += al256((size_t)n_sols * N * N * (N / 2 + 1) * sizeof(float2));
+  L.raw = off;
+  off += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
+  L.setup = off;
+  off += al256(big_rollout_setup_bytes(nw));
+  L.state = off;
+  off += al256((size_t)nw * m.cells * sizeof(float));
+  L.grid = std::max(1, std::min(nw, sm_count_now()));
+  L.scratch = off;
+  off += al256((size_t)L.grid * big_kind_scratch(m.nb_dims, m.H) * sizeof(float2));
+  L.end = off;
+  return L;
 }
 
 size_t streamed_ws(const Model& m, int n_sols, int n_init, int steps, bool with_raw) {
@@ -196,6 +239,7 @@ size_t lgx_run_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init, int
   const int e = select_engine(plan->m, engine);
   if (e == LGX_ENGINE_RESIDENT) return resident_ws(plan->m, n_sols, n_init, steps);
   if (e == LGX_ENGINE_STREAMED || e == LGX_ENGINE_PLAIN) return streamed_ws(plan->m, n_sols, n_init, steps, true);
+  if (e == LGX_ENGINE_CTA) return cta_layout(plan->m, n_sols, n_init, steps).end;
   return 0;
 }
 
@@ -228,7 +272,37 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
   ce = cudaMemsetAsync(ws, 0, sizeof(int), st);  // status word
   if (ce != cudaSuccess) return cuda_fail(ce, "memset");
   float* raw = nullptr;
-  if (e == LGX_ENGINE_RESIDENT) {
+  if (e == LGX_ENGINE_CTA) {
+    if (j->traj_cells || j->traj_field || j->traj_potential)
+      return fail(LGX_ERR_UNSUPPORTED, "lgx_run: the one-world-per-CTA engine (3D worlds) writes no trajectories");
+    const CtaLayout L = cta_layout(m, j->n_sols, j->n_init, j->steps);
+    char* base = static_cast<char*>(ws);
+    float2* kp = reinterpret_cast<float2*>(base + L.kp);
+    raw = reinterpret_cast<float*>(base + L.raw);
+    ce = launch_prepare_3d_spectrum(m.H, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    BigArgs b;
+    std::memset(&b, 0, sizeof(b));
+    b.n_worlds = nw;
+    b.n_init = j->n_init;
+    b.steps = j->steps;
+    b.gf_id = m.gf[0];
+    b.state_fn = m.state_fn;
+    b.mean = m.mean;
+    b.cells0 = j->cells0;
+    b.kp = kp;
+    b.gf = j->gf_params;
+    b.w = j->weights;
+    b.T = j->T;
+    b.state = j->final_cells ? j->final_cells : reinterpret_cast<float*>(base + L.state);
+    b.raw = raw;
+    b.scratch = reinterpret_cast<float2*>(base + L.scratch);
+    b.scratch_per_cta = big_kind_scratch(m.nb_dims, m.H);
+    if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
+    ce = launch_big_rollout(m.nb_dims, m.H, b, m.gf[0], L.grid, base + L.setup, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "one-world-per-CTA rollout");
+    if (j->main_events[1]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[1]), st);
+  } else if (e == LGX_ENGINE_RESIDENT) {
     Carve cv(ws, ws_bytes);
     cv.take<int>(kStatusBytes / sizeof(int));
     float2* kp = cv.take<float2>((size_t)j->n_sols * m.H * resident_kpitch(m.H));

@@ -61,16 +61,17 @@ cudaError_t launch_prepare_resident_spectrum(int N, int n_sols, const float2* k_
 
 // ---------------------------------------------------------------- uneven batch
 // One world per CTA for sizes beyond the resident slices: 2D 256^2 and 3D
-// 32^3 / 64^3.  Every world is its own solution (per-world spectrum and
-// parameters); raw moments are [n_worlds, steps, raw_stride(1)].
+// 32^3 / 64^3.  World w belongs to solution w / n_init (spectrum and
+// parameters per solution; n_init = 1 in uneven batches, where every world is
+// its own solution); raw moments are [n_sols, steps, n_init, raw_stride(1)].
 struct BigArgs {
-  int n_worlds, steps;
+  int n_worlds, n_init, steps;
   int gf_id, state_fn, mean;
   const float* cells0;   // [n_worlds, N^nd]
-  const float2* kp;      // 2D: [n_worlds, N, N/2+2] (resident layout); 3D: [n_worlds, N, N, N/2+1] / N^3
-  const float* gf;       // [n_worlds, 2]
-  const float* w;        // [n_worlds]
-  const float* T;        // [n_worlds]
+  const float2* kp;      // per solution; 2D: [N, N/2+2] (resident layout); 3D: [N, N, N/2+1] / N^3
+  const float* gf;       // [n_sols, 2]
+  const float* w;        // [n_sols]
+  const float* T;        // [n_sols]
   float* state;          // [n_worlds, N^nd]: final cells (updated in place from step 1)
   float* raw;            // [n_worlds, steps, raw_stride(1)]
   float2* scratch;       // [grid, scratch_per_cta] spectrum scratch
@@ -108,6 +109,13 @@ struct BatchSetup {
   int* head;
 };
 cudaError_t launch_batch_setup(const BatchSetup& s, cudaStream_t st);
+// lgx_run's one-world-per-CTA path: one class of big items (3D 32^3 / 64^3
+// or 2D 256^2) through the mixed kernel.  setup_ws holds the class table and
+// queue (big_rollout_setup_bytes), b.scratch grid * big_kind_scratch float2.
+size_t big_rollout_setup_bytes(int n_worlds);
+long big_kind_scratch(int nb_dims, int size);
+cudaError_t launch_big_rollout(int nb_dims, int size, const BigArgs& b, int gf_id, int grid, void* setup_ws,
+                               cudaStream_t st);
 // 3D prepared spectrum: the [n, N, N, N/2+1] half spectrum scaled by 1/N^3.
 cudaError_t launch_prepare_3d_spectrum(int N, long n, const float2* k_half, float2* kp, cudaStream_t st);
 

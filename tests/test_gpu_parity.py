@@ -279,3 +279,63 @@ def test_stop_count_equals_sequential_scan_of_engine_stats(cuda):
         st['channel_mass'] = st['channel_mass']  # [T, Ni, C]
         cont = O.check_heuristics(st)
         np.testing.assert_array_equal(sd['N'][s].cpu().numpy(), cont.sum(axis=0))
+
+
+@pytest.mark.parametrize('size', [32, 64])
+def test_run_scan_mem_optimized_3d_matches_oracle(cuda, size):
+    # 3D worlds through lgx_run's one-world-per-CTA engine (the plane-fused
+    # items): final cells within a few times the oracle's FP32-vs-FP64 spread,
+    # identical N and N_box, mass and centroid close
+    from leniax_gb300 import _lib
+    dev = torch.device('cuda')
+    Ns, Ni, steps, R = 2, 3, 16, size / 6
+    rng = np.random.Generator(np.random.PCG64(size))
+    cells = np.zeros((Ns, Ni, 1, size, size, size), np.float32)
+    p, lo = size // 3, (size - size // 3) // 2
+    cells[..., lo:lo + p, lo:lo + p, lo:lo + p] = rng.random((Ns, Ni, 1, p, p, p), dtype=np.float32)
+    ms = [0.15, 0.22]
+    Ks, gfs, ws = [], [], []
+    upd = None
+    for s in range(Ns):
+        K, mp, u = engine_model(bump_kernel_params(m=ms[s], s=0.03), [size] * 3, 1, R, dev=dev)
+        upd = upd or u
+        Ks.append(K)
+        gfs.append(mp.get_gf_params(dev))
+        ws.append(mp.get_kernels_weight_per_channel(dev))
+    Ts = torch.tensor([10., 5.])
+    stats_fn = statistics.ComputeStatsFn([size] * 3, R, 10)
+    m = upd.model
+    assert _lib.load().lgx_select_engine(m.plan.handle, Ns, Ni, 0) == _lib.ENGINES['cta']
+    sd, fin = runner.run_scan_mem_optimized(None, torch.from_numpy(cells).to(dev), torch.stack(Ks), torch.stack(gfs),
+                                            torch.stack(ws), Ts, steps, R, upd, stats_fn, with_box=True,
+                                            with_centroid=True)
+    for s in range(Ns):
+        res = {}
+        for dt in (np.float32, np.float64):
+            Ko, mpo, model = oracle_model(bump_kernel_params(m=ms[s], s=0.03), [size] * 3, 1, R, dtype=dt)
+            res[dt] = O.run_scan(cells[s].astype(dt), Ko, mpo['gf_params'], mpo['weights'], Ts[s].item(), steps, R,
+                                 model, T_static=10, keep_intermediary=False, with_box=True)
+        st, f64 = res[np.float64]
+        spread = np.abs(res[np.float32][1] - f64).max()
+        assert np.abs(fin[s].cpu().numpy() - f64).max() <= max(2e-4, 8 * spread)
+        np.testing.assert_array_equal(sd['N'][s].cpu().numpy(), st['N'])
+        np.testing.assert_array_equal(sd['N_box'][s].cpu().numpy(), st['N_box'])
+        mass, m64, m32 = sd['mass'][s].cpu().numpy(), st['mass'], res[np.float32][0]['mass']
+        assert (np.abs(mass - m64) <= np.maximum(1e-4 * np.abs(m64), 8 * np.abs(m32 - m64)) + 1e-7).all()
+        cen, c64 = sd['mass_centroid'][s].cpu().numpy(), st['mass_centroid']
+        d = np.abs(cen - c64)
+        d = np.minimum(d, size - d)
+        alive = m64 > 1e-3
+        assert (d[alive] <= 1e-3 * size).all()
+
+
+def test_3d_update_and_trajectories_are_refused(cuda):
+    dev = torch.device('cuda')
+    K, mp, upd = engine_model(bump_kernel_params(), [32, 32, 32], 1, 5, dev=dev)
+    cells = torch.zeros((1, 1, 32, 32, 32), device=dev)
+    from leniax_gb300 import _lib
+    with pytest.raises(_lib.LgxError):
+        upd(None, cells, K, mp.get_gf_params(dev), mp.get_kernels_weight_per_channel(dev), 0.1)
+    with pytest.raises(_lib.LgxError):
+        runner.run_scan(None, cells, K, mp.get_gf_params(dev), mp.get_kernels_weight_per_channel(dev),
+                        torch.tensor(10.), 4, 5, upd, statistics.ComputeStatsFn([32] * 3, 5, 10))
