@@ -42,9 +42,14 @@ struct ACF {
   static_assert(G != 8 || P == 16, "swizzled layout assumes N = 128 for G = 8");
 };
 
-// growth value and its derivatives d/du, d/dm, d/ds (growth_functions.py)
+// growth value and its derivatives d/du, d/dm, d/ds (growth_functions.py);
+// GF selects a compile-time family (GF_FAST_GAUSSIAN: gaussian, GF_FAST_POLY4:
+// poly_quad4, GF_GENERIC: any id) so the unrolled per-cell code stays small
+template <int GF>
 __device__ __forceinline__ void growth_grads(int id, float u, float m, float s, float& g, float& gu, float& gm,
                                              float& gs) {
+  if constexpr (GF == GF_FAST_GAUSSIAN) id = LGX_GF_GAUSSIAN;
+  if constexpr (GF == GF_FAST_POLY4) id = LGX_GF_POLY_QUAD4;
   if (id == LGX_GF_GAUSSIAN || id == LGX_GF_GAUSSIAN_TARGET) {
     const float d = (u - m) / s;
     const float e = expf(-(d * d) / 2.f);
@@ -197,7 +202,7 @@ __device__ __forceinline__ void rows_load(const float2* rowbuf, int s_row, int t
   }
 }
 
-template <int N, int G>
+template <int N, int G, int GF>
 __global__ void __launch_bounds__(512, 1) adjoint_resident_kernel(AdjResArgs a) {
   using CF = ACF<N, G>;
   using GE = typename CF::GE;
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(512, 1) adjoint_resident_kernel(AdjResArgs a) 
             const float sv = __ldg(sp + e * N + x), u = __ldg(up + e * N + x);
             const float lamv = e == 0 ? lam[k1].x : lam[k1].y;
             float g, gu, gm, gs;
-            growth_grads(a.gf_id, u, m, sg, g, gu, gm, gs);
+            growth_grads<GF>(a.gf_id, u, m, sg, g, gu, gm, gs);
             float mu = lamv;
             if (a.state_fn == LGX_STATE_V1 && a.clip_mask) {
               const float nn = sv + dt * (g * wf);
@@ -360,19 +365,26 @@ __global__ void __launch_bounds__(512, 1) adjoint_resident_kernel(AdjResArgs a) 
   }
 }
 
-template <int N, int G>
-cudaError_t launch_n(const AdjResArgs& a, cudaStream_t st) {
+template <int N, int G, int GF>
+cudaError_t launch_gf(const AdjResArgs& a, cudaStream_t st) {
   using CF = ACF<N, G>;
-  cudaError_t e = cudaFuncSetAttribute(adjoint_resident_kernel<N, G>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)CF::SMEM);
+  cudaError_t e = cudaFuncSetAttribute(adjoint_resident_kernel<N, G, GF>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int items = (a.n_worlds + CF::WPC - 1) / CF::WPC;
   const int grid = std::max(1, std::min(items, sms > 0 ? sms : 1));
-  adjoint_resident_kernel<N, G><<<grid, 512, CF::SMEM, st>>>(a);
+  adjoint_resident_kernel<N, G, GF><<<grid, 512, CF::SMEM, st>>>(a);
   return cudaGetLastError();
+}
+
+template <int N, int G>
+cudaError_t launch_n(const AdjResArgs& a, cudaStream_t st) {
+  if (a.gf_id == LGX_GF_GAUSSIAN) return launch_gf<N, G, GF_FAST_GAUSSIAN>(a, st);
+  if (a.gf_id == LGX_GF_POLY_QUAD4) return launch_gf<N, G, GF_FAST_POLY4>(a, st);
+  return launch_gf<N, G, GF_GENERIC>(a, st);
 }
 
 }  // namespace
