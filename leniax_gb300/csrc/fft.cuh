@@ -158,7 +158,9 @@ struct Geo {
   static constexpr int Q = P / G;         // comb members per lane after an exchange
   static constexpr int SCR = N + G;       // float2 per group scratch (padded)
   static_assert(G == 2 || G == 4 || G == 8 || G == 16, "group size");
-  static_assert(P % G == 0 && Q % 2 == 0, "need P/G even (pair-preserving exchanges)");
+  // Q even: the pair-preserving exchanges (a lane holds rows / columns in
+  // pairs); Q == 1: one index per lane (the "identity" sets below)
+  static_assert(P % G == 0 && (Q == 1 || Q % 2 == 0), "need P/G even, or P == G");
 };
 
 // Per-thread twiddle tables kept in shared memory, one N-entry table per
@@ -168,13 +170,16 @@ struct Geo {
 //   rowi  : tw[(q*G + k2)*G + t]      = W_N^(n1r(t,q)*k2),      q < Q, k2 < G
 // where n1c / n1r are the lane's row sets of the column-forward (adjacent
 // pairs) and row-inverse (mirror pairs) mirrored factorisations.
+// With Q == 1 (P == G) both sets are the identity: lane t holds n1 = t.
 template <class GE>
 __device__ __forceinline__ int n1_pairs(int t, int q) {  // q-th n1 of lane t: {2m, 2m+1}, m = t + G*(q/2)
+  if constexpr (GE::Q == 1) return t;
   int m = t + GE::G * (q >> 1);
   return 2 * m + (q & 1);
 }
 template <class GE>
 __device__ __forceinline__ int n1_mirror(int t, int q) {  // {m, P-m} (m>0) or {0, P/2} (m==0), m = t + G*(q/2)
+  if constexpr (GE::Q == 1) return t;
   int m = t + GE::G * (q >> 1);
   if (m == 0) return (q & 1) ? GE::P / 2 : 0;
   return (q & 1) ? GE::P - m : m;
@@ -211,6 +216,7 @@ template <class GE, bool INV, bool PAIRS>
 __device__ __forceinline__ void fft_standard(float2 (&v)[GE::P], float2 (&u)[GE::Q][GE::G], float2* scr,
                                              const float2* tw_std, int t, unsigned gmask) {
   constexpr int G = GE::G, P = GE::P, Q = GE::Q;
+  static_assert(!PAIRS || Q % 2 == 0, "the pair output sets need Q even");
   fft_reg<P, INV>(v);
 #pragma unroll
   for (int k2 = 1; k2 < P; ++k2) {
@@ -256,14 +262,14 @@ __device__ __forceinline__ void fft_mirrored(float2 (&v)[GE::Q][GE::G], float2 (
 #pragma unroll
   for (int q = 0; q < Q; ++q) {
     int n1 = MIRROR ? n1_mirror<GE>(t, q) : n1_pairs<GE>(t, q);
-    int pn = MIRROR ? n1 : ((n1 >> 1) + (n1 & 1) * (P / 2));
+    int pn = (MIRROR || Q == 1) ? n1 : ((n1 >> 1) + (n1 & 1) * (P / 2));
 #pragma unroll
     for (int k2 = 0; k2 < G; ++k2) scr[k2 * (P + 1) + pn] = v[q][k2];
   }
   __syncwarp(gmask);
 #pragma unroll
   for (int n1 = 0; n1 < P; ++n1) {
-    int pn = MIRROR ? n1 : ((n1 >> 1) + (n1 & 1) * (P / 2));
+    int pn = (MIRROR || Q == 1) ? n1 : ((n1 >> 1) + (n1 & 1) * (P / 2));
     w[n1] = scr[t * (P + 1) + pn];
   }
   __syncwarp(gmask);

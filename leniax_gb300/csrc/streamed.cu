@@ -54,7 +54,7 @@ struct SCfg<64> { static constexpr int G = 4; };
 template <>
 struct SCfg<128> { static constexpr int G = 8; };
 template <>
-struct SCfg<256> { static constexpr int G = 8; };
+struct SCfg<256> { static constexpr int G = 16; };  // P = 16 points per lane (Q == 1 transforms)
 template <>
 struct SCfg<512> { static constexpr int G = 16; };
 
@@ -173,19 +173,32 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_con
   const int chunk = grp & 7;
 
   float2 v[Q][G];
-#pragma unroll
-  for (int jp = 0; jp < Q / 2; ++jp) {
-    const int m = t + G * jp;
+  if constexpr (Q == 1) {
+    // lane t carries the unpacked rows n = t + P*n2: packed row n >> 1, the
+    // even row's value for even n, the odd row's for odd n (lanes 2m, 2m+1
+    // read the same 16-byte pair)
 #pragma unroll
     for (int n2 = 0; n2 < G; ++n2) {
-      const int r = m + (P / 2) * n2;
-      const float4 q = *reinterpret_cast<const float4*>(tb + swz128(r, chunk));
-      if (j != 0) {
-        v[2 * jp][n2] = make_float2(q.x + q.z, q.y - q.w);      // 2 X[2r][j]
-        v[2 * jp + 1][n2] = make_float2(q.y + q.w, q.z - q.x);  // 2 X[2r+1][j]
-      } else {
-        v[2 * jp][n2] = make_float2(q.x, q.z);  // X[2r][0] + i X[2r][N/2]
-        v[2 * jp + 1][n2] = make_float2(q.y, q.w);
+      const int n = t + P * n2;
+      const float4 q = *reinterpret_cast<const float4*>(tb + swz128(n >> 1, chunk));
+      if (j != 0) v[0][n2] = (n & 1) ? make_float2(q.y + q.w, q.z - q.x) : make_float2(q.x + q.z, q.y - q.w);
+      else v[0][n2] = (n & 1) ? make_float2(q.y, q.w) : make_float2(q.x, q.z);
+    }
+  } else {
+#pragma unroll
+    for (int jp = 0; jp < Q / 2; ++jp) {
+      const int m = t + G * jp;
+#pragma unroll
+      for (int n2 = 0; n2 < G; ++n2) {
+        const int r = m + (P / 2) * n2;
+        const float4 q = *reinterpret_cast<const float4*>(tb + swz128(r, chunk));
+        if (j != 0) {
+          v[2 * jp][n2] = make_float2(q.x + q.z, q.y - q.w);      // 2 X[2r][j]
+          v[2 * jp + 1][n2] = make_float2(q.y + q.w, q.z - q.x);  // 2 X[2r+1][j]
+        } else {
+          v[2 * jp][n2] = make_float2(q.x, q.z);  // X[2r][0] + i X[2r][N/2]
+          v[2 * jp + 1][n2] = make_float2(q.y, q.w);
+        }
       }
     }
   }
@@ -214,16 +227,27 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_con
       }
     }
     float2 u[Q][G];
-    fft_standard<GE, true, true>(w, u, cs, sm, t, gmask);
-    float4* pd4 = reinterpret_cast<float4*>(prod + ((size_t)n * tab.K + k) * (N / 2) * N);
-#pragma unroll
-    for (int a = 0; a < Q / 2; ++a) {
-      const int m = t + G * a;
+    if constexpr (Q == 1) {
+      // unpacked row n = t + P*k1 -> its half of pair j of packed row n >> 1
+      fft_standard<GE, true, false>(w, u, cs, sm, t, gmask);
+      float2* pd = prod + ((size_t)n * tab.K + k) * (N / 2) * N;
 #pragma unroll
       for (int k1 = 0; k1 < G; ++k1) {
-        const int r = m + (P / 2) * k1;
-        pd4[(size_t)r * (N / 2) + j] = make_float4(u[2 * a][k1].x, u[2 * a][k1].y, u[2 * a + 1][k1].x,
-                                                   u[2 * a + 1][k1].y);
+        const int r = t + P * k1;
+        pd[(size_t)(r >> 1) * N + 2 * j + (r & 1)] = u[0][k1];
+      }
+    } else {
+      fft_standard<GE, true, true>(w, u, cs, sm, t, gmask);
+      float4* pd4 = reinterpret_cast<float4*>(prod + ((size_t)n * tab.K + k) * (N / 2) * N);
+#pragma unroll
+      for (int a = 0; a < Q / 2; ++a) {
+        const int m = t + G * a;
+#pragma unroll
+        for (int k1 = 0; k1 < G; ++k1) {
+          const int r = m + (P / 2) * k1;
+          pd4[(size_t)r * (N / 2) + j] = make_float4(u[2 * a][k1].x, u[2 * a][k1].y, u[2 * a + 1][k1].x,
+                                                     u[2 * a + 1][k1].y);
+        }
       }
     }
   }
@@ -366,7 +390,23 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     const int it = items[i], k = item_k(it), co = item_co(it);
     float2* row = bufs + (i & 1) * RC::BUF + grp * ROWP;
     float2 v[Q][G];
-    unpack_row_pair_pa<GE>(row, v, t);
+    if constexpr (Q == 1) {
+      // lane t needs Z[k], k = t + P*n2: one pair load each (k < N/2 for n2 < G/2)
+      const float4* p4 = reinterpret_cast<const float4*>(row);
+#pragma unroll
+      for (int n2 = 0; n2 < G; ++n2) {
+        const int k = t + P * n2;
+        if (n2 < G / 2) {
+          const float4 q = p4[k];  // k == 0: pair 0 = (DC, Nyquist)
+          v[0][n2] = k == 0 ? make_float2(q.x, q.z) : make_float2(q.x - q.w, q.y + q.z);
+        } else {
+          const float4 q = p4[k == N / 2 ? 0 : N - k];
+          v[0][n2] = k == N / 2 ? make_float2(q.y, q.w) : make_float2(q.x + q.w, q.z - q.y);
+        }
+      }
+    } else {
+      unpack_row_pair_pa<GE>(row, v, t);
+    }
     __syncwarp(gmask);
     float2 w[P];
     fft_mirrored<GE, true, true>(v, w, row, tw + 2 * N, t, gmask);
