@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(kT) col_adj_kernel(int n_worlds, int n_init, c
                                                      float2* __restrict__ gk, float2* __restrict__ prod) {
   constexpr int G = ACfg<N>::G;
   using GE = Geo<N, G>;
-  constexpr int P = GE::P, GPB = kT / G, BPP = (N / 2 + GPB - 1) / GPB, KP = N / 2 + 2;
+  constexpr int P = GE::P, GPB = kT / G, BPP = (N / 2 + GPB - 1) / GPB;
   extern __shared__ __align__(16) float2 sm[];
   float2* scr = twiddles<N>(sm);
   __syncthreads();
@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kT) col_adj_kernel(int n_worlds, int n_init, c
     for (int k1 = 0; k1 < P; ++k1) {
       const int ky = t + G * k1;
       g[ky] = cadd(g[ky], cmulc(wa[k1], ws[k1]));
-      wa[k1] = cmulc(wa[k1], __ldg(kk + ky * KP + c));
+      wa[k1] = cmulc(wa[k1], __ldg(kk + (size_t)c * N + ky));
     }
   } else {
     // unpack DC / Nyquist columns of a and s through the scratch mirror
@@ -344,7 +344,7 @@ __global__ void __launch_bounds__(kT) col_adj_kernel(int n_worlds, int n_init, c
       const float2 g0 = cmulc(a0, s0), gN = cmulc(aN, sN);
       g[ky] = cadd(g[ky], make_float2(g0.x - gN.y, g0.y + gN.x));  // g0 + i gN
       // correlation: Q = C conj(A) + conj(C-) conj(B)
-      const float2 A = __ldg(kk + ky * KP), B = __ldg(kk + ky * KP + N / 2);
+      const float2 A = __ldg(kk + ky), B = __ldg(kk + (N / 2) * N + ky);
       wa[k1] = cadd(cmulc(wa[k1], A), cmulc(conjf2(ma[k1]), B));
     }
     __syncwarp(gmask);

@@ -570,7 +570,12 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   a.prod = cv.take<float2>(nw * cells / 2);
   a.partial = cv.take<float>(nw * 64 * 3);
   if (!cv.fits()) return fail(LGX_ERR_WORKSPACE, "lgx_adjoint: internal workspace layout exceeds its size query");
-  cudaError_t ce = launch_prepare_streamed_spectrum(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
+  // the resident adjoint reads the row-major prepared planes, the streamed one
+  // the column-major planes
+  const bool resident = adjoint_resident_supported(m);
+  cudaError_t ce =
+      resident ? launch_prepare_resident_spectrum(m.H, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st)
+               : launch_prepare_streamed_spectrum(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
   if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
   a.n_sols = j->n_sols;
   a.n_init = j->n_init;
@@ -590,7 +595,7 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   a.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
   a.grad_gf = j->grad_gf;
   a.grad_w = j->grad_weights;
-  if (adjoint_resident_supported(m)) {
+  if (resident) {
     // resident sizes: one persistent launch for the whole segment
     AdjResArgs r;
     r.n_worlds = (int)nw;

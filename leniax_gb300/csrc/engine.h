@@ -130,7 +130,7 @@ struct StreamedStep {
   int n_worlds, n_init;
   const float* state;      // [n_worlds, C, *world]
   float* state_out;        // [n_worlds, C, *world]
-  const float2* kp;        // [Ns, C, max_k, H, W/2+2] prepared (scaled) spectra, per solution
+  const float2* kp;        // [Ns, C, max_k, W/2+2, H] prepared (scaled) spectra, column-major, per solution
   long kp_sol_stride;      // float2 elements between solutions (0: shared)
   const float* gf;         // [Ns, K, 2]
   long gf_sol_stride;

@@ -8,8 +8,9 @@
 //   col_conv : per (world, channel, block of column pairs) the block's column
 //              tile arrives by TMA (2D tensor copies, 128-byte swizzle); per
 //              pair: unpack + N-point FFT, then for every kernel reading that
-//              channel: x prepared spectrum, inverse FFT -> prod[n][k] (same
-//              layout, 16-byte pair stores)
+//              channel: x prepared spectrum (column-major planes, so a
+//              transform's lanes read consecutive ky), inverse FFT -> prod[n][k] (same
+//              pair-adjacent layout)
 //   row_inv  : per (world, block of packed rows) the block's rows of every
 //              kernel's product plane arrive by bulk copies into a double
 //              buffer (the next kernel's rows land while this kernel's are
@@ -216,13 +217,14 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_con
     const float2* kk = kp + sol * kp_sol_stride + ((size_t)(ch * tab.max_k + tab.slot[k]) * N) * KPITCH;
     float2 w[P];
     if (j != 0) {
+      const float2* kc = kk + (size_t)j * N + t;
 #pragma unroll
-      for (int k1 = 0; k1 < P; ++k1) w[k1] = cmul(w0[k1], __ldg(kk + (t + G * k1) * KPITCH + j));
+      for (int k1 = 0; k1 < P; ++k1) w[k1] = cmul(w0[k1], __ldg(kc + G * k1));
     } else {
 #pragma unroll
       for (int k1 = 0; k1 < P; ++k1) {
         const int ky = t + G * k1;
-        const float2 A = __ldg(kk + ky * KPITCH), B = __ldg(kk + ky * KPITCH + N / 2);
+        const float2 A = __ldg(kk + ky), B = __ldg(kk + (N / 2) * N + ky);
         w[k1] = cadd(cmul(w0[k1], A), cmul(conjf2(mirror[(N - ky) & (N - 1)]), B));
       }
     }
@@ -586,10 +588,13 @@ __global__ void prepare_streamed_kernel(long n_planes, const float2* __restrict_
   constexpr int KP = N / 2 + 2, HW = N / 2 + 1;
   const float scale = 1.f / (2.f * (float)N * (float)N);
   const long total = n_planes * N * KP;
+  // column-major planes: element (ky, c) at c * N + ky, so the lanes of a
+  // column transform read consecutive ky
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const int c = (int)(i % KP);
-    const long row = i / KP;
-    const float2* src = kh + row * HW;
+    const int ky = (int)(i % N);
+    const long pc = i / N;
+    const int c = (int)(pc % KP);
+    const float2* src = kh + ((pc / KP) * N + ky) * HW;
     float2 o = make_float2(0.f, 0.f);
     if (c == 0) {
       float2 k0 = src[0], kn = src[N / 2];

@@ -68,6 +68,22 @@ def test_adjoint_matches_float64_autograd_ste(cuda, slug):
     assert abs(gw) <= 1e-6 and abs(rw) <= 1e-9  # weighted_mean with one kernel: f = g, no w dependence
 
 
+def test_adjoint_streamed_size_matches_float64_autograd(cuda):
+    # 256x256 worlds take the streamed adjoint (spectra through global memory,
+    # column-major kernel spectrum planes), not the resident one
+    size, R, steps, T, w, m, s = 256, 20, 8, 10.0, 1.0, 0.15, 0.02
+    upd, k_real, cells, target = _setup(cuda, size=size, R=R, steps=steps, n_init=1, seed=13, m=m, s=s)
+    L, gc, gk, gm, gs, gw = _engine_grads(cuda, upd, k_real, cells, target, m, s, w, T, steps, 'ste', ckpt=3)
+    kref = k_real.detach().cpu().double().numpy()
+    Lr, (rc, rk, rm, rs, rw) = GO.loss_and_grads(cells.astype(np.float64), kref, m, s, w, 1 / T, steps, target,
+                                                 clip='ste')
+    assert abs(L - Lr) <= 1e-5 * abs(Lr) + 1e-9
+    assert relerr(gc, rc) <= REL
+    assert relerr(gk, rk) <= REL
+    assert abs(gm - rm) <= REL * abs(rm) + 1e-9
+    assert abs(gs - rs) <= REL * abs(rs) + 1e-9
+
+
 def test_adjoint_mask_clip_matches_float64_autograd(cuda):
     # mask clip = the exact derivative of the clipped map.  The clipped map has
     # kinks wherever a cell's s + dt f crosses 0 or 1, so central differences
