@@ -273,6 +273,7 @@ struct RowInvCfg {
   static constexpr int BPW = (N / 2) / GPB;  // blocks per world
   static constexpr int ROWP = N + G;         // staged row pitch (float2) == Geo<N, G>::SCR
   static constexpr int BUF = GPB * ROWP;     // float2 per buffer
+  static constexpr int NBUF = 2;             // staging ring depth (items in flight: NBUF - 1)
 };
 
 // item word: bit 16 = count the potential, bits 8..15 = output channel + 1 (0: none), bits 0..7 = kernel
@@ -283,10 +284,9 @@ __device__ __forceinline__ bool item_count(int it) { return (it >> 16) & 1; }
 template <int N>
 size_t row_inv_smem(int C, int K) {
   using RC = RowInvCfg<N>;
-  return (size_t)2 * RC::BUF * sizeof(float2) + (size_t)3 * N * sizeof(float2) +
+  return (size_t)RC::NBUF * RC::BUF * sizeof(float2) + (size_t)3 * N * sizeof(float2) +
          (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float) + 16 * sizeof(uint64_t) +
-         (size_t)RC::GPB * RC::ROWP * sizeof(float2) + (size_t)kMaxChannels * sizeof(float) +
-         (size_t)(C * K + K + 1) * sizeof(int);
+         (size_t)kMaxChannels * sizeof(float) + (size_t)(C * K + K + 1) * sizeof(int);
 }
 
 template <int N, int GF>
@@ -297,19 +297,18 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     float* __restrict__ pot_out, const int* __restrict__ shift, float* __restrict__ partial, int* __restrict__ status,
     float2* __restrict__ spec_next) {
   using RC = RowInvCfg<N>;
-  constexpr int G = RC::G, GPB = RC::GPB, BPW = RC::BPW, ROWP = RC::ROWP;
+  constexpr int G = RC::G, GPB = RC::GPB, BPW = RC::BPW, ROWP = RC::ROWP, NBUF = RC::NBUF;
   using GE = Geo<N, G>;
   constexpr int P = GE::P, Q = GE::Q;
   constexpr int RAWS_MAX = RAW_CM + kMaxChannels;
   constexpr int NWARPS = RC::T / 32;
   static_assert(ROWP == GE::SCR, "a staged row doubles as the group's FFT scratch");
   extern __shared__ __align__(16) float2 sm[];
-  float2* bufs = sm;                    // [2][GPB][ROWP]
-  float2* tw = bufs + 2 * RC::BUF;      // 3N twiddles
+  float2* bufs = sm;                    // [NBUF][GPB][ROWP] staging ring
+  float2* tw = bufs + NBUF * RC::BUF;   // 3N twiddles
   float* red = reinterpret_cast<float*>(tw + 3 * N);  // [warps][RAWS_MAX]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(red + NWARPS * RAWS_MAX);  // 2 (16 slots reserved)
-  float2* fscr = reinterpret_cast<float2*>(bars + 16);                    // [GPB][ROWP] next-step row FFT scratch
-  float* wsum_s = reinterpret_cast<float*>(fscr + GPB * ROWP);            // [kMaxChannels]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(red + NWARPS * RAWS_MAX);  // NBUF (16 slots reserved)
+  float* wsum_s = reinterpret_cast<float*>(bars + 16);                    // [kMaxChannels]
   int* items = reinterpret_cast<int*>(wsum_s + kMaxChannels);
   __shared__ int s_nitems;
 
@@ -325,8 +324,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   const float* wt = wts + sol * w_sol_stride;
 
   if (threadIdx.x == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
+    for (int b = 0; b < NBUF; ++b) mbar_init(&bars[b], 1);
     fence_proxy_async();
     // work items and per-channel weight sums
     int ni = 0;
@@ -351,16 +349,17 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   __syncthreads();
   const int nit = s_nitems;
 
-  // warp 0 stages item i's GPB product rows into buffer i & 1
+  // warp 0 stages item i's GPB product rows into ring slot i % NBUF
   auto issue = [&](int i) {
-    const int b = i & 1;
+    const int b = i % NBUF;
     const float2* src = prod + (((size_t)n * K + item_k(items[i])) * (N / 2) + r0) * N;
     float2* dst = bufs + b * RC::BUF;
     if (lane == 0) mbar_arrive_expect_tx(&bars[b], (unsigned)(GPB * N * sizeof(float2)));
     __syncwarp();
     for (int g = lane; g < GPB; g += 32) bulk_load(dst + g * ROWP, src + (size_t)g * N, N * sizeof(float2), &bars[b]);
   };
-  if (wid == 0 && nit > 0) issue(0);
+  if (wid == 0)
+    for (int q = 0; q < NBUF - 1 && q < nit; ++q) issue(q);
 
   float dt;
   if (tab.dt_mode == 0) dt = __ldg(dtp);
@@ -379,18 +378,18 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   // item i: wait for its rows, inverse row transform, count / write the
   // potential, accumulate the weighted growth of channel co (co >= 0)
   auto process = [&](int i) {
-    __syncthreads();  // every group is done with buffer (i + 1) & 1 (item i - 1)
-    if (wid == 0 && i + 1 < nit) {
+    __syncthreads();  // every group is done with slot (i - 1) % NBUF (item i - 1, or the fused row FFT)
+    if (wid == 0 && i + NBUF - 1 < nit) {
       fence_proxy_async();
-      issue(i + 1);
+      issue(i + NBUF - 1);
     }
-    if (__syncthreads_or(!mbar_wait(&bars[i & 1], (i >> 1) & 1))) {
+    if (__syncthreads_or(!mbar_wait(&bars[i % NBUF], (i / NBUF) & 1))) {
       failed = true;
       failed_at = i;
       return;
     }
     const int it = items[i], k = item_k(it), co = item_co(it);
-    float2* row = bufs + (i & 1) * RC::BUF + grp * ROWP;
+    float2* row = bufs + (i % NBUF) * RC::BUF + grp * ROWP;
     float2 v[Q][G];
     if constexpr (Q == 1) {
       // lane t needs Z[k], k = t + P*n2: one pair load each (k < N/2 for n2 < G/2)
@@ -493,9 +492,12 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     const float cms = warp_sum(Sa + Sb);
     if (lane == 0) red[wid * RAWS_MAX + RAW_CM + co] = cms;
     if (spec_next) {
-      // the next step's row pass, fused: FFT of the packed new rows -> its spectrum plane
+      // the next step's row pass, fused: FFT of the packed new rows -> its
+      // spectrum plane.  Exchange scratch: this group's row of ring slot
+      // (i - 1) % NBUF, the one slot with no copy in flight (items i ..
+      // i + NBUF - 2 are); the next process() barrier orders it before reuse.
       float2 u[Q][G];
-      fft_standard<GE, false, false>(nsv, u, fscr + grp * ROWP, tw, t, gmask);
+      fft_standard<GE, false, false>(nsv, u, bufs + ((i + NBUF - 1) % NBUF) * RC::BUF + grp * ROWP, tw, t, gmask);
       float2* dst = spec_next + (((size_t)n * C + co) * (N / 2) + r) * N;
 #pragma unroll
       for (int q = 0; q < Q; ++q)
@@ -509,8 +511,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     // bounded time to drain, leave without writing moments
     if (threadIdx.x == 0 && status) atomicExch(status, kStatusCopyTimeout);
     const int f = failed_at;
-    mbar_wait(&bars[f & 1], (f >> 1) & 1);
-    if (f + 1 < nit) mbar_wait(&bars[(f + 1) & 1], ((f + 1) >> 1) & 1);
+    for (int q = f; q < f + NBUF && q < nit; ++q) mbar_wait(&bars[q % NBUF], (q / NBUF) & 1);
     return;
   }
   // block reduction: warp shuffles then shared memory
