@@ -98,6 +98,22 @@ struct GrowthP {
   int id;
 };
 
+// The fast growth forms are 2 e(x) - 1; growth_core returns e(x), so a
+// weighted sum of growths can accumulate 2 w e(x) and subtract sum(w) once.
+template <int GF>
+__device__ __forceinline__ float growth_core(const GrowthP& g, float x) {
+  static_assert(GF == GF_FAST_GAUSSIAN || GF == GF_FAST_POLY4, "2 e(x) - 1 forms only");
+  if constexpr (GF == GF_FAST_GAUSSIAN) {
+    const float d = (x - g.m) * g.a;
+    return fast_exp2(-(d * d));
+  } else {
+    const float d = x - g.m;
+    float o = fmaxf(0.f, fmaf(-(d * d), g.a, 1.f));
+    o = o * o;
+    return o * o;
+  }
+}
+
 template <int GF>
 __device__ __forceinline__ float growth_cell(const GrowthP& g, float x) {
   if constexpr (GF == GF_FAST_GAUSSIAN) {

@@ -273,7 +273,7 @@ struct RowInvCfg {
   static constexpr int BPW = (N / 2) / GPB;  // blocks per world
   static constexpr int ROWP = N + G;         // staged row pitch (float2) == Geo<N, G>::SCR
   static constexpr int BUF = GPB * ROWP;     // float2 per buffer
-  static constexpr int NBUF = 2;             // staging ring depth (items in flight: NBUF - 1)
+  static constexpr int NBUF = 3;             // staging ring depth (items in flight: NBUF - 1)
 };
 
 // item word: bit 16 = count the potential, bits 8..15 = output channel + 1 (0: none), bits 0..7 = kernel
@@ -286,7 +286,8 @@ size_t row_inv_smem(int C, int K) {
   using RC = RowInvCfg<N>;
   return (size_t)RC::NBUF * RC::BUF * sizeof(float2) + (size_t)3 * N * sizeof(float2) +
          (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float) + 16 * sizeof(uint64_t) +
-         (size_t)kMaxChannels * sizeof(float) + (size_t)(C * K + K + 1) * sizeof(int);
+         (size_t)kMaxChannels * sizeof(float) + (size_t)(C * K + K + 1) * sizeof(int) +
+         (size_t)(C * K + K + 1) * sizeof(float4) + (size_t)(C * K + 2 * K) * sizeof(float);
 }
 
 template <int N, int GF>
@@ -308,8 +309,8 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   float2* tw = bufs + NBUF * RC::BUF;   // 3N twiddles
   float* red = reinterpret_cast<float*>(tw + 3 * N);  // [warps][RAWS_MAX]
   uint64_t* bars = reinterpret_cast<uint64_t*>(red + NWARPS * RAWS_MAX);  // NBUF (16 slots reserved)
-  float* wsum_s = reinterpret_cast<float*>(bars + 16);                    // [kMaxChannels]
-  int* items = reinterpret_cast<int*>(wsum_s + kMaxChannels);
+  float* wsum_s = reinterpret_cast<float*>(bars + 16);  // [kMaxChannels]
+  float4* ipar = reinterpret_cast<float4*>(wsum_s + kMaxChannels);  // [C*K + K + 1] per item: weight, m, s, a
   __shared__ int s_nitems;
 
   const int n = blockIdx.x / BPW;
@@ -322,30 +323,46 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   const int C = tab.C, K = tab.K;
   const float* gf = gfp + sol * gf_sol_stride;
   const float* wt = wts + sol * w_sol_stride;
+  int* items = reinterpret_cast<int*>(ipar + (C * K + K + 1));  // [C*K + K + 1] item words
+  float* wgf = reinterpret_cast<float*>(items + (C * K + K + 1));  // [C*K] weights, then [K][2] (m, s)
 
+  // the solution's weights and growth parameters, one coalesced pass
+  for (int q = threadIdx.x; q < C * K + 2 * K; q += blockDim.x)
+    wgf[q] = q < C * K ? __ldg(wt + q) : __ldg(gf + (q - C * K));
+  init_twiddles<GE>(tw, tw + N, tw + 2 * N, threadIdx.x, blockDim.x);
+  __syncthreads();
   if (threadIdx.x == 0) {
     for (int b = 0; b < NBUF; ++b) mbar_init(&bars[b], 1);
     fence_proxy_async();
-    // work items and per-channel weight sums
+    // work items with their growth parameters, and per-channel weight sums
     int ni = 0;
     unsigned long long seen = 0ull;
+    auto param = [&](float w, int k) {
+      const float m = wgf[C * K + 2 * k], sg = wgf[C * K + 2 * k + 1];
+      const float a = GF == GF_FAST_GAUSSIAN ? 0.84932180028801904272f / sg
+                                             : (GF == GF_FAST_POLY4 ? 1.f / (9.f * (sg * sg)) : 0.f);
+      return make_float4(w, m, sg, a);
+    };
     for (int co = 0; co < C; ++co) {
       float ws = 0.f;
       for (int k = 0; k < K; ++k) {
-        const float w = __ldg(wt + co * K + k);
+        const float w = wgf[co * K + k];
         ws += w;
         if (w == 0.f) continue;
         const bool first = !((seen >> k) & 1ull);
         seen |= 1ull << k;
+        ipar[ni] = param(w, k);
         items[ni++] = (first ? (1 << 16) : 0) | ((co + 1) << 8) | k;
       }
       wsum_s[co] = ws;
     }
     for (int k = 0; k < K; ++k)
-      if (!((seen >> k) & 1ull)) items[ni++] = (1 << 16) | k;
+      if (!((seen >> k) & 1ull)) {
+        ipar[ni] = param(0.f, k);
+        items[ni++] = (1 << 16) | k;
+      }
     s_nitems = ni;
   }
-  init_twiddles<GE>(tw, tw + N, tw + 2 * N, threadIdx.x, blockDim.x);
   __syncthreads();
   const int nit = s_nitems;
 
@@ -377,16 +394,19 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
 
   // item i: wait for its rows, inverse row transform, count / write the
   // potential, accumulate the weighted growth of channel co (co >= 0)
+  // One block barrier per item: past it, item i has landed for every thread
+  // and every group is done with slot (i - 1) % NBUF (item i - 1, or the
+  // fused row FFT's scratch), so warp 0 refills that slot with item
+  // i + NBUF - 1.
   auto process = [&](int i) {
-    __syncthreads();  // every group is done with slot (i - 1) % NBUF (item i - 1, or the fused row FFT)
-    if (wid == 0 && i + NBUF - 1 < nit) {
-      fence_proxy_async();
-      issue(i + NBUF - 1);
-    }
     if (__syncthreads_or(!mbar_wait(&bars[i % NBUF], (i / NBUF) & 1))) {
       failed = true;
       failed_at = i;
       return;
+    }
+    if (wid == 0 && i + NBUF - 1 < nit) {
+      fence_proxy_async();
+      issue(i + NBUF - 1);
     }
     const int it = items[i], k = item_k(it), co = item_co(it);
     float2* row = bufs + (i % NBUF) * RC::BUF + grp * ROWP;
@@ -424,17 +444,22 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
       }
     }
     if (co >= 0) {
-      const float wk = __ldg(wt + co * K + k);
+      const float4 ip = ipar[i];
+      const float wk = ip.x;
       GrowthP g;
-      g.m = __ldg(gf + 2 * k);
-      g.s = __ldg(gf + 2 * k + 1);
+      g.m = ip.y;
+      g.s = ip.z;
+      g.a = ip.w;
       g.id = tab.gf[k];
-      g.a = GF == GF_FAST_GAUSSIAN ? 0.84932180028801904272f / g.s
-                                   : (GF == GF_FAST_POLY4 ? 1.f / (9.f * (g.s * g.s)) : 0.f);
 #pragma unroll
       for (int k1 = 0; k1 < P; ++k1) {
-        acc[k1].x = fmaf(wk, growth_cell<GF>(g, w[k1].x), acc[k1].x);
-        acc[k1].y = fmaf(wk, growth_cell<GF>(g, w[k1].y), acc[k1].y);
+        if constexpr (GF == GF_GENERIC) {
+          acc[k1].x = fmaf(wk, growth_cell<GF>(g, w[k1].x), acc[k1].x);
+          acc[k1].y = fmaf(wk, growth_cell<GF>(g, w[k1].y), acc[k1].y);
+        } else {  // w (2 e - 1) summed as 2 w e here, minus the channel's weight sum below
+          acc[k1].x = fmaf(2.f * wk, growth_core<GF>(g, w[k1].x), acc[k1].x);
+          acc[k1].y = fmaf(2.f * wk, growth_core<GF>(g, w[k1].y), acc[k1].y);
+        }
       }
     }
   };
@@ -457,6 +482,10 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     for (int k1 = 0; k1 < P; ++k1) {
       const int x = t + G * k1;
       float fa = acc[k1].x, fb = acc[k1].y;
+      if constexpr (GF != GF_GENERIC) {
+        fa -= wsum;
+        fb -= wsum;
+      }
       if (tab.mean) {
         fa = fa / wsum;
         fb = fb / wsum;
@@ -511,7 +540,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     // bounded time to drain, leave without writing moments
     if (threadIdx.x == 0 && status) atomicExch(status, kStatusCopyTimeout);
     const int f = failed_at;
-    for (int q = f; q < f + NBUF && q < nit; ++q) mbar_wait(&bars[q % NBUF], (q / NBUF) & 1);
+    for (int q = f; q < f + NBUF - 1 && q < nit; ++q) mbar_wait(&bars[q % NBUF], (q / NBUF) & 1);  // issued: <= f + NBUF - 2
     return;
   }
   // block reduction: warp shuffles then shared memory
