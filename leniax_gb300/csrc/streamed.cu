@@ -118,6 +118,11 @@ struct ColCfg {
   static constexpr int BOXES = GPB / 8;            // TMA boxes: 8 pairs (128 bytes) x N/2 rows
   static constexpr int BOX_BYTES = (N / 2) * 128;
   static constexpr int TILE_BYTES = BOXES * BOX_BYTES;
+  // kernel spectrum columns staged by bulk copy (GPB columns + the Nyquist
+  // column for the block holding pair 0); off at N = 512, where the extra
+  // shared memory would cost a resident block per SM
+  static constexpr bool KSTAGE = N <= 256;
+  static constexpr int KB_BYTES = KSTAGE ? (GPB + 1) * N * 8 : 0;
   static_assert(GPB % 8 == 0 && (N / 2) % GPB == 0, "column tile");
 };
 
@@ -125,17 +130,31 @@ template <int N>
 constexpr size_t col_conv_smem() {
   using CC = ColCfg<N>;
   using GE = Geo<N, CC::G>;
-  // 1024 bytes of alignment slack for the swizzled tile, tile, twiddles,
-  // group scratch, DC/Nyquist mirror, mbarrier
-  return 1024 + (size_t)CC::TILE_BYTES + (size_t)3 * N * sizeof(float2) + (size_t)CC::GPB * GE::SCR * sizeof(float2) +
-         (size_t)N * sizeof(float2) + 16;
+  // 1024 bytes of alignment slack for the swizzled tile, tile (the column
+  // input, then the output staging), staged kernel columns, twiddles, group
+  // scratch, DC/Nyquist mirror, two mbarriers
+  return 1024 + (size_t)CC::TILE_BYTES + (size_t)CC::KB_BYTES + (size_t)3 * N * sizeof(float2) +
+         (size_t)CC::GPB * GE::SCR * sizeof(float2) + (size_t)N * sizeof(float2) + 16;
 }
 
+// Next kernel after k (or K) reading channel ch.
+__device__ __forceinline__ int next_kernel(const KTab& tab, int k, int ch) {
+  for (++k; k < tab.K; ++k)
+    if (tab.cin[k] == ch) break;
+  return k;
+}
+
+// One block: GPB column pairs of one (world, channel) plane.  The column tile
+// arrives by TMA; per kernel reading the channel, the kernel's GPB spectrum
+// columns arrive by bulk copy (issued one kernel ahead), and the product
+// columns leave through the same swizzled tile by TMA stores, so the kernel's
+// global traffic bypasses the load/store pipe.
 template <int N>
 __global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_constant__ CUtensorMap spec_map,
+                                                               const __grid_constant__ CUtensorMap prod_map,
                                                                int n_worlds, int n_init, KTab tab,
                                                                const float2* __restrict__ kp, long kp_sol_stride,
-                                                               float2* __restrict__ prod, int* __restrict__ status) {
+                                                               int* __restrict__ status) {
   using CC = ColCfg<N>;
   constexpr int G = CC::G, GPB = CC::GPB, BPP = CC::BPP;
   using GE = Geo<N, G>;
@@ -143,34 +162,52 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_con
   constexpr int KPITCH = N / 2 + 2;
   extern __shared__ __align__(16) unsigned char smraw[];
   unsigned char* tile = smraw + ((1024u - (smem_u32(smraw) & 1023u)) & 1023u);
-  float2* sm = reinterpret_cast<float2*>(tile + CC::TILE_BYTES);
+  float2* kb = reinterpret_cast<float2*>(tile + CC::TILE_BYTES);  // [GPB + 1][N] kernel columns
+  float2* sm = reinterpret_cast<float2*>(tile + CC::TILE_BYTES + CC::KB_BYTES);
   float2* scr = sm + 3 * N;
   float2* mirror = scr + GPB * GE::SCR;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(mirror + N);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(mirror + N);  // [0]: column tile, [1]: kernel columns
   const int plane = blockIdx.x / BPP;  // n*C + c
   if (plane >= n_worlds * tab.C) return;
   const int j0 = (blockIdx.x % BPP) * GPB;
+  const int n = plane / tab.C, ch = plane % tab.C;
+  const int sol = n / n_init;
+  auto kplane = [&](int k) {
+    return kp + sol * kp_sol_stride + ((size_t)(ch * tab.max_k + tab.slot[k]) * N) * KPITCH;
+  };
+  // kernel k's columns j0 .. j0 + GPB - 1 (+ column N/2 for pair 0) -> kb
+  auto issue_kernel = [&](int k) {
+    const unsigned main = GPB * N * sizeof(float2), nyq = j0 == 0 ? N * sizeof(float2) : 0u;
+    mbar_arrive_expect_tx(&bar[1], main + nyq);
+    const float2* kk = kplane(k);
+    bulk_load(kb, kk + (size_t)j0 * N, main, &bar[1]);
+    if (nyq) bulk_load(kb + GPB * N, kk + (size_t)(N / 2) * N, nyq, &bar[1]);
+  };
+  const int k_first = next_kernel(tab, -1, ch);
   if (threadIdx.x == 0) {
-    mbar_init(bar, 1);
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
     fence_proxy_async();
-    mbar_arrive_expect_tx(bar, CC::TILE_BYTES);
+    mbar_arrive_expect_tx(&bar[0], CC::TILE_BYTES);
     for (int b = 0; b < CC::BOXES; ++b)
-      tma_load_2d(tile + b * CC::BOX_BYTES, &spec_map, (j0 + 8 * b) * 4, plane * (N / 2), bar);
+      tma_load_2d(tile + b * CC::BOX_BYTES, &spec_map, (j0 + 8 * b) * 4, plane * (N / 2), &bar[0]);
+    if (CC::KSTAGE && k_first < tab.K) issue_kernel(k_first);
   }
   init_twiddles<GE>(sm, sm + N, sm + 2 * N, threadIdx.x, blockDim.x);
   __syncthreads();
-  if (__syncthreads_or(!mbar_wait(bar, 0))) {  // the tile never landed: record, drain, leave
-    if (threadIdx.x == 0 && status) atomicExch(status, kStatusCopyTimeout);
-    mbar_wait(bar, 0);
+  if (__syncthreads_or(!mbar_wait(&bar[0], 0))) {  // the tile never landed: record, drain, leave
+    if (threadIdx.x == 0) {
+      if (status) atomicExch(status, kStatusCopyTimeout);
+      mbar_wait(&bar[0], 0);
+      if (CC::KSTAGE && k_first < tab.K) mbar_wait(&bar[1], 0);
+    }
     return;
   }
-  const int n = plane / tab.C, ch = plane % tab.C;
-  const int sol = n / n_init;
   const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31;
   const int j = j0 + grp;  // column pair (j, N-j); j == 0 carries (0, N/2)
   const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
   float2* cs = scr + grp * GE::SCR;
-  const unsigned char* tb = tile + (grp >> 3) * CC::BOX_BYTES;
+  unsigned char* tb = tile + (grp >> 3) * CC::BOX_BYTES;
   const int chunk = grp & 7;
 
   float2 v[Q][G];
@@ -180,10 +217,10 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_con
     // read the same 16-byte pair)
 #pragma unroll
     for (int n2 = 0; n2 < G; ++n2) {
-      const int n = t + P * n2;
-      const float4 q = *reinterpret_cast<const float4*>(tb + swz128(n >> 1, chunk));
-      if (j != 0) v[0][n2] = (n & 1) ? make_float2(q.y + q.w, q.z - q.x) : make_float2(q.x + q.z, q.y - q.w);
-      else v[0][n2] = (n & 1) ? make_float2(q.y, q.w) : make_float2(q.x, q.z);
+      const int r = t + P * n2;
+      const float4 q = *reinterpret_cast<const float4*>(tb + swz128(r >> 1, chunk));
+      if (j != 0) v[0][n2] = (r & 1) ? make_float2(q.y + q.w, q.z - q.x) : make_float2(q.x + q.z, q.y - q.w);
+      else v[0][n2] = (r & 1) ? make_float2(q.y, q.w) : make_float2(q.x, q.z);
     }
   } else {
 #pragma unroll
@@ -212,47 +249,70 @@ __global__ void __launch_bounds__(ColCfg<N>::T) col_conv_kernel(const __grid_con
     for (int k1 = 0; k1 < P; ++k1) mirror[t + G * k1] = w0[k1];
     __syncwarp(gmask);
   }
-  for (int k = 0; k < tab.K; ++k) {
-    if (tab.cin[k] != ch) continue;
-    const float2* kk = kp + sol * kp_sol_stride + ((size_t)(ch * tab.max_k + tab.slot[k]) * N) * KPITCH;
+  int it = 0;
+  for (int k = k_first; k < tab.K; k = next_kernel(tab, k, ch), ++it) {
+    bool ok = true;
+    if constexpr (CC::KSTAGE) ok = mbar_wait(&bar[1], it & 1);
     float2 w[P];
-    if (j != 0) {
-      const float2* kc = kk + (size_t)j * N + t;
+    if (ok) {
+      const float2* kc = CC::KSTAGE ? kb + grp * N : kplane(k) + (size_t)j * N;
+      const float2* kn = CC::KSTAGE ? kb + GPB * N : kplane(k) + (size_t)(N / 2) * N;
+      if (j != 0) {
 #pragma unroll
-      for (int k1 = 0; k1 < P; ++k1) w[k1] = cmul(w0[k1], __ldg(kc + G * k1));
-    } else {
+        for (int k1 = 0; k1 < P; ++k1) w[k1] = cmul(w0[k1], kc[t + G * k1]);
+      } else {
 #pragma unroll
-      for (int k1 = 0; k1 < P; ++k1) {
-        const int ky = t + G * k1;
-        const float2 A = __ldg(kk + ky), B = __ldg(kk + (N / 2) * N + ky);
-        w[k1] = cadd(cmul(w0[k1], A), cmul(conjf2(mirror[(N - ky) & (N - 1)]), B));
+        for (int k1 = 0; k1 < P; ++k1) {
+          const int ky = t + G * k1;
+          const float2 A = kc[ky], B = kn[ky];
+          w[k1] = cadd(cmul(w0[k1], A), cmul(conjf2(mirror[(N - ky) & (N - 1)]), B));
+        }
       }
     }
+    // past this barrier: kb is free for the next kernel, and the previous
+    // product's store has read the tile
+    if (threadIdx.x == 0) bulk_wait_read_all();
+    if (__syncthreads_or(!ok)) {  // a kernel column copy never landed
+      if (threadIdx.x == 0) {
+        if (status) atomicExch(status, kStatusCopyTimeout);
+        mbar_wait(&bar[1], it & 1);
+        bulk_wait_all();
+      }
+      return;
+    }
+    const int k_next = next_kernel(tab, k, ch);
+    if (CC::KSTAGE && threadIdx.x == 0 && k_next < tab.K) issue_kernel(k_next);
     float2 u[Q][G];
     if constexpr (Q == 1) {
-      // unpacked row n = t + P*k1 -> its half of pair j of packed row n >> 1
+      // unpacked row r = t + P*k1 -> its half of pair j of packed row r >> 1
       fft_standard<GE, true, false>(w, u, cs, sm, t, gmask);
-      float2* pd = prod + ((size_t)n * tab.K + k) * (N / 2) * N;
 #pragma unroll
       for (int k1 = 0; k1 < G; ++k1) {
         const int r = t + P * k1;
-        pd[(size_t)(r >> 1) * N + 2 * j + (r & 1)] = u[0][k1];
+        *reinterpret_cast<float2*>(tb + swz128(r >> 1, chunk) + (r & 1) * 8) = u[0][k1];
       }
     } else {
       fft_standard<GE, true, true>(w, u, cs, sm, t, gmask);
-      float4* pd4 = reinterpret_cast<float4*>(prod + ((size_t)n * tab.K + k) * (N / 2) * N);
 #pragma unroll
       for (int a = 0; a < Q / 2; ++a) {
         const int m = t + G * a;
 #pragma unroll
         for (int k1 = 0; k1 < G; ++k1) {
           const int r = m + (P / 2) * k1;
-          pd4[(size_t)r * (N / 2) + j] = make_float4(u[2 * a][k1].x, u[2 * a][k1].y, u[2 * a + 1][k1].x,
-                                                     u[2 * a + 1][k1].y);
+          *reinterpret_cast<float4*>(tb + swz128(r, chunk)) =
+              make_float4(u[2 * a][k1].x, u[2 * a][k1].y, u[2 * a + 1][k1].x, u[2 * a + 1][k1].y);
         }
       }
     }
+    fence_proxy_async();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int b = 0; b < CC::BOXES; ++b)
+        tma_store_2d(&prod_map, (j0 + 8 * b) * 4, (n * tab.K + k) * (N / 2), tile + b * CC::BOX_BYTES);
+      bulk_commit();
+    }
   }
+  if (threadIdx.x == 0) bulk_wait_all();
 }
 
 // ------------------------------------------------------------------ row_inv
@@ -710,12 +770,13 @@ cudaError_t step_n(const StreamedStep& s, cudaStream_t st) {
   e = cudaFuncSetAttribute(col_conv_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_col);
   if (e != cudaSuccess) return e;
   const long planes = (long)s.n_worlds * m.C;
-  alignas(64) CUtensorMap spec_map;
+  alignas(64) CUtensorMap spec_map, prod_map;
   if (!encode_spec_map<N>(&spec_map, s.spec, planes)) return cudaErrorInvalidValue;
+  if (!encode_spec_map<N>(&prod_map, s.prod, (long)s.n_worlds * m.K)) return cudaErrorInvalidValue;
   if (!s.spec_ready)  // otherwise the previous step's row inverse already wrote this step's row spectra
     row_fwd_kernel<N><<<(unsigned)(planes * BPP), kThreads, sm_fwd, st>>>(s.n_worlds, m.C, s.state, s.spec);
-  col_conv_kernel<N><<<(unsigned)(planes * CC::BPP), CC::T, sm_col, st>>>(spec_map, s.n_worlds, s.n_init, tab, s.kp,
-                                                                          s.kp_sol_stride, s.prod, s.status);
+  col_conv_kernel<N><<<(unsigned)(planes * CC::BPP), CC::T, sm_col, st>>>(spec_map, prod_map, s.n_worlds, s.n_init,
+                                                                          tab, s.kp, s.kp_sol_stride, s.status);
   using RC = RowInvCfg<N>;
   bool all_gauss = true, all_poly = true;
   for (int k = 0; k < m.K; ++k) {

@@ -72,6 +72,22 @@ __device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned b
                : "memory");
 }
 
+// 2D tiled tensor store of one box from shared memory (bulk-group
+// completion; x aligned like a load, x and y non-negative).  The writing
+// threads fence their shared stores to the async proxy and meet at a barrier
+// before one thread issues it.
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(smem_u32(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// every committed store has finished reading its shared-memory source
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// every committed store has completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // Byte offset of 16-byte chunk `chunk` (0..7) of row `row` in a box loaded
 // with CU_TENSOR_MAP_SWIZZLE_128B (128-byte rows, box base 1024-aligned).
 __device__ __forceinline__ int swz128(int row, int chunk) { return row * 128 + ((chunk ^ (row & 7)) << 4); }
