@@ -333,7 +333,8 @@ struct RowInvCfg {
   static constexpr int BPW = (N / 2) / GPB;  // blocks per world
   static constexpr int ROWP = N + G;         // staged row pitch (float2) == Geo<N, G>::SCR
   static constexpr int BUF = GPB * ROWP;     // float2 per buffer
-  static constexpr int NBUF = 3;             // staging ring depth (items in flight: NBUF - 1)
+  static constexpr int NBUF = 2;             // staging ring depth (items in flight: NBUF - 1)
+  static constexpr int SSTP = 2 * N + 16;    // staged state rows (2r, 2r+1) pitch per group (floats)
 };
 
 // item word: bit 16 = count the potential, bits 8..15 = output channel + 1 (0: none), bits 0..7 = kernel
@@ -344,7 +345,8 @@ __device__ __forceinline__ bool item_count(int it) { return (it >> 16) & 1; }
 template <int N>
 size_t row_inv_smem(int C, int K) {
   using RC = RowInvCfg<N>;
-  return (size_t)RC::NBUF * RC::BUF * sizeof(float2) + (size_t)3 * N * sizeof(float2) +
+  return (size_t)RC::NBUF * RC::BUF * sizeof(float2) + (size_t)RC::GPB * RC::SSTP * sizeof(float) +
+         (size_t)3 * N * sizeof(float2) +
          (size_t)(RC::T / 32) * (RAW_CM + kMaxChannels) * sizeof(float) + 16 * sizeof(uint64_t) +
          (size_t)kMaxChannels * sizeof(float) + (size_t)(C * K + K + 1) * sizeof(int) +
          (size_t)(C * K + K + 1) * sizeof(float4) + (size_t)(C * K + 2 * K) * sizeof(float);
@@ -366,9 +368,10 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   static_assert(ROWP == GE::SCR, "a staged row doubles as the group's FFT scratch");
   extern __shared__ __align__(16) float2 sm[];
   float2* bufs = sm;                    // [NBUF][GPB][ROWP] staging ring
-  float2* tw = bufs + NBUF * RC::BUF;   // 3N twiddles
+  float* sst = reinterpret_cast<float*>(bufs + NBUF * RC::BUF);  // [GPB][SSTP] the channel's state rows
+  float2* tw = reinterpret_cast<float2*>(sst + GPB * RC::SSTP);  // 3N twiddles
   float* red = reinterpret_cast<float*>(tw + 3 * N);  // [warps][RAWS_MAX]
-  uint64_t* bars = reinterpret_cast<uint64_t*>(red + NWARPS * RAWS_MAX);  // NBUF (16 slots reserved)
+  uint64_t* bars = reinterpret_cast<uint64_t*>(red + NWARPS * RAWS_MAX);  // NBUF ring + 1 state (16 reserved)
   float* wsum_s = reinterpret_cast<float*>(bars + 16);  // [kMaxChannels]
   float4* ipar = reinterpret_cast<float4*>(wsum_s + kMaxChannels);  // [C*K + K + 1] per item: weight, m, s, a
   __shared__ int s_nitems;
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   init_twiddles<GE>(tw, tw + N, tw + 2 * N, threadIdx.x, blockDim.x);
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int b = 0; b < NBUF; ++b) mbar_init(&bars[b], 1);
+    for (int b = 0; b <= NBUF; ++b) mbar_init(&bars[b], 1);
     fence_proxy_async();
     // work items with their growth parameters, and per-channel weight sums
     int ni = 0;
@@ -435,8 +438,17 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     __syncwarp();
     for (int g = lane; g < GPB; g += 32) bulk_load(dst + g * ROWP, src + (size_t)g * N, N * sizeof(float2), &bars[b]);
   };
+  // warp 0 stages channel co's state rows (2r, 2r+1) of every group into sst
+  auto issue_state = [&](int co) {
+    const float* src = state + (((size_t)n * C + co) * N + 2 * r0) * N;
+    if (lane == 0) mbar_arrive_expect_tx(&bars[NBUF], (unsigned)(GPB * 2 * N * sizeof(float)));
+    __syncwarp();
+    for (int g = lane; g < GPB; g += 32)
+      bulk_load(sst + g * RC::SSTP, src + (size_t)g * 2 * N, 2 * N * sizeof(float), &bars[NBUF]);
+  };
   if (wid == 0)
     for (int q = 0; q < NBUF - 1 && q < nit; ++q) issue(q);
+  int st_issued = 0, st_done = 0;  // state-row copies issued / waited for (block-uniform)
 
   float dt;
   if (tab.dt_mode == 0) dt = __ldg(dtp);
@@ -464,11 +476,16 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
       failed_at = i;
       return;
     }
-    if (wid == 0 && i + NBUF - 1 < nit) {
-      fence_proxy_async();
-      issue(i + NBUF - 1);
-    }
     const int it = items[i], k = item_k(it), co = item_co(it);
+    // a channel's first item: its state rows start moving (the previous
+    // channel's epilogue, the last reader of sst, is behind the barrier)
+    const bool first = co >= 0 && (i == 0 || item_co(items[i - 1]) != co);
+    st_issued += first ? 1 : 0;
+    if (wid == 0) {
+      fence_proxy_async();
+      if (i + NBUF - 1 < nit) issue(i + NBUF - 1);
+      if (first) issue_state(co);
+    }
     float2* row = bufs + (i % NBUF) * RC::BUF + grp * ROWP;
     float2 v[Q][G];
     if constexpr (Q == 1) {
@@ -528,12 +545,27 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
   for (int co = 0; co < C && !failed; ++co) {
 #pragma unroll
     for (int k1 = 0; k1 < P; ++k1) acc[k1] = make_float2(0.f, 0.f);
+    const int i_begin = i;
     while (!failed && i < nit && item_co(items[i]) == co) process(i++);
     if (failed) break;
+    if (i == i_begin) {  // a channel no kernel feeds: fetch its state rows here
+      __syncthreads();
+      ++st_issued;
+      if (wid == 0) {
+        fence_proxy_async();
+        issue_state(co);
+      }
+    }
+    if (__syncthreads_or(!mbar_wait(&bars[NBUF], (st_issued - 1) & 1))) {
+      failed = true;
+      failed_at = i;
+      break;
+    }
+    st_done = st_issued;
     // field (weighted_sum / weighted_mean, core.py:202-242), state update, moments
     const float wsum = wsum_s[co];
     const size_t base = ((size_t)n * C + co) * N * N;
-    const float* sa_row = state + base + (size_t)(2 * r) * N;
+    const float* sa_row = sst + grp * RC::SSTP;
     float* da_row = state_out + base + (size_t)(2 * r) * N;
     float* fa_row = field_out ? field_out + base + (size_t)(2 * r) * N : nullptr;
     float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f;
@@ -550,7 +582,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
         fa = fa / wsum;
         fb = fb / wsum;
       }
-      const float sa = __ldg(sa_row + x), sb = __ldg(sa_row + N + x);
+      const float sa = sa_row[x], sb = sa_row[N + x];
       nsv[k1] = make_float2(state_fn(tab.state_fn, sa, fa, dt), state_fn(tab.state_fn, sb, fb, dt));
       da_row[x] = nsv[k1].x;
       da_row[N + x] = nsv[k1].y;
@@ -601,6 +633,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
     if (threadIdx.x == 0 && status) atomicExch(status, kStatusCopyTimeout);
     const int f = failed_at;
     for (int q = f; q < f + NBUF - 1 && q < nit; ++q) mbar_wait(&bars[q % NBUF], (q / NBUF) & 1);  // issued: <= f + NBUF - 2
+    if (st_issued > st_done) mbar_wait(&bars[NBUF], (st_issued - 1) & 1);
     return;
   }
   // block reduction: warp shuffles then shared memory
@@ -827,6 +860,8 @@ size_t streamed_workspace_bytes(const Model& m, int n_worlds, int n_sols) {
 }
 
 cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st) {
+  // the row inverse bulk-copies state rows: the state base must be 16-byte aligned
+  if ((reinterpret_cast<uintptr_t>(s.state) & 15u) != 0) return cudaErrorMisalignedAddress;
   switch (s.m->H) {
     case 32: return step_n<32>(s, st);
     case 64: return step_n<64>(s, st);
