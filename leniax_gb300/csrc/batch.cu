@@ -223,7 +223,7 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
         const int x = t + G * k1;
         const float pa = w[k1].x, pb = w[k1].y;
         const float sa = src[(2 * r) * N + x], sb = src[(2 * r + 1) * N + x];
-        const float fa = growth_cell<GF>(gq, pa) * wf, fb = growth_cell<GF>(gq, pb) * wf;
+        const float fa = weighted_growth<GF>(gq, pa, wf), fb = weighted_growth<GF>(gq, pb, wf);
         st[(2 * r) * N + x] = state_fn(a.state_fn, sa, fa, dt);
         st[(2 * r + 1) * N + x] = state_fn(a.state_fn, sb, fb, dt);
         const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
@@ -445,7 +445,7 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
           const int x = t + G * k1;
           const float pa = w[k1].x, pb = w[k1].y;
           const float sa = sra[x], sb = sra[N + x];
-          const float fa = growth_cell<GF>(gq, pa) * wf, fb = growth_cell<GF>(gq, pb) * wf;
+          const float fa = weighted_growth<GF>(gq, pa, wf), fb = weighted_growth<GF>(gq, pb, wf);
           dsa[x] = state_fn(a.state_fn, sa, fa, dt);
           dsa[N + x] = state_fn(a.state_fn, sb, fb, dt);
           const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);

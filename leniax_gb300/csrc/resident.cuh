@@ -302,8 +302,8 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
           const int x = t + G * k1;
           const float pa = w[k1].x, pb = w[k1].y;
           const float sa = z[k1].x, sb = z[k1].y;
-          const float fa = growth_cell<GF>(gp, pa) * wf;
-          const float fb = growth_cell<GF>(gp, pb) * wf;
+          const float fa = weighted_growth<GF>(gp, pa, wf);
+          const float fb = weighted_growth<GF>(gp, pb, wf);
           if (sfid == LGX_STATE_V1) {
             z[k1] = make_float2(__saturatef(fmaf(dt, fa, sa)), __saturatef(fmaf(dt, fb, sb)));
           } else {
