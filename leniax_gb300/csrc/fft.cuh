@@ -185,26 +185,53 @@ __device__ __forceinline__ int n1_mirror(int t, int q) {  // {m, P-m} (m>0) or {
   return (q & 1) ? GE::P - m : m;
 }
 
+// The three tables of every (N, G), evaluated at compile time with the
+// octant-reduced series above (exact zeros and ones at the quarter points,
+// like sincospi) and stored once in global memory; blocks copy them into
+// shared memory at start.  Evaluating them per block with double-precision
+// sincospi cost more than the transforms in short-lived blocks: the FP64
+// pipe of this part is narrow.
+struct alignas(8) TwEntry {
+  float x, y;
+};
+template <int N, int G>
+struct TwiddleTables {
+  static constexpr int P = N / G, Q = P / G;
+  TwEntry v[3 * N];
+  static constexpr TwEntry entry(int m) {  // W_N^m = exp(-2 pi i m / N)
+    return TwEntry{(float)cx_trig(m, N, false), (float)(-cx_trig(m, N, true))};
+  }
+  static constexpr int pairs(int t, int q) {  // n1_pairs
+    if (Q == 1) return t;
+    const int m = t + G * (q >> 1);
+    return 2 * m + (q & 1);
+  }
+  static constexpr int mirror(int t, int q) {  // n1_mirror
+    if (Q == 1) return t;
+    const int m = t + G * (q >> 1);
+    if (m == 0) return (q & 1) ? P / 2 : 0;
+    return (q & 1) ? P - m : m;
+  }
+  constexpr TwiddleTables() : v{} {
+    for (int i = 0; i < N; ++i) {
+      const int t = i % G, k2 = i / G, kk = (i / G) % G, q = i / (G * G);
+      v[i] = entry((t * k2) % N);
+      v[N + i] = entry((pairs(t, q) * kk) % N);
+      v[2 * N + i] = entry((mirror(t, q) * kk) % N);
+    }
+  }
+};
+template <int N, int G>
+__device__ const TwiddleTables<N, G> kTwiddles{};
+
 template <class GE>
 __device__ void init_twiddles(float2* tw_std, float2* tw_colf, float2* tw_rowi, int tid, int nthreads) {
-  constexpr int N = GE::N, G = GE::G, P = GE::P, Q = GE::Q;
+  constexpr int N = GE::N;
+  const float2* src = reinterpret_cast<const float2*>(kTwiddles<GE::N, GE::G>.v);
   for (int i = tid; i < N; i += nthreads) {
-    {  // std
-      int k2 = i / G, t = i % G;
-      double s, c;
-      sincospi(-2.0 * double((t * k2) % N) / double(N), &s, &c);
-      tw_std[i] = make_float2((float)c, (float)s);
-    }
-    {
-      int t = i % G, k2 = (i / G) % G, q = i / (G * G);
-      if (q < Q) {
-        double s, c;
-        sincospi(-2.0 * double((n1_pairs<GE>(t, q) * k2) % N) / double(N), &s, &c);
-        tw_colf[i] = make_float2((float)c, (float)s);
-        sincospi(-2.0 * double((n1_mirror<GE>(t, q) * k2) % N) / double(N), &s, &c);
-        tw_rowi[i] = make_float2((float)c, (float)s);
-      }
-    }
+    tw_std[i] = __ldg(src + i);
+    tw_colf[i] = __ldg(src + N + i);
+    tw_rowi[i] = __ldg(src + 2 * N + i);
   }
 }
 
