@@ -512,16 +512,8 @@ __global__ void __launch_bounds__(512, 1) mixed_kernel(MixedArgs ma) {
   init_twiddles<Geo<128, 8>>(sm + TW128, sm + TW128 + 128, sm + TW128 + 256, threadIdx.x, blockDim.x);
   init_twiddles<Geo<256, 8>>(sm + TW256, sm + TW256 + 256, sm + TW256 + 512, threadIdx.x, blockDim.x);
   // G = 2 line transforms use only the standard table
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
-    double s, c;
-    sincospi(-2.0 * double(((i % 2) * (i / 2)) % 64) / 64.0, &s, &c);
-    sm[TW64G2 + i] = make_float2((float)c, (float)s);
-  }
-  for (int i = threadIdx.x; i < 32; i += blockDim.x) {
-    double s, c;
-    sincospi(-2.0 * double(((i % 2) * (i / 2)) % 32) / 32.0, &s, &c);
-    sm[TW32G2 + i] = make_float2((float)c, (float)s);
-  }
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) sm[TW64G2 + i] = reinterpret_cast<const float2*>(kTwiddles<64, 2>.v)[i];
+  for (int i = threadIdx.x; i < 32; i += blockDim.x) sm[TW32G2 + i] = reinterpret_cast<const float2*>(kTwiddles<32, 2>.v)[i];
   __syncthreads();
   __shared__ BatchClassArgs s_cls[kMaxBatchClasses];
   __shared__ int s_item;

@@ -159,12 +159,7 @@ __global__ void __launch_bounds__(128) zline_fft_kernel(long lines, float2* __re
   constexpr long PLANE = (long)N * HW;
   __shared__ float2 tw[N];
   __shared__ float2 scr[32 * GE::SCR];
-  for (int i = threadIdx.x; i < N; i += blockDim.x) {
-    const int k2 = i / G, t = i % G;
-    double sn, cs;
-    sincospi(-2.0 * double((t * k2) % N) / double(N), &sn, &cs);
-    tw[i] = make_float2((float)cs, (float)sn);
-  }
+  for (int i = threadIdx.x; i < N; i += blockDim.x) tw[i] = reinterpret_cast<const float2*>(kTwiddles<N, G>.v)[i];
   __syncthreads();
   const int grp = threadIdx.x / G, t = threadIdx.x % G, lane = threadIdx.x & 31;
   const unsigned gmask = ((1u << G) - 1u) << (lane & ~(G - 1));
