@@ -23,6 +23,7 @@
 #include <mutex>
 
 #include "resident.cuh"
+#include "tma.cuh"
 
 namespace lgx {
 
@@ -301,6 +302,7 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
     // ---------------------------------------------------------- A. planes forward
     for (int zb = 0; zb < N; zb += SL) {
       const int z = zb + sub;
+      if (tid == 0 && z + SL < N) prefetch_l2(src + (size_t)(z + SL) * N * N, N * N * sizeof(float));
       {
         const float* pl = src + (size_t)z * N * N;
         float2 v[P];
@@ -403,6 +405,10 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
     const int sz = shv[0], sy = shv[1], sx = shv[2];
     for (int zb = 0; zb < N; zb += SL) {
       const int z = zb + sub;
+      if (tid == 0 && z + SL < N) {
+        prefetch_l2(X + (size_t)(z + SL) * PLANE, (unsigned)(PLANE * sizeof(float2)));
+        prefetch_l2(src + (size_t)(z + SL) * N * N, N * N * sizeof(float));
+      }
       {
         const float2* xz = X + (size_t)z * PLANE;
         float2 w[P];

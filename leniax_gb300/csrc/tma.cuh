@@ -88,6 +88,16 @@ __device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bu
 // every committed store has completed
 __device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
+// Bulk prefetch of [src, src + bytes) into L2; nothing to wait for.  A
+// source that is not 16-byte aligned is skipped (a hint only), the size
+// rounded down to whole 16-byte units.
+__device__ __forceinline__ void prefetch_l2(const void* src, unsigned bytes) {
+  bytes &= ~15u;
+  if ((reinterpret_cast<uintptr_t>(src) & 15u) != 0 || bytes == 0) return;
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(reinterpret_cast<uint64_t>(src)), "r"(bytes)
+               : "memory");
+}
+
 // Byte offset of 16-byte chunk `chunk` (0..7) of row `row` in a box loaded
 // with CU_TENSOR_MAP_SWIZZLE_128B (128-byte rows, box base 1024-aligned).
 __device__ __forceinline__ int swz128(int row, int chunk) { return row * 128 + ((chunk ^ (row & 7)) << 4); }
