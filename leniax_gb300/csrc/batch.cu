@@ -155,7 +155,7 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
 #pragma unroll
       for (int q = 0; q < Q; ++q)
 #pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) spec[r * N + t + G * q + P * k1] = u[q][k1];
+        for (int k1 = 0; k1 < G; ++k1) spec[r * N + pa_pos<N>(t + G * q + P * k1)] = u[q][k1];
     }
     __syncthreads();
     for (int c = grp; c < N / 2; c += NG) {  // column pass
@@ -166,13 +166,14 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
 #pragma unroll
         for (int n2 = 0; n2 < G; ++n2) {
           const int r = m + (P / 2) * n2;
+          // pair c of packed row r: (slot c, slot N - c); pair 0: (slot 0, slot N/2)
+          const float4 q = reinterpret_cast<const float4*>(spec + r * N)[c];
+          const float2 z1 = make_float2(q.x, q.y), z2 = make_float2(q.z, q.w);
           if (c != 0) {
-            const float2 z1 = spec[r * N + c], z2 = spec[r * N + N - c];
             v[2 * jp][n2] = caddc(z1, z2);
             const float2 d = csubc(z1, z2);
             v[2 * jp + 1][n2] = make_float2(d.y, -d.x);
           } else {
-            const float2 z1 = spec[r * N], z2 = spec[r * N + N / 2];
             v[2 * jp][n2] = make_float2(z1.x, z2.x);
             v[2 * jp + 1][n2] = make_float2(z1.y, z2.y);
           }
@@ -197,12 +198,14 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
       }
       float2 u[Q][G];
       fft_standard<GE, true, true>(w, u, scr, tw_std, t, gmask);
+      // rows 2r and 2r+1 of column pair c -> pair c of packed row r
 #pragma unroll
-      for (int q = 0; q < Q; ++q) {
-        const int m = t + G * (q >> 1);
-        const int col = (c != 0) ? ((q & 1) ? N - c : c) : ((q & 1) ? N / 2 : 0);
+      for (int a = 0; a < Q / 2; ++a) {
+        const int m = t + G * a;
 #pragma unroll
-        for (int k1 = 0; k1 < G; ++k1) spec[(m + (P / 2) * k1) * N + col] = u[q][k1];
+        for (int k1 = 0; k1 < G; ++k1)
+          reinterpret_cast<float4*>(spec + (m + (P / 2) * k1) * N)[c] =
+              make_float4(u[2 * a][k1].x, u[2 * a][k1].y, u[2 * a + 1][k1].x, u[2 * a + 1][k1].y);
       }
     }
     __syncthreads();
@@ -213,7 +216,7 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
     const int sy = shv[0], sx = shv[1];
     for (int r = grp; r < N / 2; r += NG) {  // row inverse, growth, update, moments
       float2 v[Q][G];
-      unpack_row_pair<GE>(spec + r * N, v, t);
+      unpack_row_pair_pa<GE>(spec + r * N, v, t);
       float2 w[P];
       fft_mirrored<GE, true, true>(v, w, scr, tw_rowi, t, gmask);
       const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);

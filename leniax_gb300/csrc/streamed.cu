@@ -66,17 +66,6 @@ __device__ __forceinline__ float2* init_tw(float2* sm) {
   return sm + 3 * N;
 }
 
-// Pair-adjacent layout of a packed-row spectrum Z[0..N-1]: pair j (16 bytes)
-// holds (Z[j], Z[N-j]) for 0 < j < N/2 and pair 0 holds (Z[0], Z[N/2]).  The
-// column pass reads and writes whole pairs, and its tiles start on 16-byte
-// boundaries, as TMA requires.  After the column pass, pair j of packed row r
-// holds (column j at row 2r, column j at row 2r+1); pair 0 the DC and Nyquist
-// columns packed as DC + i Nyquist.
-template <int N>
-__host__ __device__ __forceinline__ int pa_pos(int k) {
-  return k == 0 ? 0 : (k == N / 2 ? 1 : (k < N / 2 ? 2 * k : 2 * (N - k) + 1));
-}
-
 // ------------------------------------------------------------------ row_fwd
 template <int N>
 __global__ void __launch_bounds__(kThreads) row_fwd_kernel(int n_worlds, int C, const float* __restrict__ state,
