@@ -162,9 +162,29 @@ class LeniaRolloutFunction(torch.autograd.Function):
         g_w = torch.zeros((Ns, 1, 1), dtype=torch.float32, device=dev)
         ws = workspace(lib.lgx_adjoint_workspace_bytes(update_fn.model.plan.handle, Ns, Ni), dev)
         seg_starts = list(range(0, steps, k))
+        # Segment j - 1's trajectory is recomputed on a side stream while
+        # segment j's adjoint runs: the two persistent launches take
+        # different SMs when a batch fills fewer than half of them.
+        main = torch.cuda.current_stream(dev)
+        side = torch.cuda.Stream(device=dev)
+        side.wait_stream(main)
+
+        def recompute(j):
+            with torch.cuda.stream(side):
+                tr = _segment(update_fn, ckpts[j], k_half, gf, w, Tt, min(k, steps - seg_starts[j]), traj=True)
+                ev = torch.cuda.Event()
+                ev.record(side)
+            return tr, ev
+
+        nxt = recompute(len(seg_starts) - 1)
         for j in reversed(range(len(seg_starts))):
             n = min(k, steps - seg_starts[j])
-            tc, tp = _segment(update_fn, ckpts[j], k_half, gf, w, Tt, n, traj=True)
+            (tc, tp), ready = nxt
+            if j > 0:
+                nxt = recompute(j - 1)
+            main.wait_event(ready)
+            tc.record_stream(main)
+            tp.record_stream(main)
             job = AdjointJob()
             job.n_sols, job.n_init, job.steps = Ns, Ni, n
             job.k_half, job.gf_params, job.weights, job.T = (k_half.data_ptr(), gf.data_ptr(), w.data_ptr(),
