@@ -137,10 +137,45 @@ __device__ __forceinline__ float weighted_growth(const GrowthP& g, float x, floa
   else return fmaf(2.f * w, growth_core<GF>(g, x), -w);
 }
 
+// weighted_growth of a cell pair on the packed FP32x2 pipe (gaussian form:
+// -(u a)^2 evaluated as u^2 (-a^2)).
+template <int GF>
+__device__ __forceinline__ float2 weighted_growth2(const GrowthP& g, float2 p, float w) {
+  if constexpr (GF == GF_FAST_GAUSSIAN) {
+    const float2 u = __fadd2_rn(p, make_float2(-g.m, -g.m));
+    const float na2 = -(g.a * g.a);
+    const float2 q = __fmul2_rn(__fmul2_rn(u, u), make_float2(na2, na2));
+    const float2 e = make_float2(fast_exp2(q.x), fast_exp2(q.y));
+    return __ffma2_rn(make_float2(2.f * w, 2.f * w), e, make_float2(-w, -w));
+  } else {
+    return make_float2(weighted_growth<GF>(g, p.x, w), weighted_growth<GF>(g, p.y, w));
+  }
+}
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
+}
+
+// Sums of 16 values across the warp in 16 shuffles (one per value would take
+// 80): at each butterfly level a lane keeps half of its values and sends the
+// other half to its partner.  Returns, in lane L, the warp total of value
+// L >> 1 (lanes L and L ^ 1 hold the same total).
+__device__ __forceinline__ float warp_sum16(float (&v)[16]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int lvl = 0; lvl < 4; ++lvl) {
+    const int mask = 16 >> lvl, half = 8 >> lvl;
+    const bool hi = (lane & mask) != 0;
+#pragma unroll
+    for (int i = 0; i < half; ++i) {
+      const float send = hi ? v[i] : v[half + i];
+      const float keep = hi ? v[half + i] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, mask);
+    }
+  }
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
 }
 
 // Named barrier over `count` threads (count a multiple of 32).

@@ -293,7 +293,8 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
         const float cya = (float)(((2 * r - sy) & (N - 1)) - N / 2);
         const float cyb = (float)(((2 * r + 1 - sy) & (N - 1)) - N / 2);
         const int xb = t - sx;
-        float Sa = 0.f, Sb = 0.f, Ga = 0.f, Gb = 0.f, mxx = 0.f, mx2x = 0.f, gxx = 0.f;
+        float2 S2 = make_float2(0.f, 0.f), G2 = make_float2(0.f, 0.f);  // (row 2r, row 2r+1) sums
+        float mxx = 0.f, mx2x = 0.f, gxx = 0.f;
         float cpot = 0.f, cmass = 0.f, cgrow = 0.f;
         bool liveA = false, liveB = false, liveX = false;
         const size_t tbase = ((size_t)step * a.n_worlds + world) * (size_t)(N * N);
@@ -301,9 +302,10 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
         for (int k1 = 0; k1 < P; ++k1) {
           const int x = t + G * k1;
           const float pa = w[k1].x, pb = w[k1].y;
-          const float sa = z[k1].x, sb = z[k1].y;
-          const float fa = weighted_growth<GF>(gp, pa, wf);
-          const float fb = weighted_growth<GF>(gp, pb, wf);
+          const float2 s2 = z[k1];
+          const float sa = s2.x, sb = s2.y;
+          const float2 f2 = weighted_growth2<GF>(gp, w[k1], wf);
+          const float fa = f2.x, fb = f2.y;
           if (sfid == LGX_STATE_V1) {
             z[k1] = make_float2(__saturatef(fmaf(dt, fa, sa)), __saturatef(fmaf(dt, fb, sb)));
           } else {
@@ -312,10 +314,8 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
           // statistics moments of the pre-update cells (statistics.py:64-100)
           const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
           const float cx = (float)(((xb + G * k1) & (N - 1)) - N / 2);
-          Sa += sa;
-          Sb += sb;
-          Ga += fpa;
-          Gb += fpb;
+          S2 = __fadd2_rn(S2, s2);
+          G2 = __fadd2_rn(G2, make_float2(fpa, fpb));
           const float ss = sa + sb, gg = fpa + fpb;
           mxx = fmaf(ss, cx, mxx);
           mx2x = fmaf(ss * cx, cx, mx2x);
@@ -345,7 +345,8 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
         }
         // live cell on the outer layer of the un-centred torus (box stop set)
         const bool border = liveX || (r == 0 && liveA) || (r == N / 2 - 1 && liveB);
-        float acc[11];
+        const float Sa = S2.x, Sb = S2.y, Ga = G2.x, Gb = G2.y;
+        float acc[16];
         acc[0] = Sa + Sb;
         acc[1] = Ga + Gb;
         acc[2] = cpot;
@@ -357,14 +358,11 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
         acc[8] = gxx;
         acc[9] = cya * cya * Sa + cyb * cyb * Sb;
         acc[10] = mx2x;
+        acc[11] = border ? 1.f : 0.f;  // a count of border lanes; the finaliser tests > 0
 #pragma unroll
-        for (int i = 0; i < 11; ++i) acc[i] = warp_sum(acc[i]);
-        const bool anyb = __any_sync(0xffffffffu, border);
-        if (lane == 0) {
-#pragma unroll
-          for (int i = 0; i < 11; ++i) part[wid * 16 + i] = acc[i];
-          part[wid * 16 + 11] = anyb ? 1.f : 0.f;
-        }
+        for (int i = 12; i < 16; ++i) acc[i] = 0.f;
+        const float tot = warp_sum16(acc);  // lane L: total of value L >> 1
+        if ((lane & 1) == 0 && lane < 24) part[wid * 16 + (lane >> 1)] = tot;
       }
       // no barrier here: the next row pass of this group touches only its own
       // packed row, and the next step's first barrier orders these partials
