@@ -137,16 +137,30 @@ __device__ __forceinline__ float weighted_growth(const GrowthP& g, float x, floa
   else return fmaf(2.f * w, growth_core<GF>(g, x), -w);
 }
 
-// weighted_growth of a cell pair on the packed FP32x2 pipe (gaussian form:
+// growth_core of a cell pair on the packed FP32x2 pipe (gaussian form:
 // -(u a)^2 evaluated as u^2 (-a^2)).
 template <int GF>
-__device__ __forceinline__ float2 weighted_growth2(const GrowthP& g, float2 p, float w) {
+__device__ __forceinline__ float2 growth_core2(const GrowthP& g, float2 p) {
+  static_assert(GF == GF_FAST_GAUSSIAN || GF == GF_FAST_POLY4, "2 e(x) - 1 forms only");
+  const float2 u = __fadd2_rn(p, make_float2(-g.m, -g.m));
+  const float2 u2 = __fmul2_rn(u, u);
   if constexpr (GF == GF_FAST_GAUSSIAN) {
-    const float2 u = __fadd2_rn(p, make_float2(-g.m, -g.m));
     const float na2 = -(g.a * g.a);
-    const float2 q = __fmul2_rn(__fmul2_rn(u, u), make_float2(na2, na2));
-    const float2 e = make_float2(fast_exp2(q.x), fast_exp2(q.y));
-    return __ffma2_rn(make_float2(2.f * w, 2.f * w), e, make_float2(-w, -w));
+    const float2 q = __fmul2_rn(u2, make_float2(na2, na2));
+    return make_float2(fast_exp2(q.x), fast_exp2(q.y));
+  } else {
+    const float2 t = __ffma2_rn(u2, make_float2(-g.a, -g.a), make_float2(1.f, 1.f));
+    float2 o = make_float2(fmaxf(0.f, t.x), fmaxf(0.f, t.y));
+    o = __fmul2_rn(o, o);
+    return __fmul2_rn(o, o);
+  }
+}
+
+// weighted_growth of a cell pair.
+template <int GF>
+__device__ __forceinline__ float2 weighted_growth2(const GrowthP& g, float2 p, float w) {
+  if constexpr (GF == GF_FAST_GAUSSIAN || GF == GF_FAST_POLY4) {
+    return __ffma2_rn(make_float2(2.f * w, 2.f * w), growth_core2<GF>(g, p), make_float2(-w, -w));
   } else {
     return make_float2(weighted_growth<GF>(g, p.x, w), weighted_growth<GF>(g, p.y, w));
   }

@@ -523,8 +523,7 @@ __global__ void __launch_bounds__(RowInvCfg<N>::T) row_inv_kernel(
           acc[k1].x = fmaf(wk, growth_cell<GF>(g, w[k1].x), acc[k1].x);
           acc[k1].y = fmaf(wk, growth_cell<GF>(g, w[k1].y), acc[k1].y);
         } else {  // w (2 e - 1) summed as 2 w e here, minus the channel's weight sum below
-          acc[k1].x = fmaf(2.f * wk, growth_core<GF>(g, w[k1].x), acc[k1].x);
-          acc[k1].y = fmaf(2.f * wk, growth_core<GF>(g, w[k1].y), acc[k1].y);
+          acc[k1] = __ffma2_rn(make_float2(2.f * wk, 2.f * wk), growth_core2<GF>(g, w[k1]), acc[k1]);
         }
       }
     }
