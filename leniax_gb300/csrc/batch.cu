@@ -370,6 +370,13 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
       const unsigned zmask = ((1u << LG) - 1u) << (lane & ~(LG - 1));
       float2* zs = work + zg * GZ::SCR;
       for (int l = zg; l < N * HW; l += NGZ) {
+        // L2 prefetch of the next round of lines: z row zg of the scratch and of the spectrum
+        const int next = l - zg + NGZ;
+        if (zt == 0 && zg < N && next < N * HW) {
+          const unsigned bytes = (unsigned)(min(NGZ, N * HW - next) * sizeof(float2));
+          prefetch_l2(X + (size_t)zg * PLANE + next, bytes);
+          prefetch_l2(kp + (size_t)zg * PLANE + next, bytes);
+        }
         float2* base = X + l;  // l = ky * HW + kx
         const float2* kb = kp + l;
         float2 v[PZ];
