@@ -153,10 +153,10 @@ LGX_API size_t lgx_run_workspace_bytes(const lgx_plan* plan, int n_sols, int n_i
 LGX_API int lgx_run(const lgx_plan* plan, const lgx_rollout* job, void* workspace, size_t workspace_bytes,
             void* stream);
 
-/* Device status of the last lgx_run / lgx_update that used `workspace`: 0 on
- * success, 1 if a staged (TMA / bulk) copy of the streamed engine did not land
- * within its bounded wait (the step's outputs are then incomplete).  Copies
- * the word to the host on `stream` and synchronises that stream. */
+/* Device status of the last lgx_run / lgx_update / lgx_batch_run that used
+ * `workspace`: 0 on success, 1 if a staged (TMA / bulk) copy did not land
+ * within its bounded wait (the outputs are then incomplete).  Copies the word
+ * to the host on `stream` and synchronises that stream. */
 LGX_API int lgx_workspace_status(const void* workspace, void* stream, int* status);
 
 /* Workspace bytes lgx_update needs for n worlds. */

@@ -224,6 +224,11 @@ class UnevenBatch:
             self.launch()
         return self
 
+    def status(self) -> int:
+        """Device status word of the last run (0: ok; 1: a staged copy did not
+        land within its bounded wait).  Synchronises the current stream."""
+        return _lib.workspace_status(self.ws.data_ptr(), torch.cuda.current_stream(self.device).cuda_stream)
+
     def results(self) -> List[Dict[str, torch.Tensor]]:
         """Per class: ``final`` cells and, with statistics, leniax's stats dict
         (arrays ``[n, steps, 1]``), ``N``, ``N_box`` and ``mass_centroid``."""

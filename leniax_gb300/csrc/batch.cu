@@ -52,15 +52,19 @@ struct Big3D {
   static constexpr int SL = 512 / NT;     // planes in flight
   static constexpr int PITCH = N + G;
   static constexpr int BUF = (N / 2) * PITCH, CSCR = (N / 2) * GE::SCR;
-  static constexpr int PLANES = SL * (BUF + CSCR);
+  static constexpr int XS = N * HW;               // one half-spectrum plane, staged per slice (phase C)
+  static constexpr int XSOFF = SL * (BUF + CSCR);
+  static constexpr int PLANES = XSOFF + SL * XS;
   static constexpr int ZSCR = (512 / LG) * GZ::SCR;
   static constexpr int REGION = PLANES > ZSCR ? PLANES : ZSCR;  // float2, phases A/C and B share it
   static_assert(NT % 32 == 0 && 512 % NT == 0 && N % SL == 0, "plane slices");
 };
 
+constexpr int kBigBars = 8;  // mbarriers after the reduction area (one per plane slice)
+
 template <int N, int LG>
 constexpr size_t big3d_smem() {
-  return (size_t)Big3D<N, LG>::REGION * sizeof(float2) + kBigRed * sizeof(float);
+  return (size_t)Big3D<N, LG>::REGION * sizeof(float2) + kBigRed * sizeof(float) + kBigBars * sizeof(uint64_t);
 }
 
 constexpr size_t kWorkBytes =
@@ -287,6 +291,9 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
   float2* rowbuf = buf + grp * PITCH;
   float* red = reinterpret_cast<float*>(work + B3::REGION);
   int* shv = reinterpret_cast<int*>(red + 16 * 16);
+  uint64_t* xbar = reinterpret_cast<uint64_t*>(red + kBigRed) + sub;  // this slice's plane copies
+  float2* xs = work + B3::XSOFF + sub * B3::XS;                       // this slice's staged plane
+  static_assert(SL <= kBigBars, "one mbarrier per slice");
   float2* X = a.scratch + (size_t)blockIdx.x * a.scratch_per_cta;
   const int sol = world / a.n_init;
   const float2* kp = a.kp + (size_t)sol * N * PLANE;  // [N][N][HW], scaled by 1/N^3
@@ -299,6 +306,16 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
   const int c = grp;  // column pair of the column passes: (c, N-c); c == 0 carries (0, N/2)
   const int c1 = c != 0 ? c : 0, c2 = c != 0 ? N - c : N / 2;
   if (threadIdx.x == 0) shv[0] = shv[1] = shv[2] = 0;
+  if (tid == 0) {
+    mbar_init(xbar, 1);
+    fence_proxy_async();
+  }
+  unsigned xph = 0;  // phase parity of this slice's next plane copy
+  // bulk copy of spectrum plane z into the slice's staging buffer
+  auto stage_plane = [&](int z) {
+    mbar_arrive_expect_tx(xbar, (unsigned)(PLANE * sizeof(float2)));
+    bulk_load(xs, X + (size_t)z * PLANE, (unsigned)(PLANE * sizeof(float2)), xbar);
+  };
   __syncthreads();
   for (int step = 0; step < a.steps; ++step) {
     const float* src = step == 0 ? c0 : st;
@@ -408,6 +425,14 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
     }
     __syncthreads();
     // ---------------------------------------------------------- C. planes inverse
+    // Each slice's spectrum planes arrive by bulk copy into its staging
+    // buffer: plane z + SL is issued once every thread of the slice is past
+    // its reads of plane z (the slice barrier between the column and row
+    // inverses), so it lands during plane z's row inverse.
+    if (tid == 0) {
+      fence_proxy_async();
+      stage_plane(sub);
+    }
     float acc[14];
 #pragma unroll
     for (int i = 0; i < 14; ++i) acc[i] = 0.f;
@@ -415,12 +440,14 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
     const int sz = shv[0], sy = shv[1], sx = shv[2];
     for (int zb = 0; zb < N; zb += SL) {
       const int z = zb + sub;
-      if (tid == 0 && z + SL < N) {
-        prefetch_l2(X + (size_t)(z + SL) * PLANE, (unsigned)(PLANE * sizeof(float2)));
-        prefetch_l2(src + (size_t)(z + SL) * N * N, N * N * sizeof(float));
+      if (tid == 0 && z + SL < N) prefetch_l2(src + (size_t)(z + SL) * N * N, N * N * sizeof(float));
+      if (!mbar_wait(xbar, xph)) {  // the plane never landed: record it, give it a bounded second wait
+        if (tid == 0 && a.status) atomicExch(a.status, kStatusCopyTimeout);
+        mbar_wait(xbar, xph);
       }
+      xph ^= 1u;
       {
-        const float2* xz = X + (size_t)z * PLANE;
+        const float2* xz = xs;
         float2 w[P];
 #pragma unroll
         for (int k1 = 0; k1 < P; ++k1) {
@@ -443,6 +470,10 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
         }
       }
       named_bar(bar_id, NT);
+      if (tid == 0 && z + SL < N) {  // the slice is done with xs: stage its next plane
+        fence_proxy_async();
+        stage_plane(z + SL);
+      }
       {
         const int r = grp;
         float2 v[Q][G];
@@ -495,6 +526,8 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
     }
     big_finish_step(a, world, step, 3, sizes, acc, border, red, shv);
   }
+  __syncthreads();
+  if (tid == 0) mbar_inval(xbar);  // the area holds other items' data next
 }
 
 template <int N, int G, int GF>

@@ -120,7 +120,7 @@ int validate(const lgx_batch_job* j) {
 struct Layout {
   int grid;
   long scratch_per_cta;
-  size_t cls_off, items_off, head_off, scratch_off, end;
+  size_t status_off, cls_off, items_off, head_off, scratch_off, end;
   size_t kp_off[LGX_BATCH_MAX_CLASSES], raw_off[LGX_BATCH_MAX_CLASSES];
   int n_items[LGX_BATCH_MAX_CLASSES];
   int total_items;
@@ -130,6 +130,8 @@ Layout layout_of(const lgx_batch_job* j) {
   Layout L;
   std::memset(&L, 0, sizeof(L));
   size_t off = 0;
+  L.status_off = off;  // first int: device status word (lgx_workspace_status)
+  off = al256(off + sizeof(int));
   L.cls_off = off;
   off = al256(off + sizeof(BatchClassArgs) * kMaxBatchClasses);
   for (int i = 0; i < j->n_classes; ++i) {
@@ -236,7 +238,8 @@ int lgx_batch_run(const lgx_batch_job* j, void* ws, size_t ws_bytes, void* strea
   if (!ws || ws_bytes < L.end)
     return bfail(LGX_ERR_WORKSPACE, "lgx_batch_run: workspace %zu < %zu bytes", ws_bytes, L.end);
   char* base = static_cast<char*>(ws);
-  cudaError_t e = cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(base + L.status_off, 0, sizeof(int), st);  // status word
+  if (e != cudaSuccess) return bfail(LGX_ERR_CUDA, "lgx_batch_run memset: %s", cudaGetErrorString(e));
 
   BatchSetup su;
   std::memset(&su, 0, sizeof(su));
@@ -275,6 +278,7 @@ int lgx_batch_run(const lgx_batch_job* j, void* ws, size_t ws_bytes, void* strea
       b.raw = raw;
       b.scratch = reinterpret_cast<float2*>(base + L.scratch_off);
       b.scratch_per_cta = L.scratch_per_cta;
+      b.status = reinterpret_cast<int*>(base + L.status_off);
     } else {
       ResidentArgs& r = a.r;
       r.n_worlds = c.n_worlds;

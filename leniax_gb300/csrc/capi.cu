@@ -298,6 +298,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     b.raw = raw;
     b.scratch = reinterpret_cast<float2*>(base + L.scratch);
     b.scratch_per_cta = big_kind_scratch(m.nb_dims, m.H);
+    b.status = static_cast<int*>(ws);
     if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
     ce = launch_big_rollout(m.nb_dims, m.H, b, m.gf[0], L.grid, base + L.setup, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "one-world-per-CTA rollout");

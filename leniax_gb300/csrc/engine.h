@@ -76,6 +76,7 @@ struct BigArgs {
   float* raw;            // [n_worlds, steps, raw_stride(1)]
   float2* scratch;       // [grid, scratch_per_cta] spectrum scratch
   long scratch_per_cta;  // float2 elements
+  int* status;           // device status word (set when a staged copy never lands), or null
 };
 enum BatchKind : int { BK_R32 = 0, BK_R64 = 1, BK_R128 = 2, BK_B2D256 = 3, BK_B3D32 = 4, BK_B3D64 = 5 };
 constexpr int kMaxBatchClasses = 8;

@@ -75,7 +75,7 @@ def test_uneven_batch_matches_oracle_per_world(cuda):
     b = lbatch.UnevenBatch(classes, steps)
     b.run()
     res = b.results()
-    torch.cuda.synchronize()
+    assert b.status() == 0  # every staged copy landed
     for ci, ((nd, size, n, _), (R, m, s, T)) in enumerate(zip(SPEC, params)):
         out = res[ci]
         fin = out['final'].cpu().numpy()
