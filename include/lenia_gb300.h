@@ -228,6 +228,14 @@ LGX_API int lgx_kernel_spectrum(int H, int W, int planes, const float* k_real, f
  * least `blocks` floats (written only if an impossible value appears). */
 LGX_API long long lgx_fp32_probe(float* sink, int blocks, int iters, void* stream);
 
+/* Failure-detection self test (no counterpart in the reference): one block
+ * arms an mbarrier for two arrivals, makes one, and waits on it with the
+ * engines' bounded wait, limited to `max_polls` polls.  The wait runs out,
+ * the kernel writes the engines' timeout status (1) to `status` (a device int)
+ * and returns; nothing faults and the context stays usable.  Returns
+ * LGX_OK / LGX_ERR_INVALID / LGX_ERR_CUDA. */
+LGX_API int lgx_selftest_wait_timeout(int max_polls, int* status, void* stream);
+
 /* ---------------------------------------------------------------------------
  * Allocation-free rollout.  No counterpart in the reference: leniax runs on
  * JAX, which owns all device buffers.

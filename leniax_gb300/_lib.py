@@ -36,7 +36,7 @@ EXPORTED = (
     'lgx_version', 'lgx_last_error', 'lgx_plan_create', 'lgx_plan_destroy', 'lgx_select_engine',
     'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update', 'lgx_fp32_probe',
     'lgx_batch_workspace_bytes', 'lgx_batch_run', 'lgx_workspace_status', 'lgx_ring_kernels_workspace_bytes',
-    'lgx_ring_kernels'
+    'lgx_ring_kernels', 'lgx_selftest_wait_timeout'
 )
 
 
@@ -127,6 +127,8 @@ def load():
         lib.lgx_workspace_status.restype = ctypes.c_int
         lib.lgx_fp32_probe.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]
         lib.lgx_fp32_probe.restype = ctypes.c_longlong
+        lib.lgx_selftest_wait_timeout.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        lib.lgx_selftest_wait_timeout.restype = ctypes.c_int
         if lib.lgx_version() != 1:
             raise RuntimeError('leniax_gb300 engine ABI version mismatch')
         _lib = lib

@@ -39,6 +39,10 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned by
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   uint32_t ok;
   asm volatile(
@@ -52,9 +56,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
 }
 
 // Wait for phase `parity` of `bar` to complete; false if it did not within
-// kMbarMaxTries polls.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-  for (int i = 0; i < kMbarMaxTries; ++i)
+// `max_tries` polls (kMbarMaxTries by default).
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, int max_tries = kMbarMaxTries) {
+  for (int i = 0; i < max_tries; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }
