@@ -578,7 +578,7 @@ def check_heuristics(stats: Dict[str, np.ndarray]) -> np.ndarray:
     return out
 
 
-# Search-batch stop set (BASELINE search config): a world stops at the first
+# Search-batch stop set (the search workload's stop conditions): a world stops at the first
 # step whose pre-update state has raw mass below 1e-3, raw mass above
 # 0.9 * area, or a live cell (> EPSILON) on the outer rows/columns of the
 # un-centred torus.  This is this project's own stop set, not leniax's.

@@ -11,7 +11,7 @@ from tests.cases import bump_kernel_params, patch_init
 
 pytestmark = pytest.mark.gpu
 
-REL = 1e-3  # gradient relative error bound (spec: <= 1e-3 vs finite differences)
+REL = 1e-3  # gradient relative error bound vs finite differences / float64 autograd
 
 
 def relerr(a, b):

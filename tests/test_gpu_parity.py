@@ -9,7 +9,7 @@ from tests.cases import bump_kernel_params, golden_case, golden_world, patch_ini
 
 pytestmark = pytest.mark.gpu
 
-# single step vs leniax's FP32 op order (spec: max abs error <= 1e-5)
+# single step vs leniax's FP32 op order: max abs error <= 1e-5
 STEP_TOL = 1e-5
 
 
