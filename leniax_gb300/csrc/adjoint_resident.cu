@@ -19,6 +19,7 @@
 #include <algorithm>
 
 #include "resident.cuh"
+#include "tma.cuh"
 
 namespace lgx {
 
@@ -242,6 +243,12 @@ __global__ void __launch_bounds__(512, 1) adjoint_resident_kernel(AdjResArgs a) 
     const float2* kk = a.kp + (size_t)sol * N * KP;
     float2* gk = a.gk + ((size_t)world * (N / 2) + c) * N;
     for (int st = a.steps - 1; st >= 0; --st) {
+      // L2 prefetch of the previous step's trajectory planes (cells, potential), 16 KB pieces
+      if (st > 0 && tid < 2 * (int)(plane * sizeof(float) / 16384)) {
+        const int per = (int)(plane * sizeof(float) / 16384), piece = tid % per;
+        const float* base = (tid < per ? a.traj_cells : a.traj_pot) + ((size_t)(st - 1) * a.n_worlds + world) * plane;
+        prefetch_l2(base + (size_t)piece * 4096, 16384);
+      }
       // ---------------------------------------------------------- pointwise + row FFTs of a and s
       {
         const size_t off = ((size_t)st * a.n_worlds + world) * plane + (size_t)(2 * grp) * N;
