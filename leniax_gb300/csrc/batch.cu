@@ -126,6 +126,11 @@ __device__ __forceinline__ void big_finish_step(const BigArgs& a, int world, int
 }
 
 // ------------------------------------------------------------------ big 2D
+// Euler rate of a big item's world (BigArgs::dt_mode).
+__device__ __forceinline__ float big_dt(const BigArgs& a, int world, int sol) {
+  return a.dt_mode == 1 ? __ldg(a.dt) : (a.dt_mode == 2 ? __ldg(a.dt + world) : 1.f / __ldg(a.T + sol));
+}
+
 template <int N, int GF>
 __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float2* tw, float2* work) {
   constexpr int G = 8;
@@ -144,7 +149,7 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
   float* st = a.state + (size_t)world * N * N;
   const GrowthP gq = big_growth<GF>(a, sol);
   const float wk = __ldg(a.w + sol), wf = a.mean ? wk / wk : wk;
-  const float dt = 1.f / __ldg(a.T + sol);
+  const float dt = big_dt(a, world, sol);
   const int sizes[3] = {N, N, 1};
   if (threadIdx.x == 0) shv[0] = shv[1] = shv[2] = 0;
   __syncthreads();
@@ -301,7 +306,7 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
   float* st = a.state + (size_t)world * N * N * N;
   const GrowthP gq = big_growth<GF>(a, sol);
   const float wk = __ldg(a.w + sol), wf = a.mean ? wk / wk : wk;
-  const float dt = 1.f / __ldg(a.T + sol);
+  const float dt = big_dt(a, world, sol);
   const int sizes[3] = {N, N, N};
   const int c = grp;  // column pair of the column passes: (c, N-c); c == 0 carries (0, N/2)
   const int c1 = c != 0 ? c : 0, c2 = c != 0 ? N - c : N / 2;
@@ -495,6 +500,21 @@ __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float
           const float fa = weighted_growth<GF>(gq, pa, wf), fb = weighted_growth<GF>(gq, pb, wf);
           dsa[x] = state_fn(a.state_fn, sa, fa, dt);
           dsa[N + x] = state_fn(a.state_fn, sb, fb, dt);
+          if (a.traj_cells || a.traj_field || a.traj_pot) {  // run_scan trajectories (runner.py:119-164)
+            const size_t tb = ((size_t)step * a.n_worlds + world) * N * N * N + ((size_t)z * N + 2 * r) * N + x;
+            if (a.traj_cells) {
+              a.traj_cells[tb] = sa;
+              a.traj_cells[tb + N] = sb;
+            }
+            if (a.traj_field) {
+              a.traj_field[tb] = fa;
+              a.traj_field[tb + N] = fb;
+            }
+            if (a.traj_pot) {
+              a.traj_pot[tb] = pa;
+              a.traj_pot[tb + N] = pb;
+            }
+          }
           const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
           const float cx = (float)(((x - sx) & (N - 1)) - N / 2);
           Sa += sa;

@@ -273,8 +273,6 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
   if (ce != cudaSuccess) return cuda_fail(ce, "memset");
   float* raw = nullptr;
   if (e == LGX_ENGINE_CTA) {
-    if (j->traj_cells || j->traj_field || j->traj_potential)
-      return fail(LGX_ERR_UNSUPPORTED, "lgx_run: the one-world-per-CTA engine (3D worlds) writes no trajectories");
     const CtaLayout L = cta_layout(m, j->n_sols, j->n_init, j->steps);
     char* base = static_cast<char*>(ws);
     float2* kp = reinterpret_cast<float2*>(base + L.kp);
@@ -299,6 +297,9 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     b.scratch = reinterpret_cast<float2*>(base + L.scratch);
     b.scratch_per_cta = big_kind_scratch(m.nb_dims, m.H);
     b.status = static_cast<int*>(ws);
+    b.traj_cells = j->traj_cells;
+    b.traj_field = j->traj_field;
+    b.traj_pot = j->traj_potential;
     if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
     ce = launch_big_rollout(m.nb_dims, m.H, b, m.gf[0], L.grid, base + L.setup, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "one-world-per-CTA rollout");
@@ -444,8 +445,10 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
 size_t lgx_update_workspace_bytes(const lgx_plan* plan, int n) {
   if (!plan || n < 1) return 0;
   const Model& m = plan->m;
-  // lgx_update runs one streamed step for every model (resident sizes included)
+  // lgx_update runs one streamed step for every 2D model (resident sizes
+  // included) and a one-step one-world-per-CTA rollout for 3D models
   if (streamed_supported(m)) return streamed_ws(m, 1, n, 1, false);
+  if (cta_supported(m)) return cta_layout(m, 1, n, 1).end;
   return 0;
 }
 
@@ -462,6 +465,41 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
   if (!ws || ws_bytes < need) return fail(LGX_ERR_WORKSPACE, "lgx_update: workspace %zu < %zu bytes", ws_bytes, need);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   cudaError_t ce;
+  if (cta_supported(m)) {
+    // 3D: one step of the plane-fused item, field and potential as its step-0 trajectory
+    const CtaLayout L = cta_layout(m, 1, n, 1);
+    char* base = static_cast<char*>(ws);
+    ce = cudaMemsetAsync(ws, 0, sizeof(int), st);  // status word
+    if (ce != cudaSuccess) return cuda_fail(ce, "memset");
+    float2* kp = reinterpret_cast<float2*>(base + L.kp);
+    ce = launch_prepare_3d_spectrum(m.H, 1, reinterpret_cast<const float2*>(k_half), kp, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    BigArgs b;
+    std::memset(&b, 0, sizeof(b));
+    b.n_worlds = n;
+    b.n_init = n;  // every world belongs to the one solution
+    b.steps = 1;
+    b.gf_id = m.gf[0];
+    b.state_fn = m.state_fn;
+    b.mean = m.mean;
+    b.cells0 = state;
+    b.kp = kp;
+    b.gf = gf_params;
+    b.w = weights;
+    b.dt = dt;
+    b.dt_mode = dt_per_world ? 2 : 1;
+    b.state = state_out;
+    b.raw = reinterpret_cast<float*>(base + L.raw);
+    b.scratch = reinterpret_cast<float2*>(base + L.scratch);
+    b.scratch_per_cta = big_kind_scratch(m.nb_dims, m.H);
+    b.status = static_cast<int*>(ws);
+    b.traj_field = field_out;
+    b.traj_pot = potential_out;
+    ce = launch_big_rollout(m.nb_dims, m.H, b, m.gf[0], L.grid, base + L.setup, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "3D update");
+    g_err.clear();
+    return LGX_OK;
+  }
   if (!streamed_supported(m) && !resident_supported(m)) return fail(LGX_ERR_UNSUPPORTED, "lgx_update: unsupported");
   if (streamed_supported(m)) {
     StreamedBufs b = carve_streamed(m, 1, n, 1, ws, ws_bytes, false);

@@ -77,6 +77,12 @@ struct BigArgs {
   float2* scratch;       // [grid, scratch_per_cta] spectrum scratch
   long scratch_per_cta;  // float2 elements
   int* status;           // device status word (set when a staged copy never lands), or null
+  // 3D items: per-step outputs [steps, n_worlds, N^3] (pre-update cells, field, potential), or null
+  float* traj_cells;
+  float* traj_field;
+  float* traj_pot;
+  const float* dt;  // dt_mode 1: dt[0]; 2: dt[world]
+  int dt_mode;      // 0: 1 / T[sol] (rollouts); 1: one dt; 2: one dt per world (single updates)
 };
 enum BatchKind : int { BK_R32 = 0, BK_R64 = 1, BK_R128 = 2, BK_B2D256 = 3, BK_B3D32 = 4, BK_B3D64 = 5 };
 constexpr int kMaxBatchClasses = 8;

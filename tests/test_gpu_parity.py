@@ -329,13 +329,44 @@ def test_run_scan_mem_optimized_3d_matches_oracle(cuda, size):
         assert (d[alive] <= 1e-3 * size).all()
 
 
-def test_3d_update_and_trajectories_are_refused(cuda):
+@pytest.mark.parametrize('size', [32, 64])
+def test_3d_update_single_step_matches_oracle(cuda, size):
+    # core.update on 3D worlds runs one step of the one-world-per-CTA item,
+    # field and potential as its step-0 trajectory; scalar and per-world dt
+    R = size / 6
+    rng = np.random.Generator(np.random.PCG64(size + 3))
+    cells = np.zeros((3, 1, size, size, size), np.float32)
+    p, lo = size // 3, (size - size // 3) // 2
+    cells[..., lo:lo + p, lo:lo + p, lo:lo + p] = rng.random((3, 1, p, p, p), dtype=np.float32)
+    (s, f, pt), (so, fo, po) = single_step_case(bump_kernel_params(s=0.03), [size] * 3, 1, R, cells, 10)
+    assert np.abs(pt - po).max() < 5e-6
+    assert np.abs(s - so).max() <= STEP_TOL
+    assert np.abs(f - fo).max() < 2e-4
     dev = torch.device('cuda')
-    K, mp, upd = engine_model(bump_kernel_params(), [32, 32, 32], 1, 5, dev=dev)
-    cells = torch.zeros((1, 1, 32, 32, 32), device=dev)
-    from leniax_gb300 import _lib
-    with pytest.raises(_lib.LgxError):
-        upd(None, cells, K, mp.get_gf_params(dev), mp.get_kernels_weight_per_channel(dev), 0.1)
-    with pytest.raises(_lib.LgxError):
-        runner.run_scan(None, cells, K, mp.get_gf_params(dev), mp.get_kernels_weight_per_channel(dev),
-                        torch.tensor(10.), 4, 5, upd, statistics.ComputeStatsFn([32] * 3, 5, 10))
+    K, mp, upd = engine_model(bump_kernel_params(s=0.03), [size] * 3, 1, R, dev=dev)
+    Ko, mpo, model = oracle_model(bump_kernel_params(s=0.03), [size] * 3, 1, R)
+    dts = np.array([0.1, 0.2, 0.05], np.float32)
+    s2, _, _ = upd(None, torch.from_numpy(cells).to(dev), K, mp.get_gf_params(dev),
+                   mp.get_kernels_weight_per_channel(dev), torch.from_numpy(dts).to(dev))
+    for i in range(3):
+        so_i, _, _ = O.update(cells[i:i + 1], Ko, mpo['gf_params'], mpo['weights'], dts[i], model)
+        assert np.abs(s2[i:i + 1].cpu().numpy() - so_i).max() <= STEP_TOL
+
+
+def test_3d_run_scan_trajectories_match_oracle(cuda):
+    dev = torch.device('cuda')
+    size, R, steps = 32, 5.0, 6
+    rng = np.random.Generator(np.random.PCG64(11))
+    cells = np.zeros((1, 1, size, size, size), np.float32)
+    cells[..., 11:21, 11:21, 11:21] = rng.random((1, 1, 10, 10, 10), dtype=np.float32)
+    K, mp, upd = engine_model(bump_kernel_params(s=0.03), [size] * 3, 1, R, dev=dev)
+    Ko, mpo, model = oracle_model(bump_kernel_params(s=0.03), [size] * 3, 1, R)
+    cs_o, fs_o, ps_o, st_o = O.run_scan(cells, Ko, mpo['gf_params'], mpo['weights'], 10, steps, R, model)
+    cs, fs, ps, st = runner.run_scan(None, torch.from_numpy(cells).to(dev), K, mp.get_gf_params(dev),
+                                     mp.get_kernels_weight_per_channel(dev), torch.tensor(10.), steps, R, upd,
+                                     statistics.ComputeStatsFn([size] * 3, R, 10))
+    assert tuple(cs.shape) == cs_o.shape and tuple(ps.shape) == ps_o.shape
+    assert np.abs(cs.cpu().numpy() - cs_o).max() < 2e-5
+    assert np.abs(ps.cpu().numpy() - ps_o).max() < 5e-6
+    assert np.abs(fs.cpu().numpy() - fs_o).max() < 5e-4
+    assert np.abs(st['N'].cpu().numpy() - st_o['N']).max() == 0
