@@ -49,6 +49,18 @@ def test_plan_accepts_valid_models():
     assert lib.lgx_run_workspace_bytes(p2.handle, 2, 3, 16, 0) > 0
 
 
+def test_3d_plans_select_the_cta_engine_and_size_workspaces():
+    lib = _lib.load()
+    p = _plan(nb_dims=3, world=(32, 32, 32))
+    assert lib.lgx_select_engine(p.handle, 1, 2, 0) == _lib.ENGINES['cta']
+    assert lib.lgx_update_workspace_bytes(p.handle, 3) > 0  # core.update on 3D worlds
+    assert lib.lgx_run_workspace_bytes(p.handle, 1, 2, 4, 0) > 0
+    # several channels in 3D: no engine, no update workspace
+    p2 = _plan(nb_dims=3, world=(32, 32, 32), nb_channels=2, kernel_cin=[0, 1], kernel_slot=[0, 0], growth_ids=[1, 1])
+    assert lib.lgx_select_engine(p2.handle, 1, 2, 0) == -1
+    assert lib.lgx_update_workspace_bytes(p2.handle, 3) == 0
+
+
 @pytest.mark.parametrize('kw,code', [
     (dict(world=(100, 128)), _lib.LGX_ERR_UNSUPPORTED),
     (dict(nb_dims=4), _lib.LGX_ERR_INVALID),
