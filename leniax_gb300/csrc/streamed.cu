@@ -108,9 +108,10 @@ struct ColCfg {
   static constexpr int BOX_BYTES = (N / 2) * 128;
   static constexpr int TILE_BYTES = BOXES * BOX_BYTES;
   // kernel spectrum columns staged by bulk copy (GPB columns + the Nyquist
-  // column for the block holding pair 0); off at N = 512, where the extra
-  // shared memory would cost a resident block per SM
-  static constexpr bool KSTAGE = N <= 256;
+  // column for the block holding pair 0) up to N = 128; from N = 256 on the
+  // staging buffer would cost a resident block per SM, which measured slower
+  // than the (coalesced, column-major) direct loads
+  static constexpr bool KSTAGE = N <= 128;
   static constexpr int KB_BYTES = KSTAGE ? (GPB + 1) * N * 8 : 0;
   static_assert(GPB % 8 == 0 && (N / 2) % GPB == 0, "column tile");
 };
