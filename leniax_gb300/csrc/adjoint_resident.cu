@@ -244,10 +244,13 @@ __global__ void __launch_bounds__(512, 1) adjoint_resident_kernel(AdjResArgs a) 
     float2* gk = a.gk + ((size_t)world * (N / 2) + c) * N;
     for (int st = a.steps - 1; st >= 0; --st) {
       // L2 prefetch of the previous step's trajectory planes (cells, potential), 16 KB pieces
-      if (st > 0 && tid < 2 * (int)(plane * sizeof(float) / 16384)) {
-        const int per = (int)(plane * sizeof(float) / 16384), piece = tid % per;
-        const float* base = (tid < per ? a.traj_cells : a.traj_pot) + ((size_t)(st - 1) * a.n_worlds + world) * plane;
-        prefetch_l2(base + (size_t)piece * 4096, 16384);
+      constexpr int kPieces = (int)((size_t)N * N * sizeof(float) / 16384);
+      if constexpr (kPieces > 0) {
+        if (st > 0 && tid < 2 * kPieces) {
+          const float* base =
+              (tid < kPieces ? a.traj_cells : a.traj_pot) + ((size_t)(st - 1) * a.n_worlds + world) * plane;
+          prefetch_l2(base + (size_t)(tid % kPieces) * 4096, 16384);
+        }
       }
       // ---------------------------------------------------------- pointwise + row FFTs of a and s
       {
