@@ -329,6 +329,45 @@ def test_run_scan_mem_optimized_3d_matches_oracle(cuda, size):
         assert (d[alive] <= 1e-3 * size).all()
 
 
+def _unfed_channel_params():
+    # C = 2, K = 3: every kernel writes channel 0, so channel 1 gets no field
+    # (its state only moves by dt * 0); weighted_sum mode keeps the field finite
+    base = dict(k_slug='circle_2d', kf_slug='gauss_bump', kf_params=[1.0], gf_slug='gaussian', c_out=0)
+    return [dict(base, k_params=[1.0, [1.0]], gf_params=[0.15, 0.015], h=0.5, c_in=0),
+            dict(base, k_params=[0.6, [0.5, 1.0]], gf_params=[0.25, 0.03], h=0.3, c_in=1),
+            dict(base, k_params=[0.8, [1.0]], gf_params=[0.2, 0.02], h=0.2, c_in=0)]
+
+
+@pytest.mark.parametrize('size', [64, 128])
+def test_streamed_channel_without_incoming_kernels(cuda, size):
+    # the streamed row inverse fetches an unfed channel's state rows outside
+    # the kernel items (no item of that channel starts its copy)
+    R = 13
+    rng = np.random.Generator(np.random.PCG64(size + 5))
+    cells = np.zeros((2, 2, size, size), np.float32)
+    lo = size // 4
+    cells[:, :, lo:3 * lo, lo:3 * lo] = rng.random((2, 2, 2 * lo, 2 * lo), dtype=np.float32)
+    (s, f, p), (so, fo, po) = single_step_case(_unfed_channel_params(), [size, size], 2, R, cells, 10, average=False)
+    assert np.abs(p - po).max() < 2e-6
+    assert np.abs(s - so).max() <= STEP_TOL
+    assert np.abs(f - fo).max() < 2e-4
+    assert np.abs(f[:, 1]).max() == 0.0  # channel 1: no field
+    # a short rollout through lgx_run (fused next-step row FFTs of both channels)
+    dev = torch.device('cuda')
+    K, mp, upd = engine_model(_unfed_channel_params(), [size, size], 2, R, average=False, dev=dev)
+    Ko, mpo, model = oracle_model(_unfed_channel_params(), [size, size], 2, R, average=False)
+    steps = 4
+    _, fin = runner.run_scan_mem_optimized(None, torch.from_numpy(cells[None]).to(dev), K[None],
+                                           mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None],
+                                           torch.tensor([10.]), steps, R, upd,
+                                           statistics.ComputeStatsFn([size, size], R, 10), engine='streamed',
+                                           check_status=True)
+    for i in range(2):
+        _, fo_i = O.run_scan(cells[i:i + 1], Ko, mpo['gf_params'], mpo['weights'], 10, steps, R, model,
+                             keep_intermediary=False)
+        assert np.abs(fin[0, i].cpu().numpy() - fo_i[0]).max() <= 4 * STEP_TOL
+
+
 @pytest.mark.parametrize('size', [32, 64])
 def test_3d_update_single_step_matches_oracle(cuda, size):
     # core.update on 3D worlds runs one step of the one-world-per-CTA item,
