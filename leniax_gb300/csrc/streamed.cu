@@ -4,19 +4,22 @@
 //
 //   row_fwd  : per (world, channel, packed row) N-point FFT of rows (2r, 2r+1)
 //              packed as one complex row -> spec[n][c][r][.] in the
-//              pair-adjacent layout (pa_pos below)
+//              pair-adjacent layout (pa_pos, fft.cuh); first step only
 //   col_conv : per (world, channel, block of column pairs) the block's column
 //              tile arrives by TMA (2D tensor copies, 128-byte swizzle); per
 //              pair: unpack + N-point FFT, then for every kernel reading that
 //              channel: x prepared spectrum (column-major planes, so a
-//              transform's lanes read consecutive ky), inverse FFT -> prod[n][k] (same
-//              pair-adjacent layout)
+//              transform's lanes read consecutive ky; bulk-staged up to
+//              N = 128), inverse FFT -> prod[n][k] (same pair-adjacent
+//              layout), written back through the tile by TMA stores
 //   row_inv  : per (world, block of packed rows) the block's rows of every
-//              kernel's product plane arrive by bulk copies into a double
-//              buffer (the next kernel's rows land while this kernel's are
-//              transformed); inverse row FFTs -> potential, growth, weighted
-//              field in registers (core.py:163-242), state update
-//              (core.py:245-319), per-block raw statistics moments
+//              kernel's product plane arrive by bulk copies into a staging
+//              ring (the next kernel's rows land while this kernel's are
+//              transformed), each channel's state rows by one bulk copy;
+//              inverse row FFTs -> potential, growth, weighted field in
+//              registers (core.py:163-242), state update (core.py:245-319),
+//              per-block raw statistics moments, and the next step's forward
+//              row FFT of the new rows
 //   reduce   : per world: block moments -> raw moments of the step, carried
 //              torus shift update (statistics.py:117-119)
 //
