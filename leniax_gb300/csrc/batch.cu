@@ -275,8 +275,13 @@ __device__ __noinline__ void big2d_item(const BigArgs& a, int world, const float
 //      DC / Nyquist column is split with its ky mirror);
 //   B. z pass over the scratch: lines (ky, kx) on groups of LG lanes, forward
 //      FFT, x prepared spectrum (scaled 1/N^3), inverse FFT;
-//   C. planes inverse: column inverse (DC and Nyquist columns re-packed as
-//      DC + i Nyquist), row inverse -> potential, growth, update, moments.
+//   C. planes inverse: each slice's spectrum plane arrives by bulk copy into
+//      shared memory (issued one plane ahead, mbarrier with a bounded wait);
+//      column inverse (DC and Nyquist columns re-packed as DC + i Nyquist),
+//      row inverse -> potential, growth, update, moments, and the run_scan
+//      trajectories when asked.
+// The next state plane (A, C) and the z pass's next round of lines (B) are
+// prefetched into L2 with bulk prefetches.
 template <int N, int LG, int GF>
 __device__ __noinline__ void big3d_item(const BigArgs& a, int world, const float2* tw4, const float2* twz,
                                         float2* work) {
