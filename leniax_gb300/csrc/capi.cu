@@ -186,8 +186,12 @@ int lgx_plan_create(const lgx_model_desc* d, lgx_plan** out) {
   std::memset(&m, 0, sizeof(m));
   m.nb_dims = d->nb_dims;
   for (int i = 0; i < d->nb_dims; ++i) {
-    if (!is_pow2(d->world[i]) || d->world[i] < 8)
-      return fail(LGX_ERR_UNSUPPORTED, "world axis %d has size %d: power-of-two sizes >= 8 only", i, d->world[i]);
+    const bool generic = d->nb_dims == 2 && generic_size(d->world[i]);  // 2D: even sides of 2, 3, 5, 7
+    if ((!is_pow2(d->world[i]) || d->world[i] < 8) && !generic)
+      return fail(LGX_ERR_UNSUPPORTED,
+                  "world axis %d has size %d: power-of-two sizes >= 8 (2D also even sides of factors 2, 3, 5, 7 "
+                  "up to 512)",
+                  i, d->world[i]);
     m.world[i] = d->world[i];
   }
   m.C = d->nb_channels;

@@ -159,6 +159,14 @@ struct StreamedStep {
   bool emit_spec;          // write the row spectra of `state_out` into spec for the next step
 };
 cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st);
+// The step's moment reducer (bpw blocks of partials per world).
+cudaError_t launch_streamed_reduce(const StreamedStep& s, int bpw, cudaStream_t st);
+// Square 2D worlds of even side factoring into 2, 3, 5, 7 (not a power of
+// two): the mixed-radix streamed step of generic.cu.
+bool generic_size(int n);
+cudaError_t launch_generic_step(const StreamedStep& s, cudaStream_t st);
+cudaError_t launch_prepare_generic_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,
+                                            cudaStream_t st);
 cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,
                                              cudaStream_t st);
 

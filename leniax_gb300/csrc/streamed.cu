@@ -812,11 +812,7 @@ cudaError_t step_n(const StreamedStep& s, cudaStream_t st) {
   else if (all_poly) e = launch_row_inv<N, GF_FAST_POLY4>(s, tab, st);
   else e = launch_row_inv<N, GF_GENERIC>(s, tab, st);
   if (e != cudaSuccess) return e;
-  const int wpb = 8;
-  reduce_kernel<<<(s.n_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.n_worlds, s.n_init, RC::BPW, m.C, N, N,
-                                                                  s.partial, s.raw, s.raw_sol_stride,
-                                                                  s.raw_world_stride, s.shift);
-  return cudaGetLastError();
+  return launch_streamed_reduce(s, RC::BPW, st);
 }
 
 }  // namespace
@@ -824,7 +820,7 @@ cudaError_t step_n(const StreamedStep& s, cudaStream_t st) {
 bool streamed_supported(const Model& m) {
   if (m.nb_dims != 2 || m.H != m.W) return false;
   if (m.C > kMaxChannels || m.K > kMaxKernels) return false;
-  if (!(m.H == 32 || m.H == 64 || m.H == 128 || m.H == 256 || m.H == 512)) return false;
+  if (!(m.H == 32 || m.H == 64 || m.H == 128 || m.H == 256 || m.H == 512) && !generic_size(m.H)) return false;
   return true;
 }
 
@@ -836,7 +832,7 @@ int streamed_blocks_per_world(const Model& m) {
     case 256: return RowInvCfg<256>::BPW;
     case 512: return RowInvCfg<512>::BPW;
   }
-  return 1;
+  return m.H / 2;  // generic sizes: one block per packed row
 }
 
 size_t streamed_workspace_bytes(const Model& m, int n_worlds, int n_sols) {
@@ -851,6 +847,14 @@ size_t streamed_workspace_bytes(const Model& m, int n_worlds, int n_sols) {
   return b;
 }
 
+cudaError_t launch_streamed_reduce(const StreamedStep& s, int bpw, cudaStream_t st) {
+  const int wpb = 8;
+  reduce_kernel<<<(s.n_worlds + wpb - 1) / wpb, 32 * wpb, 0, st>>>(s.n_worlds, s.n_init, bpw, s.m->C, s.m->H, s.m->W,
+                                                                  s.partial, s.raw, s.raw_sol_stride,
+                                                                  s.raw_world_stride, s.shift);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st) {
   // the row inverse bulk-copies state rows: the state base must be 16-byte aligned
   if ((reinterpret_cast<uintptr_t>(s.state) & 15u) != 0) return cudaErrorMisalignedAddress;
@@ -861,6 +865,7 @@ cudaError_t launch_streamed_step(const StreamedStep& s, cudaStream_t st) {
     case 256: return step_n<256>(s, st);
     case 512: return step_n<512>(s, st);
   }
+  if (generic_size(s.m->H)) return launch_generic_step(s, st);
   return cudaErrorInvalidValue;
 }
 
@@ -876,7 +881,9 @@ cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const f
     case 128: prepare_streamed_kernel<128><<<blocks, threads, 0, st>>>(planes, k_half, kp); break;
     case 256: prepare_streamed_kernel<256><<<blocks, threads, 0, st>>>(planes, k_half, kp); break;
     case 512: prepare_streamed_kernel<512><<<blocks, threads, 0, st>>>(planes, k_half, kp); break;
-    default: return cudaErrorInvalidValue;
+    default:
+      if (generic_size(m.H)) return launch_prepare_generic_spectrum(m, n_sols, k_half, kp, st);
+      return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
