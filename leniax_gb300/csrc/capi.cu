@@ -194,6 +194,10 @@ int lgx_plan_create(const lgx_model_desc* d, lgx_plan** out) {
                   i, d->world[i]);
     m.world[i] = d->world[i];
   }
+  for (int i = 0; i < d->nb_dims; ++i)  // the mixed-radix step runs square worlds only
+    if (!is_pow2(d->world[i]) && d->world[0] != d->world[d->nb_dims - 1])
+      return fail(LGX_ERR_UNSUPPORTED, "world %d x %d: sides that are not powers of two need a square world",
+                  d->world[0], d->world[d->nb_dims - 1]);
   m.C = d->nb_channels;
   m.K = d->nb_kernels;
   m.max_k = d->max_k;

@@ -62,7 +62,8 @@ def test_3d_plans_select_the_cta_engine_and_size_workspaces():
 
 
 @pytest.mark.parametrize('kw,code', [
-    (dict(world=(100, 128)), _lib.LGX_ERR_UNSUPPORTED),
+    (dict(world=(100, 128)), _lib.LGX_ERR_UNSUPPORTED),  # a side that is not a power of two: square only
+    (dict(world=(66, 66)), _lib.LGX_ERR_UNSUPPORTED),    # 66 = 2 * 3 * 11: no radix-11 pass
     (dict(nb_dims=4), _lib.LGX_ERR_INVALID),
     (dict(kernel_cin=[1]), _lib.LGX_ERR_INVALID),
     (dict(growth_ids=[42]), _lib.LGX_ERR_UNSUPPORTED),
