@@ -164,6 +164,7 @@ cudaError_t launch_streamed_reduce(const StreamedStep& s, int bpw, cudaStream_t 
 // Square 2D worlds of even side factoring into 2, 3, 5, 7 (not a power of
 // two): the mixed-radix streamed step of generic.cu.
 bool generic_size(int n);
+int generic_blocks_per_world(int n);
 cudaError_t launch_generic_step(const StreamedStep& s, cudaStream_t st);
 cudaError_t launch_prepare_generic_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,
                                             cudaStream_t st);

@@ -18,7 +18,8 @@
 //
 // Each line transform is a mixed-radix Stockham FFT (radices 4, 2, 3, 5, 7,
 // self-sorting, ping-pong between two shared buffers) run by a whole block,
-// one stage per barrier.  Growth uses leniax's operation order (growth_fn).
+// one stage per barrier; the row passes transform several packed rows per
+// block (gen_lines).  Growth uses leniax's operation order (growth_fn).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,6 +39,14 @@ struct GPlan {  // radices of one N-point transform, passed by value
   int n, stages;
   int r[kGMaxStages];
 };
+
+// Packed rows per block of the row passes: the largest of 8, 4, 2, 1 that
+// divides N/2 with at most 1024 points in flight.
+__host__ __device__ inline int gen_lines(int N) {
+  for (int nl = 8; nl > 1; nl >>= 1)
+    if ((N / 2) % nl == 0 && nl * N <= 1024) return nl;
+  return 1;
+}
 
 struct GTab {  // per-plan kernel table, passed by value
   int C, K, max_k, mean, state_fn, dt_mode;
@@ -82,9 +91,13 @@ __device__ void fill_twiddles(float2* tw, int N) {
 // by W_{Ns R}^{q (j mod Ns)}, takes the R-point DFT and writes
 // out[(j / Ns) Ns R + (j mod Ns) + t Ns].
 template <bool INV, int R>
-__device__ __forceinline__ void stockham_stage(const float2* in, float2* out, int N, int Ns, const float2* tw) {
+__device__ __forceinline__ void stockham_stage(const float2* in_all, float2* out_all, int N, int Ns, const float2* tw,
+                                               int nl) {
   const int nb = N / R, stride = N / (Ns * R);
-  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+  for (int jj = threadIdx.x; jj < nl * nb; jj += blockDim.x) {
+    const int line = jj / nb, j = jj - line * nb;  // lines of N points, contiguous
+    const float2* in = in_all + line * N;
+    float2* out = out_all + line * N;
     const int k = j % Ns;
     float2 v[R];
 #pragma unroll
@@ -110,10 +123,11 @@ __device__ __forceinline__ void stockham_stage(const float2* in, float2* out, in
   }
 }
 
-// N-point FFT of a (the block's line) into a or b (returned); unnormalised
-// for INV.  Every thread of the block calls it; it ends on a barrier.
+// N-point FFTs of the block's nl contiguous lines in a into a or b
+// (returned); unnormalised for INV.  Every thread of the block calls it; it
+// ends on a barrier.
 template <bool INV>
-__device__ float2* fft_line(float2* a, float2* b, const GPlan& p, const float2* tw) {
+__device__ float2* fft_line(float2* a, float2* b, const GPlan& p, const float2* tw, int nl = 1) {
   const int N = p.n;
   float2* in = a;
   float2* out = b;
@@ -121,11 +135,11 @@ __device__ float2* fft_line(float2* a, float2* b, const GPlan& p, const float2* 
   for (int s = 0; s < p.stages; ++s) {
     const int R = p.r[s];
     switch (R) {
-      case 2: stockham_stage<INV, 2>(in, out, N, Ns, tw); break;
-      case 3: stockham_stage<INV, 3>(in, out, N, Ns, tw); break;
-      case 4: stockham_stage<INV, 4>(in, out, N, Ns, tw); break;
-      case 5: stockham_stage<INV, 5>(in, out, N, Ns, tw); break;
-      default: stockham_stage<INV, 7>(in, out, N, Ns, tw); break;
+      case 2: stockham_stage<INV, 2>(in, out, N, Ns, tw, nl); break;
+      case 3: stockham_stage<INV, 3>(in, out, N, Ns, tw, nl); break;
+      case 4: stockham_stage<INV, 4>(in, out, N, Ns, tw, nl); break;
+      case 5: stockham_stage<INV, 5>(in, out, N, Ns, tw, nl); break;
+      default: stockham_stage<INV, 7>(in, out, N, Ns, tw, nl); break;
     }
     __syncthreads();
     Ns *= R;
@@ -140,19 +154,22 @@ __device__ float2* fft_line(float2* a, float2* b, const GPlan& p, const float2* 
 __global__ void __launch_bounds__(kGT) gen_row_fwd_kernel(GPlan p, const float* __restrict__ state,
                                                           float2* __restrict__ spec) {
   extern __shared__ __align__(16) float2 gsm[];
-  const int N = p.n, H = N / 2;
+  const int N = p.n, H = N / 2, NL = gen_lines(N), BPP = H / NL;
   float2* tw = gsm;
   float2* A = tw + N;
-  float2* B = A + N;
-  const long plane = blockIdx.x / H;
-  const int r = blockIdx.x % H;
+  float2* B = A + NL * N;
+  const long plane = blockIdx.x / BPP;
+  const int r0 = (blockIdx.x % BPP) * NL;  // packed rows r0 .. r0 + NL - 1: state rows 2 r0 .. 2 r0 + 2 NL - 1
   fill_twiddles(tw, N);
-  const float* src = state + (size_t)plane * N * N + (size_t)(2 * r) * N;
-  for (int x = threadIdx.x; x < N; x += blockDim.x) A[x] = make_float2(src[x], src[N + x]);
+  const float* src = state + (size_t)plane * N * N + (size_t)(2 * r0) * N;
+  for (int i = threadIdx.x; i < NL * N; i += blockDim.x) {
+    const int l = i / N, x = i - l * N;
+    A[i] = make_float2(src[(size_t)(2 * l) * N + x], src[(size_t)(2 * l + 1) * N + x]);
+  }
   __syncthreads();
-  const float2* res = fft_line<false>(A, B, p, tw);
-  float2* dst = spec + ((size_t)plane * H + r) * N;
-  for (int k = threadIdx.x; k < N; k += blockDim.x) dst[k] = res[k];
+  const float2* res = fft_line<false>(A, B, p, tw, NL);
+  float2* dst = spec + ((size_t)plane * H + r0) * N;  // NL consecutive rows
+  for (int i = threadIdx.x; i < NL * N; i += blockDim.x) dst[i] = res[i];
 }
 
 // ------------------------------------------------------------ column conv
@@ -222,6 +239,7 @@ __global__ void __launch_bounds__(kGT) gen_col_conv_kernel(GPlan p, int n_worlds
 }
 
 // ------------------------------------------------------------ rows inverse
+// One block per (world, NL consecutive packed rows).
 __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
     GPlan p, int n_worlds, int n_init, GTab tab, const float2* __restrict__ prod, const float* __restrict__ gfp,
     long gf_sol_stride, const float* __restrict__ wts, long w_sol_stride, const float* __restrict__ dtp,
@@ -229,13 +247,13 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
     float* __restrict__ pot_out, const int* __restrict__ shift, float* __restrict__ partial) {
   extern __shared__ __align__(16) float2 gsm[];
   constexpr int NWARPS = kGT / 32, RAWS_MAX = RAW_CM + kMaxChannels;
-  const int N = p.n, H = N / 2;
+  const int N = p.n, H = N / 2, NL = gen_lines(N), BPW = H / NL;
   float2* tw = gsm;
   float2* A = tw + N;
-  float2* B = A + N;
-  float* fld = reinterpret_cast<float*>(B + N);  // [2N] field of the current channel, rows 2r, 2r+1
-  float* red = fld + 2 * N;                       // [warps][RAWS_MAX]
-  const int n = blockIdx.x / H, r = blockIdx.x % H;
+  float2* B = A + NL * N;
+  float* fld = reinterpret_cast<float*>(B + NL * N);  // [NL][2N] field of the current channel, rows 2r, 2r+1
+  float* red = fld + 2 * NL * N;                      // [warps][RAWS_MAX]
+  const int n = blockIdx.x / BPW, r0 = (blockIdx.x % BPW) * NL;
   if (n >= n_worlds) return;
   const int sol = n / n_init, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int C = tab.C, K = tab.K;
@@ -247,7 +265,6 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
   else if (tab.dt_mode == 1) dt = __ldg(dtp + n);
   else dt = 1.f / __ldg(dtp + sol);
   const int sy = shift[3 * n], sx = shift[3 * n + 1];
-  const float cya = (float)(pmod(2 * r - sy, N) - N / 2), cyb = (float)(pmod(2 * r + 1 - sy, N) - N / 2);
   for (int i = threadIdx.x; i < NWARPS * RAWS_MAX; i += blockDim.x) red[i] = 0.f;
   float cpot = 0.f, m00 = 0.f, g00 = 0.f, cmass = 0.f, cgrow = 0.f, mxy = 0.f, mxx = 0.f, gxy = 0.f, gxx = 0.f,
         m2y = 0.f, m2x = 0.f;
@@ -255,10 +272,12 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
   unsigned long long counted = 0ull;
   const float4* pr = reinterpret_cast<const float4*>(prod);
 
-  // kernel k's potential rows into the returned buffer (x < N: (row 2r, row 2r+1))
+  // kernel k's potential rows into the returned buffer: element l N + x holds
+  // (row 2(r0+l), row 2(r0+l)+1) at column x
   auto potential = [&](int k) -> const float2* {
-    const float4* row = pr + (((size_t)n * K + k) * H + r) * H;
-    for (int kx = threadIdx.x; kx < N; kx += blockDim.x) {
+    for (int i = threadIdx.x; i < NL * N; i += blockDim.x) {
+      const int l = i / N, kx = i - l * N;
+      const float4* row = pr + (((size_t)n * K + k) * H + r0 + l) * H;
       float2 z;
       if (kx == 0 || kx == H) {
         const float4 q = row[0];  // (P[2r][0] + i P[2r][N/2], P[2r+1][0] + i P[2r+1][N/2])
@@ -270,17 +289,18 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
         const float4 q = row[N - kx];  // conj(P[2r][N-kx]) + i conj(P[2r+1][N-kx])
         z = make_float2(q.x + q.w, q.z - q.y);
       }
-      A[kx] = z;
+      A[i] = z;
     }
     __syncthreads();
-    return fft_line<true>(A, B, p, tw);
+    return fft_line<true>(A, B, p, tw, NL);
   };
   auto count = [&](int k, const float2* pot) {
-    for (int x = threadIdx.x; x < N; x += blockDim.x) {
-      const float pa = pot[x].x, pb = pot[x].y;
+    for (int i = threadIdx.x; i < NL * N; i += blockDim.x) {
+      const int l = i / N, x = i - l * N;
+      const float pa = pot[i].x, pb = pot[i].y;
       cpot += (pa > kEps ? 1.f : 0.f) + (pb > kEps ? 1.f : 0.f);
       if (pot_out) {
-        float* po = pot_out + ((size_t)n * K + k) * N * N + (size_t)(2 * r) * N;
+        float* po = pot_out + ((size_t)n * K + k) * N * N + (size_t)(2 * (r0 + l)) * N;
         po[x] = pa;
         po[N + x] = pb;
       }
@@ -290,7 +310,7 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
   for (int co = 0; co < C; ++co) {
     float wsum = 0.f;
     for (int k = 0; k < K; ++k) wsum += __ldg(wt + co * K + k);
-    for (int i = threadIdx.x; i < 2 * N; i += blockDim.x) fld[i] = 0.f;
+    for (int i = threadIdx.x; i < 2 * NL * N; i += blockDim.x) fld[i] = 0.f;
     __syncthreads();
     for (int k = 0; k < K; ++k) {
       const float wk = __ldg(wt + co * K + k);
@@ -300,25 +320,29 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
       counted |= 1ull << k;
       const float m = __ldg(gf + 2 * k), s = __ldg(gf + 2 * k + 1);
       const int id = tab.gf[k];
-      for (int x = threadIdx.x; x < N; x += blockDim.x) {
-        fld[x] = fmaf(wk, growth_fn(id, pot[x].x, m, s), fld[x]);
-        fld[N + x] = fmaf(wk, growth_fn(id, pot[x].y, m, s), fld[N + x]);
+      for (int i = threadIdx.x; i < NL * N; i += blockDim.x) {
+        const int l = i / N, x = i - l * N;
+        float* fl = fld + (size_t)l * 2 * N;
+        fl[x] = fmaf(wk, growth_fn(id, pot[i].x, m, s), fl[x]);
+        fl[N + x] = fmaf(wk, growth_fn(id, pot[i].y, m, s), fl[N + x]);
       }
       __syncthreads();
     }
     // field, state update and moments of channel co (statistics.py:64-100)
-    const size_t base = ((size_t)n * C + co) * N * N + (size_t)(2 * r) * N;
     float cm = 0.f;
-    for (int x = threadIdx.x; x < N; x += blockDim.x) {
+    for (int i = threadIdx.x; i < NL * N; i += blockDim.x) {
+      const int l = i / N, x = i - l * N, r = r0 + l;
+      const size_t base = ((size_t)n * C + co) * N * N + (size_t)(2 * r) * N;
       const float cx = (float)(pmod(x - sx, N) - N / 2);
 #pragma unroll
       for (int e = 0; e < 2; ++e) {
-        float f = fld[e * N + x];
+        float f = fld[(size_t)l * 2 * N + e * N + x];
         if (tab.mean) f = f / wsum;
         const float sv = __ldg(state + base + (size_t)e * N + x);
         state_out[base + (size_t)e * N + x] = state_fn(tab.state_fn, sv, f, dt);
         if (field_out) field_out[base + (size_t)e * N + x] = f;
-        const float fp = fmaxf(f, 0.f), cy = e ? cyb : cya;
+        const int y = 2 * r + e;
+        const float fp = fmaxf(f, 0.f), cy = (float)(pmod(y - sy, N) - N / 2);
         m00 += sv;
         g00 += fp;
         cm += sv;
@@ -331,7 +355,6 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
         const bool live = sv > kEps;
         cmass += live ? 1.f : 0.f;
         cgrow += fp > kEps ? 1.f : 0.f;
-        const int y = 2 * r + e;
         border |= live && (x == 0 || x == N - 1 || y == 0 || y == N - 1);
       }
     }
@@ -370,7 +393,7 @@ __global__ void __launch_bounds__(kGT) gen_row_inv_kernel(
     float sum = 0.f;
     for (int w = 0; w < NWARPS; ++w) sum += red[w * RAWS_MAX + threadIdx.x];
     if (threadIdx.x == RAW_BORDER) sum = sum > 0.f ? 1.f : 0.f;
-    partial[((size_t)n * H + r) * RAWS + threadIdx.x] = sum;
+    partial[((size_t)n * BPW + blockIdx.x % BPW) * RAWS + threadIdx.x] = sum;
   }
 }
 
@@ -448,20 +471,23 @@ cudaError_t launch_generic_step(const StreamedStep& s, cudaStream_t st) {
     tab.gf[k] = m.gf[k];
   }
   const long planes = (long)s.n_worlds * m.C;
-  const size_t sm_fwd = (size_t)3 * N * sizeof(float2);
+  const int NL = gen_lines(N), BPW = H / NL;
+  const size_t sm_fwd = (size_t)(1 + 2 * NL) * N * sizeof(float2);
   const size_t sm_col = (size_t)6 * N * sizeof(float2);
-  const size_t sm_inv = (size_t)3 * N * sizeof(float2) + (size_t)2 * N * sizeof(float) +
+  const size_t sm_inv = (size_t)(1 + 2 * NL) * N * sizeof(float2) + (size_t)2 * NL * N * sizeof(float) +
                         (size_t)(kGT / 32) * (RAW_CM + kMaxChannels) * sizeof(float);
   // the row spectra are recomputed every step (no fused next-step transform here)
-  gen_row_fwd_kernel<<<(unsigned)(planes * H), kGT, sm_fwd, st>>>(p, s.state, s.spec);
+  gen_row_fwd_kernel<<<(unsigned)(planes * BPW), kGT, sm_fwd, st>>>(p, s.state, s.spec);
   gen_col_conv_kernel<<<(unsigned)(planes * H), kGT, sm_col, st>>>(p, s.n_worlds, s.n_init, tab, s.spec, s.kp,
                                                                      s.kp_sol_stride, s.prod);
-  gen_row_inv_kernel<<<(unsigned)((long)s.n_worlds * H), kGT, sm_inv, st>>>(
+  gen_row_inv_kernel<<<(unsigned)((long)s.n_worlds * BPW), kGT, sm_inv, st>>>(
       p, s.n_worlds, s.n_init, tab, s.prod, s.gf, s.gf_sol_stride, s.w, s.w_sol_stride, s.dt, s.state, s.state_out,
       s.field_out, s.pot_out, s.shift, s.partial);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  return launch_streamed_reduce(s, H, st);
+  return launch_streamed_reduce(s, BPW, st);
 }
+
+int generic_blocks_per_world(int N) { return (N / 2) / gen_lines(N); }
 
 }  // namespace lgx

@@ -832,7 +832,7 @@ int streamed_blocks_per_world(const Model& m) {
     case 256: return RowInvCfg<256>::BPW;
     case 512: return RowInvCfg<512>::BPW;
   }
-  return m.H / 2;  // generic sizes: one block per packed row
+  return generic_blocks_per_world(m.H);  // generic sizes: a few packed rows per block
 }
 
 size_t streamed_workspace_bytes(const Model& m, int n_worlds, int n_sols) {
