@@ -36,10 +36,28 @@ KPARAMS = [{
     'k_slug': 'circle_2d', 'k_params': [1.0, [1.0]], 'kf_slug': 'gauss_bump', 'kf_params': [1.0], 'gf_slug': 'gaussian',
     'gf_params': [0.15, 0.015], 'h': 1.0, 'c_in': 0, 'c_out': 0
 }]
-# per world-step algorithmic flops (P = cells per channel, C = K = 1):
-#   (C+K)*2.5*P*log2(P) + 6*K*(P/2+1) + 8*K*P + 2*K*P + 4*C*P + 10*C*P
 P_CELLS = SIZE * SIZE
-FLOPS_PER_WORLD_STEP = 2 * 2.5 * P_CELLS * np.log2(P_CELLS) + 6 * (P_CELLS // 2 + 1) + (8 + 2 + 4 + 10) * P_CELLS
+
+
+def flops_per_world_step(C, K, P, stats=True):
+    """Algorithmic flops of one Euler step of one world with P cells per
+    channel: r2c + c2r transforms (C + K) * 2.5 P log2 P, spectrum multiply
+    6 K (P/2 + 1), growth 8 K P (exp counted as 1), weighting 2 K P, Euler +
+    clip 4 C P, statistics 10 C P."""
+    f = (C + K) * 2.5 * P * np.log2(P) + 6 * K * (P // 2 + 1) + (8 + 2) * K * P + 4 * C * P
+    return f + (10 * C * P if stats else 0)
+
+
+def adjoint_flops_per_world_step(P):
+    """Algorithmic flops of one reverse step of a C = K = 1 world: transforms
+    of dL/du and of the state and the inverse of the correlation 3 * 2.5 P
+    log2 P, the conjugate-spectrum product and the kernel-gradient
+    accumulation 14 (P/2 + 1), the pointwise adjoint (clip gradient, growth
+    derivative, parameter partial sums) 20 P."""
+    return 3 * 2.5 * P * np.log2(P) + 14 * (P // 2 + 1) + 20 * P
+
+
+FLOPS_PER_WORLD_STEP = flops_per_world_step(1, 1, P_CELLS)
 CPU_SAMPLE_WORLDS, CPU_SAMPLE_STEPS = 64, 320
 PLAIN_SAMPLE_WORLDS, PLAIN_SAMPLE_STEPS = 4, 64
 
@@ -140,11 +158,13 @@ def measured_peaks():
         return {}
 
 
-# DRAM bytes (read + write) of one resident_kernel launch of this workload,
-# from the ncu full-set capture summarised in profiles/resident_kernel_search1024.md:
-# 134.4 MB read + 92.2 MB written for 2048 worlds x 16 steps; state traffic
-# scaled to 1024 worlds plus the raw moments (19 floats per world-step) of 1024 steps.
-RESIDENT_TRAFFIC_BYTES = 191.7e6
+# DRAM bytes (read + write) of the resident kernel, measured with ncu
+# (dram__bytes_read.sum + dram__bytes_write.sum) on this workload at 1024
+# worlds x 64 and x 128 steps and split into a per-world term (state in and
+# out) and a per-world-step term (the raw moment record); the bench scales
+# them to its own worlds and steps.
+RESIDENT_DRAM_BYTES_PER_WORLD = 131072.0
+RESIDENT_DRAM_BYTES_PER_WORLD_STEP = 76.0
 
 
 def run_ours(args, rank, world_size):
@@ -274,9 +294,9 @@ def run_ours(args, rank, world_size):
     torch.cuda.synchronize()
     plain_value = PLAIN_SAMPLE_WORLDS * P_CELLS * PLAIN_SAMPLE_STEPS / (p0.elapsed_time(p1) / 1e3)
 
-    adjoint = measure_adjoint(dev)
-    multichannel = measure_multichannel(dev)
-    uneven = measure_uneven(dev)
+    adjoint = measure_adjoint(dev, fp32_peak=fp32_peak)
+    multichannel = measure_multichannel(dev, fp32_peak=fp32_peak)
+    uneven = measure_uneven(dev, fp32_peak=fp32_peak)
 
     gpu_launches = args.steps * 4  # prepare spectrum, resident kernel, stats, heuristics per rollout
     out = {
@@ -302,7 +322,8 @@ def run_ours(args, rank, world_size):
         'e2e': {'value': e2e_value, 'unit': METRIC, 'h2d_bytes_per_step': int(h2d), 'd2h_bytes_per_step': int(d2h)},
         'roofline': {
             'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s', 'frac': achieved / fp32_peak,
-            'traffic': RESIDENT_TRAFFIC_BYTES, 'kernel': 'resident_kernel<128,8>', 'kernel_ms': kern_ms,
+            'traffic': N_WORLDS * (RESIDENT_DRAM_BYTES_PER_WORLD + RESIDENT_DRAM_BYTES_PER_WORLD_STEP * STEPS_EULER),
+            'kernel': 'resident_kernel<128,8>', 'kernel_ms': kern_ms,
             'flops_per_launch': flops_launch,
             'peak_source': 'measured in-bench (FFMA probe kernel, burst); MEASURED_PEAKS.json has no FP32 entry'
         },
@@ -321,13 +342,16 @@ def run_ours(args, rank, world_size):
     return out
 
 
-def measure_adjoint(dev, worlds=64, steps=256, ckpt=16, reps=3):
+def measure_adjoint(dev, worlds=64, steps=256, ckpt=16, reps=3, fp32_peak=None):
     """Differentiation workload: 64 worlds of 128x128 (the single-world model),
     256 steps with checkpoints every 16, MSE of the final state against a
     target made by the forward engine from the same inits at m=0.16, s=0.017;
     gradients with respect to the initial cells, m, s and the ring weights b
     (two rings, so dL/db is not identically zero).  Reports fwd+bwd
-    world-steps/s timed with CUDA events around forward + backward."""
+    world-steps/s timed with CUDA events around forward + backward, and its
+    FP32 roofline: per fwd + bwd world-step the forward step twice (the
+    checkpointed forward and the backward's recompute, without statistics)
+    plus one reverse step."""
     import torch
     from leniax_gb300 import grad as lgrad
     from leniax_gb300 import helpers, kernels
@@ -358,8 +382,13 @@ def measure_adjoint(dev, worlds=64, steps=256, ckpt=16, reps=3):
         if i > 0:
             times.append(e0.elapsed_time(e1) / 1e3)
     t = pystats.median(times)
+    fpws = 2 * flops_per_world_step(1, 1, P_CELLS, stats=False) + adjoint_flops_per_world_step(P_CELLS)
+    achieved = fpws * worlds * steps / t / 1e12
     return {
         'metric': 'fwd+bwd world-steps/s', 'value': worlds * steps / t, 'unit': 'world-steps/s',
+        'roofline': {'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s',
+                     'frac': achieved / fp32_peak if fp32_peak else None, 'flops_per_fwd_bwd_world_step': fpws,
+                     'note': f'{worlds} worlds take {worlds} of the SMs (one world per SM)'},
         'cell_updates_per_s': worlds * steps * P_CELLS / t, 'seconds': t,
         'config': f'{worlds} worlds x 128x128, {steps} steps, checkpoint every {ckpt}, grads wrt cells0, m, s, b',
         'loss': float(loss.detach()),
@@ -389,14 +418,16 @@ def _timed(fn, stream, flush, reps):
     return pystats.median(ts)
 
 
-def measure_multichannel(dev, worlds=256, size=256, C=3, per_channel=5, steps=512, reps=2):
+def measure_multichannel(dev, worlds=256, size=256, C=3, per_channel=5, steps=512, reps=2, fp32_peak=None):
     """Multi-channel model on the streamed engine: 256 worlds of 256x256,
     C=3 channels, K=15 kernels (5 per channel, seeded R in [10, 20], 1-3
     rings, m in [0.1, 0.4], s in [0.01, 0.05], target weights normalised per
     channel), dt=0.2, uniform[0,1) 64x64 central patches per channel, 512
     steps with leniax statistics and both stop sets.  Streamed case roofline:
-    HBM bytes of the compulsory traffic (state in + out, half spectrum in:
-    8*C*P + 8*K*(P/2+1) bytes per world-step) over the rollout time."""
+    HBM bytes of the compulsory traffic per Euler step -- every world's state
+    in and out (8 C P bytes per world) and each solution's half spectrum in
+    once (8 K (P/2+1) bytes; this batch is one solution) -- over the rollout
+    time; beside it the FP32 roofline of the algorithmic flops."""
     import torch
     from leniax_gb300 import helpers, kernels, runner, statistics, workloads
     R_world, T_mc = 20.0, 5.0
@@ -419,9 +450,12 @@ def measure_multichannel(dev, worlds=256, size=256, C=3, per_channel=5, steps=51
     ms = _timed(lambda: run(steps), torch.cuda.current_stream(dev), flush, reps)
     P = size * size
     cu = worlds * C * P * steps
-    bytes_ws = 8 * C * P + 8 * nk * (P // 2 + 1)
-    achieved = bytes_ws * worlds * steps / (ms / 1e3) / 1e9
+    n_sols = 1
+    bytes_step = 8 * C * P * worlds + 8 * nk * (P // 2 + 1) * n_sols
+    achieved = bytes_step * steps / (ms / 1e3) / 1e9
     peak = measured_peaks().get('hbm_gbs')
+    flops = flops_per_world_step(C, nk, P) * worlds * steps
+    tflops = flops / (ms / 1e3) / 1e12
     sd = out['r'][0]
     return {
         'workload': f'multichannel-{worlds}x{size}x{size}-c{C}k{nk}-{steps}steps', 'engine': 'streamed',
@@ -429,13 +463,16 @@ def measure_multichannel(dev, worlds=256, size=256, C=3, per_channel=5, steps=51
         'ms_per_euler_step': ms / steps, 'mean_N': float(sd['N'].float().mean()),
         'roofline': {'bound': 'hbm', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak if peak else None,
-                     'algorithmic_bytes_per_world_step': bytes_ws,
-                     'note': 'compulsory traffic over the whole step (4 kernels); peak = measured copy bandwidth'},
+                     'algorithmic_bytes_per_euler_step': bytes_step,
+                     'note': 'compulsory traffic over the whole step; peak = measured copy bandwidth'},
+        'roofline_fp32': {'bound': 'fp32', 'achieved': tflops, 'peak': fp32_peak, 'unit': 'TFLOP/s',
+                          'frac': tflops / fp32_peak if fp32_peak else None,
+                          'flops_per_world_step': flops_per_world_step(C, nk, P)},
         'l2': 'flushed between timed rollouts (256 MB write)',
     }
 
 
-def measure_uneven(dev, steps=256, reps=3):
+def measure_uneven(dev, steps=256, reps=3, fp32_peak=None):
     """Uneven search batch in one persistent launch, replayed from a CUDA
     graph: 4096 C=K=1 worlds (2048 of 64x64, 1229 of 128x128, 614 of
     256x256, 205 of 64x64x64), per-world R in [5, 26], m in [0.1, 0.35], s in
@@ -469,9 +506,13 @@ def measure_uneven(dev, steps=256, reps=3):
     ms_seq = _timed(seq, stream, flush, max(1, reps - 1))
     res = b.results()
     n_alive = sum(float(r['stats']['N_box'].sum()) for r in res) / sum(c.n for c in classes)
+    flops = sum(c.n * flops_per_world_step(1, 1, int(np.prod(c.world))) for c in classes) * steps
+    tflops = flops / (ms / 1e3) / 1e12
     return {
         'workload': 'uneven-4096-worlds-64sq-128sq-256sq-64cube-256steps', 'metric': METRIC,
         'value': b.cells_per_run / (ms / 1e3), 'unit': METRIC, 'ms_per_rollout': ms,
+        'roofline': {'bound': 'fp32', 'achieved': tflops, 'peak': fp32_peak, 'unit': 'TFLOP/s',
+                     'frac': tflops / fp32_peak if fp32_peak else None, 'flops_per_rollout': flops},
         'classes': [{'world': list(c.world), 'worlds': c.n} for c in classes],
         'settings': settings, 'autotune_seconds': tune_s, 'graph': True,
         'one_class_per_launch': {'value': b.cells_per_run / (ms_seq / 1e3), 'ms_per_rollout': ms_seq},

@@ -251,9 +251,12 @@ LGX_API int lgx_selftest_wait_timeout(int max_polls, int* status, void* stream);
  *
  * The engine's scratch is a fixed device array of LGX_NOALLOC_SCRATCH_BYTES
  * that every GPU loading this library holds until the process exits.  The
- * first call on a device resolves the array's device address with that device
- * current; make that first call before any stream capture.  The call itself
- * performs no allocation.  All calls on a device share the one array: calls
+ * first call on a device -- and the first call in any other CUDA context on
+ * it, e.g. after a device reset or from a non-primary context -- resolves the
+ * array's device address in that context; make that first call before any
+ * stream capture.  The call itself performs no allocation.  steps = 0 behaves
+ * as in lgx_run (initial cells copied to final_cells, stop counts 0) and uses
+ * no scratch.  All calls on a device share the one array: calls
  * whose GPU work overlaps (other streams, other host threads) race on it and
  * must be serialised by the caller.  Batches needing more scratch than the
  * array holds (lgx_noalloc_scratch_bytes) are rejected with LGX_ERR_WORKSPACE;

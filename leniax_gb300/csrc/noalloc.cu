@@ -29,7 +29,11 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[LGX_NOALLOC_SCR
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
+// Per device: the scratch address and the unique id of the CUDA context it was
+// resolved in.  A device reset, or a caller running in another (non-primary)
+// context, gives a new context id, and the address is resolved again there.
 void* g_scratch_ptr[kMaxDevices] = {nullptr};
+unsigned long long g_scratch_ctx[kMaxDevices] = {0};
 
 thread_local std::string g_na_err;
 
@@ -38,22 +42,55 @@ int na_fail(int code, const char* msg) {
   return code;
 }
 
-// Device address of the scratch array for the current device, resolved once per
-// device with that device current.  In host code g_noalloc_scratch names a
-// host-side shadow, never the device memory, so only this address is passed on.
+// Unique id of the current driver context (cuCtxGetCurrent + cuCtxGetId,
+// fetched through the runtime's driver entry points, so the library does not
+// link the driver library itself).  Returns false when it cannot be read.
+bool current_context_id(unsigned long long* id) {
+  typedef int (*GetCurrent)(void**);
+  typedef int (*GetId)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {  // under g_mu
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+    looked_up = true;
+  }
+  void* ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx) return false;
+  return get_id(ctx, id) == 0;
+}
+
+// Device address of the scratch array in the current device's current
+// context.  Resolved with that device current the first time a device (or a
+// new context on it) is seen; in host code g_noalloc_scratch names a host-side
+// shadow, never the device memory, so only this address is passed on.
 int scratch_for_current_device(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return na_fail(LGX_ERR_CUDA, "lgx_run_noalloc: no current CUDA device");
   std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
+  unsigned long long ctx = 0;
+  if (!current_context_id(&ctx) || !g_scratch_ptr[dev] || g_scratch_ctx[dev] != ctx) {
+    // first call on this device or in this context (cudaGetSymbolAddress also
+    // binds the runtime's context when no context was current yet)
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p) {
       g_na_err = std::string("lgx_run_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e);
       return LGX_ERR_CUDA;
     }
+    if (!current_context_id(&ctx))
+      return na_fail(LGX_ERR_CUDA, "lgx_run_noalloc: cannot identify the current CUDA context");
     g_scratch_ptr[dev] = p;
+    g_scratch_ctx[dev] = ctx;
   }
   *out = g_scratch_ptr[dev];
   return LGX_OK;
@@ -79,12 +116,24 @@ extern "C" LGX_API int lgx_run_noalloc(const lgx_plan* plan, const lgx_rollout* 
   if (!resident_supported(m))
     return na_fail(LGX_ERR_UNSUPPORTED,
                    "lgx_run_noalloc: resident models only (2D, C=1, K=1, square 32/64/128 worlds)");
-  if (j->n_sols < 1 || j->n_init < 1 || j->steps < 1)
-    return na_fail(LGX_ERR_INVALID, "lgx_run_noalloc: need n_sols >= 1, n_init >= 1, steps >= 1");
+  if (j->n_sols < 1 || j->n_init < 1 || j->steps < 0)
+    return na_fail(LGX_ERR_INVALID, "lgx_run_noalloc: need n_sols >= 1, n_init >= 1, steps >= 0");
   if (!j->cells0 || !j->k_half || !j->gf_params || !j->weights || !j->T)
     return na_fail(LGX_ERR_INVALID, "lgx_run_noalloc: null input tensor");
   if (!(j->stats_R > 0.f) || !(j->stats_T > 0.f))
     return na_fail(LGX_ERR_INVALID, "lgx_run_noalloc: stats_R and stats_T must be > 0");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (j->steps == 0) {  // as lgx_run: the initial cells come back, both stop counts are 0; no scratch used
+    const size_t bytes = (size_t)j->n_sols * j->n_init * m.C * m.cells * sizeof(float);
+    cudaError_t ce = cudaSuccess;
+    if (j->final_cells) ce = cudaMemcpyAsync(j->final_cells, j->cells0, bytes, cudaMemcpyDeviceToDevice, st);
+    if (ce == cudaSuccess && j->n_continue)
+      ce = cudaMemsetAsync(j->n_continue, 0, (size_t)j->n_sols * j->n_init * sizeof(float), st);
+    if (ce == cudaSuccess && j->n_box) ce = cudaMemsetAsync(j->n_box, 0, (size_t)j->n_sols * j->n_init * sizeof(float), st);
+    if (ce != cudaSuccess) return na_fail(LGX_ERR_CUDA, cudaGetErrorString(ce));
+    g_na_err.clear();
+    return LGX_OK;
+  }
   const size_t kp_bytes = al256((size_t)j->n_sols * m.H * resident_kpitch(m.H) * sizeof(float2));
   const size_t raw_bytes = (size_t)j->n_sols * j->steps * j->n_init * raw_stride(m.C) * sizeof(float);
   if (kp_bytes + raw_bytes > (size_t)LGX_NOALLOC_SCRATCH_BYTES) {
@@ -98,7 +147,6 @@ extern "C" LGX_API int lgx_run_noalloc(const lgx_plan* plan, const lgx_rollout* 
   void* base = nullptr;
   int rc = scratch_for_current_device(&base);
   if (rc != LGX_OK) return rc;
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   float2* kp = reinterpret_cast<float2*>(base);
   float* raw = reinterpret_cast<float*>(static_cast<char*>(base) + kp_bytes);
   // The array keeps the previous call's contents: clear the moments region so

@@ -204,11 +204,14 @@ GF_REGISTER = {
 # ---------------------------------------------------------------------------
 # Kernels -- leniax/kernels.py
 # ---------------------------------------------------------------------------
-def circle_kernel(R, k_params, kf_slug, kf_params, nb_dims=2, dtype=np.float32):
+def circle_kernel(R, k_params, kf_slug, kf_params, nb_dims=2, dtype=np.float32, normalize=True):
     """Radial ring kernel, kernels.py:176-212 (``circle_2d``), generalised to
     ``nb_dims`` axes (distance over all axes).  For ``nb_dims == 2`` it is the
     reference's ``circle_2d``; the D-dimensional form is this project's
-    extension (leniax builds only 2D kernels, kernels.py:192-197)."""
+    extension (leniax builds only 2D kernels, kernels.py:192-197).
+    ``normalize=False`` skips the division by the sum (kernels.py:207-208):
+    with a one-hot ``b`` it gives one ring of the kernel, so a test can form
+    the kernel as a differentiable function of the ring weights."""
     dtype = np.dtype(dtype).type
     r = k_params[0]
     bs = np.asarray(k_params[1], dtype=dtype)
@@ -222,8 +225,17 @@ def circle_kernel(R, k_params, kf_slug, kf_params, nb_dims=2, dtype=np.float32):
     kfp = np.asarray(kf_params, dtype=dtype)
     raw_kernel = KF_REGISTER[kf_slug](kfp, np.mod(B_dist, dtype(1)))
     kernel = (distances < 1) * raw_kernel * bs_mat
-    kernel = (kernel / kernel.sum()).astype(dtype)
-    return kernel[np.newaxis, ...]
+    if normalize:
+        kernel = kernel / kernel.sum()
+    return kernel.astype(dtype)[np.newaxis, ...]
+
+
+def world_kernel(R, k_params, kf_slug, kf_params, world_size, dtype=np.float64, normalize=True):
+    """The world-sized, fftshifted real kernel whose ``fftn`` is leniax's
+    spectrum: ``circle_kernel`` centred by ``_pad_kernel`` (kernels.py:93-101)
+    and shifted by ``fftshift`` (kernels.py:148).  ``[*world_size]``."""
+    k = circle_kernel(R, k_params, kf_slug, kf_params, len(world_size), dtype, normalize)
+    return np.fft.fftshift(_pad_kernel(k, world_size)[0])
 
 
 def _pad_kernel(k, world_size):

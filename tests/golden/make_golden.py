@@ -1,9 +1,9 @@
 """Generate the golden fixtures under tests/golden/ from leniax's own test fixtures.
 
-Run in a container where the leniax sources are mounted (default
-``/root/reference``)::
+Run where the leniax sources are available, passing the root of the leniax
+project (or setting ``LENIAX_SRC``)::
 
-    python tests/golden/make_golden.py [--ref /root/reference]
+    python tests/golden/make_golden.py --ref <leniax project root>
 
 It reads ``tests/fixtures/{orbium-test,orbium-scutium-test,aquarium-test}.yaml``
 (a small YAML subset parser: PyYAML is not installed) and the matching golden
@@ -128,8 +128,11 @@ def load_frame(path):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument('--ref', default='/root/reference')
+    ap.add_argument('--ref', default=os.environ.get('LENIAX_SRC'),
+                    help='root of the leniax project (default: $LENIAX_SRC)')
     args = ap.parse_args()
+    if not args.ref:
+        ap.error('pass --ref <leniax project root> or set LENIAX_SRC')
     fx = os.path.join(args.ref, 'tests', 'fixtures')
     for case, (yml, frame, decimal) in CASES.items():
         cfg = parse_yaml_subset(open(os.path.join(fx, yml)).read())

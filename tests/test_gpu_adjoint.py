@@ -7,6 +7,7 @@ import torch
 from leniax_gb300 import grad as lgrad
 from leniax_gb300 import helpers, kernels
 from oracle import lenia_grad_oracle as GO
+from oracle import lenia_oracle as O
 from tests.cases import bump_kernel_params, patch_init
 
 pytestmark = pytest.mark.gpu
@@ -146,9 +147,15 @@ def test_ring_weight_gradient_through_kernel_builder(cuda):
                         torch.tensor([T]), upd, steps, 4, 'ste')
     loss = ((fin - torch.from_numpy(target[None]).to(cuda))**2).mean()
     (gb, ) = torch.autograd.grad(loss, [b])
-    # float64 reference: the same kernel builder in float64 on the CPU, autograd end to end
+    # float64 reference built from the oracle: each ring of circle_2d
+    # (kernels.py:176-212) unnormalised and placed on the world (pad +
+    # fftshift); the kernel is sum_j b_j ring_j / sum_j b_j sum(ring_j), so
+    # autograd differentiates the normalisation too
+    rings = np.stack([O.world_kernel(R, [1.0, list(onehot)], 'gauss_bump', [1.0], [size, size], normalize=False)
+                      for onehot in ([1.0, 0.0], [0.0, 1.0])])
+    rings = torch.from_numpy(rings)
     b64 = torch.tensor([0.5, 1.0], dtype=torch.float64, requires_grad=True)
-    kr64 = lgrad.ring_kernel(R, 1.0, b64.float(), 'gauss_bump', [1.0], [size, size]).double()
+    kr64 = (b64[:, None, None] * rings).sum(0) / (b64 * rings.sum(dim=(1, 2))).sum()
     fin64 = GO.rollout(torch.from_numpy(cells.astype(np.float64)), kr64, m, s, 1.0, 1 / T, steps, clip='ste')
     l64 = ((fin64 - torch.from_numpy(target.astype(np.float64)))**2).mean()
     (gb64, ) = torch.autograd.grad(l64, [b64])

@@ -1,5 +1,6 @@
 """On-device ring-kernel construction vs leniax's host construction
-(get_kernels_and_mapping + circle_2d, kernels.py:66-212, restated in numpy)."""
+(get_kernels_and_mapping + circle_2d, kernels.py:66-212) as the oracle
+restates it in numpy."""
 import numpy as np
 import pytest
 import torch
@@ -39,10 +40,10 @@ def test_ring_kernels_match_host_construction(cuda, world, kf_slug, kf_params, b
 
 
 def _real_ref(world, R, r, b, kf_slug, kf_params):
-    """fftshifted world-size real kernel, float32, as leniax places it before its fftn."""
-    k = kernels.circle_nd(R, [r, list(b)], kf_slug, kf_params, len(world))[0]
-    pads = [((ws - ks) // 2, (ws - ks) // 2 + (ws - ks) % 2) for ws, ks in zip(world, k.shape)]
-    return np.fft.fftshift(np.pad(k, pads))
+    """fftshifted world-size real kernel, float32, as leniax places it before
+    its fftn: the oracle's circle_kernel, _pad_kernel and fftshift
+    (kernels.py:93-101,148,176-212)."""
+    return O.world_kernel(R, [r, list(b)], kf_slug, kf_params, world, dtype=np.float32)
 
 
 def _spectrum_ref(world, R, r, b, kf_slug, kf_params):

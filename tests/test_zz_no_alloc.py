@@ -27,54 +27,73 @@ def _bind(lib):
     lib.lgx_noalloc_last_error.restype = ctypes.c_char_p
 
 
-def _job(cells, kh, gf, w, T, steps, outs):
+def _job(cells, kh, gf, w, T, steps, outs, R):
     job = _lib.Rollout()
     job.n_sols, job.n_init, job.steps = cells.shape[0], cells.shape[1], steps
     job.cells0, job.k_half, job.gf_params, job.weights, job.T = (cells.data_ptr(), kh.data_ptr(), gf.data_ptr(),
                                                                   w.data_ptr(), T.data_ptr())
-    job.stats_R, job.stats_T = 13.0, 10.0
+    job.stats_R, job.stats_T = R, 10.0
     job.final_cells = outs['final'].data_ptr()
     job.stats = outs['stats'].data_ptr()
     job.n_continue = outs['N'].data_ptr()
     job.n_box = outs['N_box'].data_ptr()
     job.centroid = outs['centroid'].data_ptr()
+    if 'traj' in outs:
+        job.traj_cells, job.traj_field, job.traj_potential = (t.data_ptr() for t in outs['traj'])
     job.engine = _lib.ENGINES['resident']
     return job
 
 
-def _outs(cells, steps, dev):
+def _outs(cells, steps, dev, traj=False):
     Ns, Ni = cells.shape[:2]
-    return {
+    out = {
         'final': torch.empty_like(cells),
-        'stats': torch.full((Ns, steps, Ni, 1 + _lib.NSTAT_SCALAR), float('nan'), device=dev),
+        'stats': torch.full((Ns, max(steps, 1), Ni, 1 + _lib.NSTAT_SCALAR), float('nan'), device=dev),
         'N': torch.full((Ns, Ni), -1.0, device=dev),
         'N_box': torch.full((Ns, Ni), -1.0, device=dev),
-        'centroid': torch.full((Ns, steps, Ni, 2), float('nan'), device=dev),
+        'centroid': torch.full((Ns, max(steps, 1), Ni, 2), float('nan'), device=dev),
     }
+    if traj:
+        shape = (steps, Ns * Ni) + tuple(cells.shape[2:])
+        out['traj'] = tuple(torch.full(shape, float('nan'), device=dev) for _ in range(3))
+    return out
 
 
-def test_noalloc_rollout_matches_workspace_rollout_twice(cuda):
+def _model(size, dev):
+    R = {32: 6, 64: 10, 128: 13}[size]
+    # two solutions with their own kernel radius, growth parameters and T
+    specs = []
+    for sol, (m, s, r) in enumerate(((0.15, 0.015, 1.0), (0.2, 0.03, 0.8))):
+        kp = bump_kernel_params(m=m, s=s, r=r)
+        K, mp = kernels.get_kernels_and_mapping(kp, [size, size], 1, R, True, dev)
+        specs.append((K, mp))
+    upd = helpers.build_update_fn(specs[0][0].shape, specs[0][1])
+    kh = torch.stack([torch.view_as_real(K[..., :size // 2 + 1].contiguous()).reshape(1, 1, size, size // 2 + 1, 2)
+                      for K, _ in specs]).contiguous()
+    gf = torch.stack([mp.get_gf_params(dev) for _, mp in specs]).contiguous()
+    w = torch.stack([mp.get_kernels_weight_per_channel(dev) for _, mp in specs]).contiguous()
+    return upd, kh, gf, w, torch.tensor([10.0, 5.0], device=dev), R
+
+
+@pytest.mark.parametrize('size,traj', [(32, False), (64, False), (128, False), (64, True)])
+def test_noalloc_rollout_matches_workspace_rollout_twice(cuda, size, traj):
     dev = cuda
     lib = _lib.load()
     _bind(lib)
-    size, steps = 128, 48
-    K, mp = kernels.get_kernels_and_mapping(bump_kernel_params(), [size, size], 1, 13, True, dev)
-    upd = helpers.build_update_fn(K.shape, mp)
+    steps, n_sols, n_init = (24 if traj else 48), 2, 5
+    upd, kh, gf, w, T, R = _model(size, dev)
     plan = upd.model.plan.handle
-    kh = torch.view_as_real(K[..., :size // 2 + 1].contiguous()).reshape(1, 1, 1, size, size // 2 + 1, 2).contiguous()
     stream = torch.cuda.current_stream(dev).cuda_stream
     for call, seed in enumerate((3, 4)):
-        cells = torch.from_numpy(patch_init(6, size, 40, seed=seed, scale_range=(0.6, 1.0))[None]).to(dev)
-        gf = torch.tensor([[[0.15, 0.015]]], device=dev)
-        w = torch.ones((1, 1, 1), device=dev)
-        T = torch.tensor([10.0], device=dev)
-        assert 0 < lib.lgx_noalloc_scratch_bytes(plan, 1, 6, steps) <= 16 * 1024 * 1024
-        ref = _outs(cells, steps, dev)
-        ws = torch.empty(lib.lgx_run_workspace_bytes(plan, 1, 6, steps, _lib.ENGINES['resident']), dtype=torch.uint8,
-                         device=dev)
-        _lib.check(lib.lgx_run(plan, _job(cells, kh, gf, w, T, steps, ref), ws.data_ptr(), ws.numel(), stream))
-        got = _outs(cells, steps, dev)
-        rc = lib.lgx_run_noalloc(plan, _job(cells, kh, gf, w, T, steps, got), stream)
+        cells = torch.from_numpy(np.stack([patch_init(n_init, size, size // 3, seed=seed + 10 * s,
+                                                      scale_range=(0.6, 1.0)) for s in range(n_sols)])).to(dev)
+        assert 0 < lib.lgx_noalloc_scratch_bytes(plan, n_sols, n_init, steps) <= 16 * 1024 * 1024
+        ref = _outs(cells, steps, dev, traj)
+        ws = torch.empty(lib.lgx_run_workspace_bytes(plan, n_sols, n_init, steps, _lib.ENGINES['resident']),
+                         dtype=torch.uint8, device=dev)
+        _lib.check(lib.lgx_run(plan, _job(cells, kh, gf, w, T, steps, ref, R), ws.data_ptr(), ws.numel(), stream))
+        got = _outs(cells, steps, dev, traj)
+        rc = lib.lgx_run_noalloc(plan, _job(cells, kh, gf, w, T, steps, got, R), stream)
         assert rc == _lib.LGX_OK, lib.lgx_noalloc_last_error()
         torch.cuda.synchronize()
         # same kernels on the same inputs: the state tolerance of the parity tests (1e-5) holds with margin
@@ -82,6 +101,24 @@ def test_noalloc_rollout_matches_workspace_rollout_twice(cuda):
         assert torch.allclose(got['stats'], ref['stats'], rtol=1e-5, atol=1e-6, equal_nan=False), call
         assert torch.allclose(got['centroid'], ref['centroid'], rtol=1e-5, atol=1e-5), call
         assert torch.equal(got['N'], ref['N']) and torch.equal(got['N_box'], ref['N_box']), call
+        if traj:
+            for a, b in zip(got['traj'], ref['traj']):
+                assert (a - b).abs().max().item() <= 1e-5, call
+
+
+def test_noalloc_zero_steps_returns_the_initial_cells(cuda):
+    dev = cuda
+    lib = _lib.load()
+    _bind(lib)
+    upd, kh, gf, w, T, R = _model(64, dev)
+    cells = torch.from_numpy(np.stack([patch_init(3, 64, 20, seed=s) for s in range(2)])).to(dev)
+    got = _outs(cells, 0, dev)
+    rc = lib.lgx_run_noalloc(upd.model.plan.handle, _job(cells, kh, gf, w, T, 0, got, R),
+                             torch.cuda.current_stream(dev).cuda_stream)
+    assert rc == _lib.LGX_OK, lib.lgx_noalloc_last_error()
+    torch.cuda.synchronize()
+    assert torch.equal(got['final'], cells)
+    assert float(got['N'].abs().sum()) == 0.0 and float(got['N_box'].abs().sum()) == 0.0
 
 
 def test_noalloc_rejects_batches_beyond_the_fixed_scratch(cuda):
@@ -105,7 +142,7 @@ def test_noalloc_rejects_batches_beyond_the_fixed_scratch(cuda):
         'N_box': torch.empty(1, device=dev),
         'centroid': torch.empty(1, device=dev)
     }
-    job = _job(cells, kh, gf, w, T, steps, outs)
+    job = _job(cells, kh, gf, w, T, steps, outs, 13.0)
     rc = lib.lgx_run_noalloc(plan, job, torch.cuda.current_stream(dev).cuda_stream)
     assert rc == _lib.LGX_ERR_WORKSPACE
     assert b'scratch' in lib.lgx_noalloc_last_error()
