@@ -68,9 +68,19 @@ extern "C" {
 #define LGX_ENGINE_AUTO 0
 #define LGX_ENGINE_RESIDENT 1 /* one world per CTA slice, state in registers across steps */
 #define LGX_ENGINE_STREAMED 2 /* multi-pass, spectra through HBM/L2, any C/K             */
-#define LGX_ENGINE_PLAIN 3    /* one world per launch, one step per launch (reference)  */
+#define LGX_ENGINE_PLAIN 3    /* one world and one Euler step per launch (the reference
+                                 one-world-per-launch step): the fused one-kernel step of
+                                 the resident engine for its models, else the streamed
+                                 engine's kernel sequence                               */
 #define LGX_ENGINE_CTA 4      /* one world per CTA, persistent over a work queue: 3D
-                                 worlds of side 32 / 64 (C = K = 1); no trajectories   */
+                                 worlds of side 32 / 64 (C = K = 1)                     */
+#define LGX_ENGINE_PLAIN_STREAMED 5 /* one world and one step per launch through the streamed
+                                 engine's kernel sequence (row, column, row-inverse and
+                                 reduce kernels), for any model the streamed engine runs */
+#define LGX_ENGINE_ND 6       /* general N-D engine: any 2D / 3D world whose sides (2..512)
+                                 factor into 2, 3, 5 and 7 -- odd, non-square and 3D sides
+                                 such as 48^3 included -- with any C and K; mixed-radix line
+                                 FFT passes over full complex spectra in HBM              */
 
 /* number of scalar statistics besides the C channel masses */
 #define LGX_NSTAT_SCALAR 11
@@ -175,42 +185,54 @@ LGX_API int lgx_update(const lgx_plan* plan, int n, const float* state, const fl
 /* ---------------------------------------------------------------------------
  * Differentiation.  leniax differentiates its rollout with jax.grad through
  * the FFT (runner.py:363-448, make_pipeline_fn / make_gradient_fn); this
- * engine provides the adjoint by hand.  Models: 2D, C = 1, K = 1, square
- * worlds of 32..256.  The caller checkpoints states with lgx_run, recomputes
- * each segment's states s_t and potentials u_t (lgx_run trajectories), and
- * walks the segments backwards with lgx_adjoint. */
+ * engine provides the adjoint by hand, for every model lgx_run runs with the
+ * resident, streamed or N-D engines: 2D and 3D worlds, any number of channels
+ * and kernels, weighted mean or sum (core.py:202-242).  2D C = K = 1 square
+ * worlds of 32..256 take the specialised one-kernel adjoint, every other
+ * model the general N-D adjoint.  The caller checkpoints states with
+ * lgx_run, recomputes each segment's states s_t and potentials u_t (lgx_run
+ * trajectories), and walks the segments backwards with lgx_adjoint. */
 #define LGX_CLIP_GRAD_STE 0  /* clip gradient = 1 (leniax get_state v1, core.py:267-270) */
 #define LGX_CLIP_GRAD_MASK 1 /* clip gradient = 1 where 0 < s + dt f < 1, else 0 */
 
 typedef struct lgx_adjoint_job {
-  int n_sols, n_init, steps;    /* batch as in lgx_rollout; steps of this segment */
-  const float* k_half;          /* [Ns, 1, 1, H, W/2+1] complex64 kernel spectra       */
-  const float* gf_params;       /* [Ns, 1, 2]                                         */
-  const float* weights;         /* [Ns, 1, 1]                                         */
+  int n_sols, n_init, steps;    /* batch as in lgx_rollout; steps of this segment     */
+  const float* k_half;          /* [Ns, C, max_k, *world[:-1], W/2+1] complex64 spectra
+                                   (the lgx_rollout layout)                           */
+  const float* gf_params;       /* [Ns, K, 2]                                         */
+  const float* weights;         /* [Ns, C, K]                                         */
   const float* T;               /* [Ns]   dt = 1/T                                    */
-  const float* traj_cells;      /* [steps, Ns*Ni, 1, H, W] states entering each step  */
-  const float* traj_potential;  /* [steps, Ns*Ni, 1, H, W] potentials of each step    */
-  const float* lambda_in;       /* [Ns*Ni, 1, H, W] dL/d(state after the segment)     */
-  float* lambda_out;            /* [Ns*Ni, 1, H, W] dL/d(state before the segment); must
-                                   not alias lambda_in                                 */
-  float* kernel_grad_acc;       /* [Ns*Ni, H/2, W] complex64 accumulator, zeroed by the
+  const float* traj_cells;      /* [steps, Ns*Ni, C, *world] states entering each step */
+  const float* traj_potential;  /* [steps, Ns*Ni, K, *world] potentials of each step  */
+  const float* lambda_in;       /* [Ns*Ni, C, *world] dL/d(state after the segment)   */
+  float* lambda_out;            /* [Ns*Ni, C, *world] dL/d(state before the segment);
+                                   must not alias lambda_in                           */
+  float* kernel_grad_acc;       /* kernel-gradient accumulator of
+                                   lgx_adjoint_kernel_grad_acc_bytes bytes, zeroed by the
                                    caller before the first (last-in-time) segment     */
-  float* grad_gf;               /* [Ns, 1, 2] dL/d(m, s), accumulated (+=)            */
-  float* grad_weights;          /* [Ns, 1, 1] dL/dw, accumulated (+=)                 */
+  float* grad_gf;               /* [Ns, K, 2] dL/d(m, s) per kernel, accumulated (+=)  */
+  float* grad_weights;          /* [Ns, C, K] dL/d(kernels_weight_per_channel), every
+                                   entry (zero weights included), accumulated (+=)     */
   int clip_grad;                /* LGX_CLIP_GRAD_*                                    */
 } lgx_adjoint_job;
 
-/* Workspace bytes of lgx_adjoint for a batch. */
+/* Workspace bytes of lgx_adjoint (and lgx_adjoint_kernel_grad) for a batch;
+ * 0 when the model has no adjoint. */
 LGX_API size_t lgx_adjoint_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init);
+
+/* Bytes of the kernel-gradient accumulator (lgx_adjoint_job.kernel_grad_acc)
+ * for a batch; 0 when the model has no adjoint. */
+LGX_API size_t lgx_adjoint_kernel_grad_acc_bytes(const lgx_plan* plan, int n_sols, int n_init);
 
 /* Reverse one segment of a rollout (see above). */
 LGX_API int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* job, void* workspace, size_t workspace_bytes,
                         void* stream);
 
-/* dL/d(real kernel) [Ns, H, W] from the accumulator after the last segment:
- * the gradient with respect to the world-sized, fftshifted real kernel whose
- * fftn is the spectrum (kernels.py:145-149); chain it to ring weights b etc.
- * on the caller side.  Workspace: lgx_adjoint_workspace_bytes. */
+/* dL/d(real kernel) [Ns, K, *world] from the accumulator after the last
+ * segment: the gradient with respect to each kernel's world-sized, fftshifted
+ * real kernel whose fftn is its spectrum (kernels.py:145-149), summed over the
+ * inits of a solution; chain it to ring weights b etc. on the caller side.
+ * Workspace: lgx_adjoint_workspace_bytes. */
 LGX_API int lgx_adjoint_kernel_grad(const lgx_plan* plan, int n_sols, int n_init, const float* kernel_grad_acc,
                                     float* grad_kernel, void* workspace, size_t workspace_bytes, void* stream);
 
@@ -220,6 +242,13 @@ LGX_API int lgx_adjoint_kernel_grad(const lgx_plan* plan, int n_sols, int n_init
  * planes * H * W * 4 bytes. */
 LGX_API int lgx_kernel_spectrum(int H, int W, int planes, const float* k_real, float* k_half, void* workspace,
                                 size_t workspace_bytes, void* stream);
+
+/* The same for any world of the N-D engine: fftn of `planes` real planes
+ * [planes, *world] written as Hermitian halves [planes, *world[:-1], W/2+1]
+ * complex64.  world[] holds nb_dims (2 or 3) sides, outermost first. */
+LGX_API size_t lgx_kernel_spectrum_nd_workspace_bytes(int nb_dims, const int* world, int planes);
+LGX_API int lgx_kernel_spectrum_nd(int nb_dims, const int* world, int planes, const float* k_real, float* k_half,
+                                   void* workspace, size_t workspace_bytes, void* stream);
 
 /* Measurement helper (no counterpart in the reference): launch a pure-FMA
  * kernel of `blocks` x 256 threads and return the number of FP32 flops it

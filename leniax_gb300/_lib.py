@@ -29,14 +29,15 @@ GF_IDS = {
     'identity': 6,
 }
 STATE_IDS = {'v1': 0, 'v2': 1, 'simple': 2}
-ENGINES = {'auto': 0, 'resident': 1, 'streamed': 2, 'plain': 3, 'cta': 4}
+ENGINES = {'auto': 0, 'resident': 1, 'streamed': 2, 'plain': 3, 'cta': 4, 'plain_streamed': 5, 'nd': 6}
 NSTAT_SCALAR = 11
 
 EXPORTED = (
     'lgx_version', 'lgx_last_error', 'lgx_plan_create', 'lgx_plan_destroy', 'lgx_select_engine',
     'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update', 'lgx_fp32_probe',
     'lgx_batch_workspace_bytes', 'lgx_batch_run', 'lgx_workspace_status', 'lgx_ring_kernels_workspace_bytes',
-    'lgx_ring_kernels', 'lgx_selftest_wait_timeout'
+    'lgx_ring_kernels', 'lgx_selftest_wait_timeout', 'lgx_adjoint_kernel_grad_acc_bytes', 'lgx_kernel_spectrum_nd',
+    'lgx_kernel_spectrum_nd_workspace_bytes'
 )
 
 

@@ -64,6 +64,7 @@ class Model:
         self.C = nb_channels
         self.K = len(cin)
         self.max_k = max_k
+        self.cin, self.slot = list(cin), list(slot)  # spectrum position [c_in, slot] of each true kernel
         self.gf_slugs = gfs
         self.state_slug = get_state_fn_slug
         self.average = bool(average_weight)

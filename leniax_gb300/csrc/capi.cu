@@ -62,8 +62,6 @@ struct Carve {
   bool fits() const { return off <= cap; }
 };
 
-bool is_pow2(int x) { return x > 0 && (x & (x - 1)) == 0; }
-
 // 3D worlds of side 32 / 64 with one channel and one kernel: one world per CTA
 // (the plane-fused items of the mixed kernel).
 bool cta_supported(const Model& m) {
@@ -73,12 +71,16 @@ bool cta_supported(const Model& m) {
 int select_engine(const Model& m, int requested) {
   if (requested == LGX_ENGINE_RESIDENT) return resident_supported(m) ? LGX_ENGINE_RESIDENT : -1;
   if (requested == LGX_ENGINE_STREAMED) return streamed_supported(m) ? LGX_ENGINE_STREAMED : -1;
-  if (requested == LGX_ENGINE_PLAIN) return streamed_supported(m) ? LGX_ENGINE_PLAIN : -1;
+  if (requested == LGX_ENGINE_PLAIN)
+    return resident_supported(m) ? LGX_ENGINE_PLAIN : (streamed_supported(m) ? LGX_ENGINE_PLAIN_STREAMED : -1);
+  if (requested == LGX_ENGINE_PLAIN_STREAMED) return streamed_supported(m) ? LGX_ENGINE_PLAIN_STREAMED : -1;
   if (requested == LGX_ENGINE_CTA) return cta_supported(m) ? LGX_ENGINE_CTA : -1;
+  if (requested == LGX_ENGINE_ND) return nd_supported(m) ? LGX_ENGINE_ND : -1;
   if (requested != LGX_ENGINE_AUTO) return -1;
   if (resident_supported(m)) return LGX_ENGINE_RESIDENT;
   if (streamed_supported(m)) return LGX_ENGINE_STREAMED;
   if (cta_supported(m)) return LGX_ENGINE_CTA;
+  if (nd_supported(m)) return LGX_ENGINE_ND;
   return -1;
 }
 
@@ -128,12 +130,46 @@ CtaLayout cta_layout(const Model& m, int n_sols, int n_init, int steps) {
   return L;
 }
 
+// One world and one Euler step per launch through the resident kernel: the
+// resident layout plus a state ping-pong and the carried shifts.
+size_t plain_ws(const Model& m, int n_sols, int n_init, int steps) {
+  const size_t nw = (size_t)n_sols * n_init;
+  return resident_ws(m, n_sols, n_init, steps) + 2 * al256(nw * m.C * m.cells * sizeof(float)) +
+         al256(nw * 2 * sizeof(int));
+}
+
 size_t streamed_ws(const Model& m, int n_sols, int n_init, int steps, bool with_raw) {
   const int nw = n_sols * n_init;
   size_t b = kStatusBytes + streamed_workspace_bytes(m, nw, n_sols);
   b += 2 * al256((size_t)nw * m.C * m.cells * sizeof(float));  // state ping-pong
   if (with_raw) b += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
   return b;
+}
+
+// General N-D engine: status, prepared spectra, raw moments, state ping-pong,
+// carried shifts, the step's own buffers.
+struct NdLayout {
+  size_t kf, raw, sa, sb, shift, step, end;
+};
+
+NdLayout nd_layout(const Model& m, int n_sols, int n_init, int steps) {
+  NdLayout L;
+  const size_t nw = (size_t)n_sols * n_init;
+  size_t off = kStatusBytes;
+  L.kf = off;
+  off += nd_prepared_bytes(m, n_sols);
+  L.raw = off;
+  off += al256((size_t)n_sols * std::max(steps, 1) * n_init * raw_stride(m.C) * sizeof(float));
+  L.sa = off;
+  off += al256(nw * m.C * m.cells * sizeof(float));
+  L.sb = off;
+  off += al256(nw * m.C * m.cells * sizeof(float));
+  L.shift = off;
+  off += al256(nw * 3 * sizeof(int));
+  L.step = off;
+  off += nd_step_workspace_bytes(m, (int)nw);
+  L.end = off;
+  return L;
 }
 
 struct StreamedBufs {
@@ -186,18 +222,12 @@ int lgx_plan_create(const lgx_model_desc* d, lgx_plan** out) {
   std::memset(&m, 0, sizeof(m));
   m.nb_dims = d->nb_dims;
   for (int i = 0; i < d->nb_dims; ++i) {
-    const bool generic = d->nb_dims == 2 && generic_size(d->world[i]);  // 2D: even sides of 2, 3, 5, 7
-    if ((!is_pow2(d->world[i]) || d->world[i] < 8) && !generic)
+    if (!nd_side_ok(d->world[i]))
       return fail(LGX_ERR_UNSUPPORTED,
-                  "world axis %d has size %d: power-of-two sizes >= 8 (2D also even sides of factors 2, 3, 5, 7 "
-                  "up to 512)",
-                  i, d->world[i]);
+                  "world axis %d has size %d: sides from 2 to %d whose prime factors are 2, 3, 5 and 7", i,
+                  d->world[i], 512);
     m.world[i] = d->world[i];
   }
-  for (int i = 0; i < d->nb_dims; ++i)  // the mixed-radix step runs square worlds only
-    if (!is_pow2(d->world[i]) && d->world[0] != d->world[d->nb_dims - 1])
-      return fail(LGX_ERR_UNSUPPORTED, "world %d x %d: sides that are not powers of two need a square world",
-                  d->world[0], d->world[d->nb_dims - 1]);
   m.C = d->nb_channels;
   m.K = d->nb_kernels;
   m.max_k = d->max_k;
@@ -246,7 +276,10 @@ size_t lgx_run_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init, int
   if (!plan || n_sols < 1 || n_init < 1 || steps < 0) return 0;
   const int e = select_engine(plan->m, engine);
   if (e == LGX_ENGINE_RESIDENT) return resident_ws(plan->m, n_sols, n_init, steps);
-  if (e == LGX_ENGINE_STREAMED || e == LGX_ENGINE_PLAIN) return streamed_ws(plan->m, n_sols, n_init, steps, true);
+  if (e == LGX_ENGINE_STREAMED || e == LGX_ENGINE_PLAIN_STREAMED)
+    return streamed_ws(plan->m, n_sols, n_init, steps, true);
+  if (e == LGX_ENGINE_PLAIN) return plain_ws(plan->m, n_sols, n_init, steps);
+  if (e == LGX_ENGINE_ND) return nd_layout(plan->m, n_sols, n_init, steps).end;
   if (e == LGX_ENGINE_CTA) return cta_layout(plan->m, n_sols, n_init, steps).end;
   return 0;
 }
@@ -312,6 +345,111 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     ce = launch_big_rollout(m.nb_dims, m.H, b, m.gf[0], L.grid, base + L.setup, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "one-world-per-CTA rollout");
     if (j->main_events[1]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[1]), st);
+  } else if (e == LGX_ENGINE_ND) {
+    const NdLayout L = nd_layout(m, j->n_sols, j->n_init, j->steps);
+    char* base = static_cast<char*>(ws);
+    float2* kf = reinterpret_cast<float2*>(base + L.kf);
+    raw = reinterpret_cast<float*>(base + L.raw);
+    float* sa = reinterpret_cast<float*>(base + L.sa);
+    float* sb = reinterpret_cast<float*>(base + L.sb);
+    int* shift = reinterpret_cast<int*>(base + L.shift);
+    ce = launch_nd_prepare(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kf, st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(shift, 0, (size_t)nw * 3 * sizeof(int), st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    const long raws = raw_stride(m.C);
+    const float* cur = j->cells0;
+    if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
+    for (int s = 0; s < j->steps; ++s) {
+      float* out = (s == j->steps - 1 && j->final_cells) ? j->final_cells : ((s & 1) ? sb : sa);
+      if (j->traj_cells) {
+        ce = cudaMemcpyAsync(j->traj_cells + (size_t)s * nw * plane, cur, (size_t)nw * plane * sizeof(float),
+                             cudaMemcpyDeviceToDevice, st);
+        if (ce != cudaSuccess) return cuda_fail(ce, "trajectory copy");
+      }
+      NdStep ns;
+      ns.m = &m;
+      ns.n_worlds = nw;
+      ns.n_init = j->n_init;
+      ns.state = cur;
+      ns.state_out = out;
+      ns.kf = kf;
+      ns.kf_sol_stride = (long)m.C * m.max_k * m.cells;
+      ns.gf = j->gf_params;
+      ns.gf_sol_stride = 2L * m.K;
+      ns.w = j->weights;
+      ns.w_sol_stride = (long)m.C * m.K;
+      ns.dt = j->T;
+      ns.dt_mode = 2;
+      ns.field_out = j->traj_field ? j->traj_field + (size_t)s * nw * plane : nullptr;
+      ns.pot_out = j->traj_potential ? j->traj_potential + (size_t)s * nw * m.K * m.cells : nullptr;
+      ns.raw = raw + (size_t)s * j->n_init * raws;
+      ns.raw_world_stride = raws;
+      ns.raw_sol_stride = (long)j->steps * j->n_init * raws;
+      ns.shift = shift;
+      ns.ws = base + L.step;
+      ce = launch_nd_step(ns, st);
+      if (ce != cudaSuccess) return cuda_fail(ce, "N-D step");
+      cur = out;
+    }
+    if (j->main_events[1]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[1]), st);
+    if (j->final_cells && cur != j->final_cells) {
+      ce = cudaMemcpyAsync(j->final_cells, cur, (size_t)nw * plane * sizeof(float), cudaMemcpyDeviceToDevice, st);
+      if (ce != cudaSuccess) return cuda_fail(ce, "final copy");
+    }
+  } else if (e == LGX_ENGINE_PLAIN) {
+    // the reference one-world-per-launch step: the resident kernel launched for
+    // one world and one Euler step at a time, the carried shift chained
+    // through global memory between launches
+    Carve cv(ws, ws_bytes);
+    cv.take<int>(kStatusBytes / sizeof(int));
+    float2* kp = cv.take<float2>((size_t)j->n_sols * m.H * resident_kpitch(m.H));
+    raw = cv.take<float>((size_t)j->n_sols * j->steps * j->n_init * raw_stride(m.C));
+    float* sa = cv.take<float>((size_t)nw * plane);
+    float* sb = cv.take<float>((size_t)nw * plane);
+    int* shift = cv.take<int>((size_t)nw * 2);
+    if (!cv.fits()) return fail(LGX_ERR_WORKSPACE, "lgx_run: internal workspace layout exceeds its size query");
+    ce = launch_prepare_resident_spectrum(m.H, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kp, st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(shift, 0, (size_t)nw * 2 * sizeof(int), st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    const long kps = (long)m.H * resident_kpitch(m.H);
+    const int raws = raw_stride(m.C);
+    const float* cur = j->cells0;
+    if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
+    for (int s = 0; s < j->steps; ++s) {
+      float* out = (s == j->steps - 1 && j->final_cells) ? j->final_cells : ((s & 1) ? sb : sa);
+      for (int wdx = 0; wdx < nw; ++wdx) {
+        const int sol = wdx / j->n_init, init = wdx % j->n_init;
+        ResidentArgs a;
+        std::memset(&a, 0, sizeof(a));
+        a.n_worlds = 1;
+        a.n_init = 1;
+        a.steps = 1;
+        a.gf_id = m.gf[0];
+        a.state_fn = m.state_fn;
+        a.mean = m.mean;
+        a.cells0 = cur + (size_t)wdx * plane;
+        a.kp = kp + sol * kps;
+        a.gf = j->gf_params + 2 * sol;
+        a.w = j->weights + sol;
+        a.T = j->T + sol;
+        a.final_cells = out + (size_t)wdx * plane;
+        a.raw = raw + (((size_t)sol * j->steps + s) * j->n_init + init) * raws;
+        const size_t tr = ((size_t)s * nw + wdx) * plane;
+        a.traj_cells = j->traj_cells ? j->traj_cells + tr : nullptr;
+        a.traj_field = j->traj_field ? j->traj_field + tr : nullptr;
+        a.traj_pot = j->traj_potential ? j->traj_potential + tr : nullptr;
+        a.shift_in = shift + 2 * wdx;
+        a.shift_out = shift + 2 * wdx;
+        ce = launch_resident(m.H, a, 1, st);
+        if (ce != cudaSuccess) return cuda_fail(ce, "plain step");
+      }
+      cur = out;
+    }
+    if (j->main_events[1]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[1]), st);
+    if (j->final_cells && cur != j->final_cells) {
+      ce = cudaMemcpyAsync(j->final_cells, cur, (size_t)nw * plane * sizeof(float), cudaMemcpyDeviceToDevice, st);
+      if (ce != cudaSuccess) return cuda_fail(ce, "final copy");
+    }
   } else if (e == LGX_ENGINE_RESIDENT) {
     Carve cv(ws, ws_bytes);
     cv.take<int>(kStatusBytes / sizeof(int));
@@ -355,7 +493,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     if (ce != cudaSuccess) return cuda_fail(ce, "memset");
     const long kp_sol = (long)m.C * m.max_k * m.H * (m.W / 2 + 2);
     const long raws = raw_stride(m.C);
-    const bool plain = (e == LGX_ENGINE_PLAIN);
+    const bool plain = (e == LGX_ENGINE_PLAIN_STREAMED);
     const float* cur = j->cells0;
     if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
     for (int s = 0; s < j->steps; ++s) {
@@ -457,6 +595,7 @@ size_t lgx_update_workspace_bytes(const lgx_plan* plan, int n) {
   // included) and a one-step one-world-per-CTA rollout for 3D models
   if (streamed_supported(m)) return streamed_ws(m, 1, n, 1, false);
   if (cta_supported(m)) return cta_layout(m, 1, n, 1).end;
+  if (nd_supported(m)) return nd_layout(m, 1, n, 1).end;
   return 0;
 }
 
@@ -505,6 +644,42 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
     b.traj_pot = potential_out;
     ce = launch_big_rollout(m.nb_dims, m.H, b, m.gf[0], L.grid, base + L.setup, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "3D update");
+    g_err.clear();
+    return LGX_OK;
+  }
+  if (!streamed_supported(m) && nd_supported(m)) {
+    // one step of the general N-D engine, scalar or per-world dt
+    const NdLayout L = nd_layout(m, 1, n, 1);
+    char* base = static_cast<char*>(ws);
+    float2* kf = reinterpret_cast<float2*>(base + L.kf);
+    int* shift = reinterpret_cast<int*>(base + L.shift);
+    ce = cudaMemsetAsync(ws, 0, sizeof(int), st);
+    if (ce == cudaSuccess) ce = launch_nd_prepare(m, 1, reinterpret_cast<const float2*>(k_half), kf, st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(shift, 0, (size_t)n * 3 * sizeof(int), st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
+    NdStep ns;
+    ns.m = &m;
+    ns.n_worlds = n;
+    ns.n_init = n;
+    ns.state = state;
+    ns.state_out = state_out;
+    ns.kf = kf;
+    ns.kf_sol_stride = 0;
+    ns.gf = gf_params;
+    ns.gf_sol_stride = 0;
+    ns.w = weights;
+    ns.w_sol_stride = 0;
+    ns.dt = dt;
+    ns.dt_mode = dt_per_world ? 1 : 0;
+    ns.field_out = field_out;
+    ns.pot_out = potential_out;
+    ns.raw = nullptr;
+    ns.raw_world_stride = 0;
+    ns.raw_sol_stride = 0;
+    ns.shift = shift;
+    ns.ws = base + L.step;
+    ce = launch_nd_step(ns, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "N-D update");
     g_err.clear();
     return LGX_OK;
   }
@@ -587,15 +762,25 @@ size_t adjoint_ws(const Model& m, int n_sols, int n_init) {
 extern "C" {
 
 size_t lgx_adjoint_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init) {
-  if (!plan || n_sols < 1 || n_init < 1 || !adjoint_supported(plan->m)) return 0;
-  return adjoint_ws(plan->m, n_sols, n_init);
+  if (!plan || n_sols < 1 || n_init < 1) return 0;
+  if (adjoint_supported(plan->m)) return adjoint_ws(plan->m, n_sols, n_init);
+  if (nd_supported(plan->m)) return nd_adjoint_workspace_bytes(plan->m, n_sols, n_init);
+  return 0;
+}
+
+size_t lgx_adjoint_kernel_grad_acc_bytes(const lgx_plan* plan, int n_sols, int n_init) {
+  if (!plan || n_sols < 1 || n_init < 1) return 0;
+  const Model& m = plan->m;
+  if (adjoint_supported(m)) return (size_t)n_sols * n_init * (m.H / 2) * m.W * sizeof(float2);
+  if (nd_supported(m)) return nd_kernel_grad_acc_bytes(m, n_sols, n_init);
+  return 0;
 }
 
 int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t ws_bytes, void* stream) {
   if (!plan || !j) return fail(LGX_ERR_INVALID, "lgx_adjoint: null plan or job");
   const Model& m = plan->m;
-  if (!adjoint_supported(m))
-    return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint: 2D, C=1, K=1, square 32..256 worlds only");
+  if (!adjoint_supported(m) && !nd_supported(m))
+    return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint: no adjoint for this model");
   if (j->n_sols < 1 || j->n_init < 1 || j->steps < 1) return fail(LGX_ERR_INVALID, "lgx_adjoint: bad batch");
   if (!j->k_half || !j->gf_params || !j->weights || !j->T || !j->traj_cells || !j->traj_potential ||
       !j->lambda_in || !j->lambda_out || !j->kernel_grad_acc || !j->grad_gf || !j->grad_weights)
@@ -603,9 +788,32 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   if (j->lambda_in == j->lambda_out) return fail(LGX_ERR_INVALID, "lgx_adjoint: lambda_out aliases lambda_in");
   if (j->clip_grad != LGX_CLIP_GRAD_STE && j->clip_grad != LGX_CLIP_GRAD_MASK)
     return fail(LGX_ERR_INVALID, "lgx_adjoint: unknown clip_grad %d", j->clip_grad);
-  const size_t need = adjoint_ws(m, j->n_sols, j->n_init);
+  const size_t need = lgx_adjoint_workspace_bytes(plan, j->n_sols, j->n_init);
   if (!ws || ws_bytes < need) return fail(LGX_ERR_WORKSPACE, "lgx_adjoint: workspace %zu < %zu bytes", ws_bytes, need);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (!adjoint_supported(m)) {
+    // the general N-D adjoint: any channels and kernels, 2D and 3D worlds
+    NdAdjoint a;
+    a.n_sols = j->n_sols;
+    a.n_init = j->n_init;
+    a.steps = j->steps;
+    a.clip_mask = j->clip_grad == LGX_CLIP_GRAD_MASK;
+    a.k_half = reinterpret_cast<const float2*>(j->k_half);
+    a.gf_params = j->gf_params;
+    a.weights = j->weights;
+    a.T = j->T;
+    a.traj_cells = j->traj_cells;
+    a.traj_potential = j->traj_potential;
+    a.lambda_in = j->lambda_in;
+    a.lambda_out = j->lambda_out;
+    a.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
+    a.grad_gf = j->grad_gf;
+    a.grad_weights = j->grad_weights;
+    cudaError_t ce = launch_nd_adjoint(m, a, ws, st);
+    if (ce != cudaSuccess) return cuda_fail(ce, "N-D adjoint segment");
+    g_err.clear();
+    return LGX_OK;
+  }
   const size_t nw = (size_t)j->n_sols * j->n_init, cells = (size_t)m.H * m.W;
   Carve cv(ws, ws_bytes);
   AdjointSegment a;
@@ -678,15 +886,45 @@ int lgx_adjoint_kernel_grad(const lgx_plan* plan, int n_sols, int n_init, const 
                             void* ws, size_t ws_bytes, void* stream) {
   if (!plan || !acc || !grad_kernel) return fail(LGX_ERR_INVALID, "lgx_adjoint_kernel_grad: null argument");
   const Model& m = plan->m;
-  if (!adjoint_supported(m)) return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint_kernel_grad: unsupported model");
+  if (!adjoint_supported(m) && !nd_supported(m))
+    return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint_kernel_grad: unsupported model");
   if (n_sols < 1 || n_init < 1) return fail(LGX_ERR_INVALID, "lgx_adjoint_kernel_grad: bad batch");
-  const size_t need = adjoint_ws(m, n_sols, n_init);
+  const size_t need = lgx_adjoint_workspace_bytes(plan, n_sols, n_init);
   if (!ws || ws_bytes < need)
     return fail(LGX_ERR_WORKSPACE, "lgx_adjoint_kernel_grad: workspace %zu < %zu bytes", ws_bytes, need);
+  if (!adjoint_supported(m)) {
+    cudaError_t ce = launch_nd_kernel_grad(m, n_sols, n_init, reinterpret_cast<const float2*>(acc), grad_kernel, ws,
+                                           static_cast<cudaStream_t>(stream));
+    if (ce != cudaSuccess) return cuda_fail(ce, "kernel gradient");
+    g_err.clear();
+    return LGX_OK;
+  }
   float2* prod = reinterpret_cast<float2*>(ws);
   cudaError_t ce = launch_gk_finish(m.H, n_sols, n_init, reinterpret_cast<const float2*>(acc), prod, grad_kernel,
                                     static_cast<cudaStream_t>(stream));
   if (ce != cudaSuccess) return cuda_fail(ce, "kernel gradient");
+  g_err.clear();
+  return LGX_OK;
+}
+
+size_t lgx_kernel_spectrum_nd_workspace_bytes(int nb_dims, const int* world, int planes) {
+  if ((nb_dims != 2 && nb_dims != 3) || !world || planes < 1) return 0;
+  for (int i = 0; i < nb_dims; ++i)
+    if (!nd_side_ok(world[i])) return 0;
+  return nd_spectrum_workspace_bytes(nb_dims, world, planes);
+}
+
+int lgx_kernel_spectrum_nd(int nb_dims, const int* world, int planes, const float* k_real, float* k_half, void* ws,
+                           size_t ws_bytes, void* stream) {
+  if (!k_real || !k_half || !world || planes < 1) return fail(LGX_ERR_INVALID, "lgx_kernel_spectrum_nd: bad argument");
+  const size_t need = lgx_kernel_spectrum_nd_workspace_bytes(nb_dims, world, planes);
+  if (need == 0)
+    return fail(LGX_ERR_UNSUPPORTED, "lgx_kernel_spectrum_nd: 2D / 3D worlds with sides of factors 2, 3, 5, 7 only");
+  if (!ws || ws_bytes < need)
+    return fail(LGX_ERR_WORKSPACE, "lgx_kernel_spectrum_nd: workspace %zu < %zu", ws_bytes, need);
+  cudaError_t ce = launch_nd_spectrum(nb_dims, world, planes, k_real, reinterpret_cast<float2*>(k_half), ws,
+                                      static_cast<cudaStream_t>(stream));
+  if (ce != cudaSuccess) return cuda_fail(ce, "kernel spectrum");
   g_err.clear();
   return LGX_OK;
 }

@@ -51,6 +51,11 @@ struct ResidentArgs {
   float* traj_field;
   float* traj_pot;
   int* status;          // device error word (0 = ok)
+  // carried torus shift (statistics.py:117-124) across launches, [n_worlds, 2]
+  // (y, x), or null: read before the first step, written after the last.  The
+  // one-world-per-launch engine chains single-step launches through it.
+  const int* shift_in;
+  int* shift_out;
 };
 cudaError_t launch_resident(int N, const ResidentArgs& a, int grid, cudaStream_t st);
 int resident_max_grid(int N);
@@ -170,6 +175,63 @@ cudaError_t launch_prepare_generic_spectrum(const Model& m, int n_sols, const fl
                                             cudaStream_t st);
 cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const float2* k_half, float2* kp,
                                              cudaStream_t st);
+
+// ---------------------------------------------------------------- general N-D engine
+// Any 2D / 3D torus whose sides factor into 2, 3, 5, 7 (2..512), any C and K:
+// mixed-radix line passes over full complex spectra in HBM (nd.cu).
+bool nd_side_ok(int n);
+bool nd_supported(const Model& m);
+int nd_blocks_per_world(const Model& m);
+// Prepared spectra [Ns, C, max_k, cells] complex: the Hermitian half
+// [Ns, C, max_k, D, H, W/2+1] extended to the full spectrum, scaled by 1/cells.
+size_t nd_prepared_bytes(const Model& m, int n_sols);
+cudaError_t launch_nd_prepare(const Model& m, int n_sols, const float2* k_half, float2* kf, cudaStream_t st);
+struct NdStep {
+  const Model* m;
+  int n_worlds, n_init;
+  const float* state;   // [n_worlds, C, cells]
+  float* state_out;     // [n_worlds, C, cells]
+  const float2* kf;     // prepared spectra per solution
+  long kf_sol_stride;   // float2 elements between solutions (0: shared)
+  const float* gf;      // [Ns, K, 2]
+  long gf_sol_stride;
+  const float* w;       // [Ns, C, K]
+  long w_sol_stride;
+  const float* dt;
+  int dt_mode;          // 0: dt[0]; 1: dt[world]; 2: 1 / T[sol]
+  float* field_out;     // [n_worlds, C, cells] or null
+  float* pot_out;       // [n_worlds, K, cells] or null
+  float* raw;           // raw moments of this step, or null
+  long raw_world_stride, raw_sol_stride;
+  int* shift;           // [n_worlds, 3] carried torus shift (read, then advanced)
+  void* ws;             // nd_step_workspace_bytes
+};
+size_t nd_step_workspace_bytes(const Model& m, int n_worlds);
+cudaError_t launch_nd_step(const NdStep& s, cudaStream_t st);
+struct NdAdjoint {
+  int n_sols, n_init, steps, clip_mask;
+  const float2* k_half;         // [Ns, C, max_k, D, H, W/2+1]
+  const float* gf_params;       // [Ns, K, 2]
+  const float* weights;         // [Ns, C, K]
+  const float* T;               // [Ns]
+  const float* traj_cells;      // [steps, nw, C, cells]
+  const float* traj_potential;  // [steps, nw, K, cells]
+  const float* lambda_in;       // [nw, C, cells]
+  float* lambda_out;            // [nw, C, cells]
+  float2* gk;                   // [nw, K, cells] kernel-gradient spectra (+=)
+  float* grad_gf;               // [Ns, K, 2] (+=)
+  float* grad_weights;          // [Ns, C, K] (+=)
+};
+size_t nd_adjoint_workspace_bytes(const Model& m, int n_sols, int n_init);
+size_t nd_kernel_grad_acc_bytes(const Model& m, int n_sols, int n_init);
+cudaError_t launch_nd_adjoint(const Model& m, const NdAdjoint& j, void* ws, cudaStream_t st);
+size_t nd_kernel_grad_workspace_bytes(const Model& m, int n_sols);
+// dL/d(world-sized real kernel) [Ns, K, cells] from the accumulated spectra.
+cudaError_t launch_nd_kernel_grad(const Model& m, int n_sols, int n_init, const float2* gk, float* out, void* ws,
+                                  cudaStream_t st);
+size_t nd_spectrum_workspace_bytes(int nb_dims, const int* world, int planes);
+cudaError_t launch_nd_spectrum(int nb_dims, const int* world, int planes, const float* k_real, float2* k_half,
+                               void* ws, cudaStream_t st);
 
 // ---------------------------------------------------------------- adjoint
 struct AdjointSegment {

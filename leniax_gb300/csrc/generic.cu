@@ -27,19 +27,12 @@
 #include "common.cuh"
 #include "engine.h"
 #include "fft.cuh"
+#include "fft_mixed.cuh"
 
 namespace lgx {
 namespace {
 
 constexpr int kGT = 128;  // threads per block
-constexpr int kGMaxStages = 12;
-constexpr int kGMaxN = 512;
-
-struct GPlan {  // radices of one N-point transform, passed by value
-  int n, stages;
-  int r[kGMaxStages];
-};
-
 // Packed rows per block of the row passes: the largest of 8, 4, 2, 1 that
 // divides N/2 with at most 1024 points in flight.
 __host__ __device__ inline int gen_lines(int N) {
@@ -54,101 +47,6 @@ struct GTab {  // per-plan kernel table, passed by value
   int slot[kMaxKernels];
   int gf[kMaxKernels];
 };
-
-// exp(-2 pi i m / L) in float: the octant reduction of cx_trig on exact
-// integers, then sincospif of a reduced fraction (one rounding).
-__device__ float2 tw_entry(int m, int L) {
-  int n = m % L;
-  if (n < 0) n += L;
-  float ss = 1.f, cs = 1.f;
-  if (2 * n > L) {
-    n = L - n;
-    ss = -1.f;
-  }
-  int mm = n, D = L;
-  if (4 * n > L) {
-    mm = L - 2 * n;
-    D = 2 * L;
-    cs = -1.f;
-  }
-  float c, s;
-  if (8 * mm > D) {  // the complementary angle pi/2 - a
-    float sb, cb;
-    sincospif((float)(D - 4 * mm) / (float)(2 * D), &sb, &cb);
-    c = sb;
-    s = cb;
-  } else {
-    sincospif((float)(2 * mm) / (float)D, &s, &c);
-  }
-  return make_float2(cs * c, -(ss * s));
-}
-
-__device__ void fill_twiddles(float2* tw, int N) {
-  for (int j = threadIdx.x; j < N; j += blockDim.x) tw[j] = tw_entry(j, N);
-}
-
-// One Stockham stage of radix R: butterfly j reads in[j + q N/R], twiddles
-// by W_{Ns R}^{q (j mod Ns)}, takes the R-point DFT and writes
-// out[(j / Ns) Ns R + (j mod Ns) + t Ns].
-template <bool INV, int R>
-__device__ __forceinline__ void stockham_stage(const float2* in_all, float2* out_all, int N, int Ns, const float2* tw,
-                                               int nl) {
-  const int nb = N / R, stride = N / (Ns * R);
-  for (int jj = threadIdx.x; jj < nl * nb; jj += blockDim.x) {
-    const int line = jj / nb, j = jj - line * nb;  // lines of N points, contiguous
-    const float2* in = in_all + line * N;
-    float2* out = out_all + line * N;
-    const int k = j % Ns;
-    float2 v[R];
-#pragma unroll
-    for (int q = 0; q < R; ++q) {
-      const float2 x = in[j + q * nb];
-      const float2 w = tw[q * k * stride];  // q k stride < N
-      v[q] = q == 0 ? x : (INV ? cmulc(x, w) : cmul(x, w));
-    }
-    float2 y[R];
-#pragma unroll
-    for (int t = 0; t < R; ++t) {
-      float2 acc = v[0];
-#pragma unroll
-      for (int q = 1; q < R; ++q) {
-        const float2 w = tw[((q * t) % R) * nb];  // W_R^{q t} = W_N^{(q t mod R) N / R}
-        acc = cadd(acc, INV ? cmulc(v[q], w) : cmul(v[q], w));
-      }
-      y[t] = acc;
-    }
-    const int base = (j / Ns) * Ns * R + k;
-#pragma unroll
-    for (int t = 0; t < R; ++t) out[base + t * Ns] = y[t];
-  }
-}
-
-// N-point FFTs of the block's nl contiguous lines in a into a or b
-// (returned); unnormalised for INV.  Every thread of the block calls it; it
-// ends on a barrier.
-template <bool INV>
-__device__ float2* fft_line(float2* a, float2* b, const GPlan& p, const float2* tw, int nl = 1) {
-  const int N = p.n;
-  float2* in = a;
-  float2* out = b;
-  int Ns = 1;
-  for (int s = 0; s < p.stages; ++s) {
-    const int R = p.r[s];
-    switch (R) {
-      case 2: stockham_stage<INV, 2>(in, out, N, Ns, tw, nl); break;
-      case 3: stockham_stage<INV, 3>(in, out, N, Ns, tw, nl); break;
-      case 4: stockham_stage<INV, 4>(in, out, N, Ns, tw, nl); break;
-      case 5: stockham_stage<INV, 5>(in, out, N, Ns, tw, nl); break;
-      default: stockham_stage<INV, 7>(in, out, N, Ns, tw, nl); break;
-    }
-    __syncthreads();
-    Ns *= R;
-    float2* t = in;
-    in = out;
-    out = t;
-  }
-  return in;
-}
 
 // ------------------------------------------------------------ rows forward
 __global__ void __launch_bounds__(kGT) gen_row_fwd_kernel(GPlan p, const float* __restrict__ state,
@@ -412,28 +310,6 @@ __global__ void gen_prepare_kernel(long planes, int N, const float2* __restrict_
     }
     kp[i] = o;
   }
-}
-
-GPlan make_plan(int N) {
-  GPlan p;
-  p.n = N;
-  p.stages = 0;
-  int n = N;
-  while (n % 4 == 0 && p.stages < kGMaxStages) {
-    p.r[p.stages++] = 4;
-    n /= 4;
-  }
-  while (n % 2 == 0 && p.stages < kGMaxStages) {
-    p.r[p.stages++] = 2;
-    n /= 2;
-  }
-  for (int f : {3, 5, 7})
-    while (n % f == 0 && p.stages < kGMaxStages) {
-      p.r[p.stages++] = f;
-      n /= f;
-    }
-  if (n != 1) p.stages = 0;
-  return p;
 }
 
 }  // namespace

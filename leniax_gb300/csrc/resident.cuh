@@ -99,8 +99,8 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
     for (int n2 = 0; n2 < P; ++n2)
       z[n2] = make_float2(__ldg(c0 + (2 * grp) * N + t + G * n2), __ldg(c0 + (2 * grp + 1) * N + t + G * n2));
     if (tid == 0) {
-      shv[0] = 0;
-      shv[1] = 0;
+      shv[0] = a.shift_in ? __ldg(a.shift_in + 2 * world) : 0;
+      shv[1] = a.shift_in ? __ldg(a.shift_in + 2 * world + 1) : 0;
     }
     named_bar(bar_id, NT);
 
@@ -368,7 +368,13 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
       // packed row, and the next step's first barrier orders these partials
     }
     named_bar(bar_id, NT);
-    if (a.steps > 0 && wid == NW - 1) finalize(a.steps - 1);
+    if (a.steps > 0 && wid == NW - 1) {
+      finalize(a.steps - 1);
+      if (a.shift_out && lane == 0) {  // the lane that advanced the shift
+        a.shift_out[2 * world] = shv[0];
+        a.shift_out[2 * world + 1] = shv[1];
+      }
+    }
     if (a.final_cells) {
       float* fc = a.final_cells + (size_t)world * N * N;
 #pragma unroll

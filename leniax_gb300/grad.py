@@ -13,10 +13,13 @@ behind a ``torch.autograd.Function``:
   spectrum correlation, growth derivative, clip gradient ``'ste'`` or
   ``'mask'``).
 
-Gradients flow to the initial cells, the world-sized fftshifted real kernel
-(and through :func:`ring_kernel` to the ring weights ``b``), the growth
-parameters ``(m, s)`` and the kernel weights.  Models: 2D, one channel, one
-kernel, square worlds of 32..256.
+Gradients flow to the initial cells, each kernel's world-sized fftshifted
+real kernel (and through :func:`ring_kernel` to the ring weights ``b``), the
+growth parameters ``(m, s)`` of every kernel and the full
+``kernels_weight_per_channel`` matrix.  Models: every model ``lgx_run`` runs
+-- 2D and 3D worlds, any number of channels and kernels, weighted mean or
+sum; 2D one-kernel square worlds of 32..256 take the engine's specialised
+one-kernel adjoint, all others its general N-D adjoint.
 """
 import ctypes
 import math
@@ -44,6 +47,13 @@ def _bind(lib):
     lib.lgx_kernel_spectrum.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
     lib.lgx_kernel_spectrum.restype = ctypes.c_int
+    lib.lgx_kernel_spectrum_nd_workspace_bytes.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int]
+    lib.lgx_kernel_spectrum_nd_workspace_bytes.restype = ctypes.c_size_t
+    lib.lgx_kernel_spectrum_nd.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    lib.lgx_kernel_spectrum_nd.restype = ctypes.c_int
+    lib.lgx_adjoint_kernel_grad_acc_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    lib.lgx_adjoint_kernel_grad_acc_bytes.restype = ctypes.c_size_t
     lib._lgx_grad_bound = True
     return lib
 
@@ -58,20 +68,40 @@ class AdjointJob(ctypes.Structure):
     ]
 
 
-def kernel_spectrum(k_real: torch.Tensor) -> torch.Tensor:
-    """fftn of world-sized fftshifted real kernels ``[..., H, W]`` on the
-    device (leniax ``kernels.py:145-149``) -> Hermitian halves
-    ``[..., H, W//2+1]`` complex64."""
+def kernel_spectrum(k_real: torch.Tensor, nb_dims: int = 2) -> torch.Tensor:
+    """fftn over the last ``nb_dims`` axes of world-sized fftshifted real
+    kernels ``[..., *world]`` on the device (leniax ``kernels.py:145-149``) ->
+    Hermitian halves ``[..., *world[:-1], W//2+1]`` complex64."""
     _require_cuda('k_real', k_real)
-    H, W = k_real.shape[-2:]
-    lead = k_real.shape[:-2]
+    world = tuple(int(w) for w in k_real.shape[-nb_dims:])
+    lead = k_real.shape[:-nb_dims]
     planes = int(math.prod(lead)) if lead else 1
     kr = k_real.contiguous()
-    out = torch.empty(lead + (H, W // 2 + 1), dtype=torch.complex64, device=k_real.device)
+    out = torch.empty(lead + world[:-1] + (world[-1] // 2 + 1, ), dtype=torch.complex64, device=k_real.device)
     lib = _bind(_lib.load())
-    ws = workspace(planes * H * W * 4, k_real.device)
-    _lib.check(lib.lgx_kernel_spectrum(H, W, planes, kr.data_ptr(), out.data_ptr(), ws.data_ptr(), ws.numel(),
-                                       _stream_handle(k_real.device)))
+    H, W = world[-2], world[-1]
+    if nb_dims == 2 and H == W and H in (32, 64, 128, 256):
+        ws = workspace(planes * H * W * 4, k_real.device)
+        _lib.check(lib.lgx_kernel_spectrum(H, W, planes, kr.data_ptr(), out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                           _stream_handle(k_real.device)))
+        return out
+    wa = (ctypes.c_int * 3)(*world)
+    nbytes = lib.lgx_kernel_spectrum_nd_workspace_bytes(nb_dims, wa, planes)
+    if nbytes == 0:
+        raise _lib.LgxError(_lib.LGX_ERR_UNSUPPORTED, f'no kernel spectrum for world {world}')
+    ws = workspace(nbytes, k_real.device)
+    _lib.check(lib.lgx_kernel_spectrum_nd(nb_dims, wa, planes, kr.data_ptr(), out.data_ptr(), ws.data_ptr(),
+                                          ws.numel(), _stream_handle(k_real.device)))
+    return out
+
+
+def _engine_spectra(m, k_half: torch.Tensor) -> torch.Tensor:
+    """Per-kernel half spectra ``[Ns, K, ...]`` placed at leniax's spectrum
+    positions ``[Ns, C, max_k, ...]`` (kernels.py:122-152; padded slots zero)."""
+    Ns = k_half.shape[0]
+    out = torch.zeros((Ns, m.C, m.max_k) + tuple(k_half.shape[2:]), dtype=k_half.dtype, device=k_half.device)
+    for k, (c, j) in enumerate(zip(m.cin, m.slot)):
+        out[:, c, j] = k_half[:, k]
     return out
 
 
@@ -91,24 +121,28 @@ def ring_kernel(R: float, r: float, b: torch.Tensor, kf_slug: str, kf_params: Se
                 world: Sequence[int]) -> torch.Tensor:
     """World-sized, fftshifted ring kernel (what leniax FFTs), differentiable
     in the ring weights ``b`` (1-D tensor).  Mirrors ``circle_2d``
-    (kernels.py:176-212), the centring pad (kernels.py:93-101) and the
+    (kernels.py:176-212) -- over every world axis for 3D worlds, the distance
+    taken over all axes -- the centring pad (kernels.py:93-101) and the
     fftshift (kernels.py:148)."""
     dev, dt = b.device, torch.float32
+    nd = len(world)
     k = math.ceil(r * R)
     idx = torch.arange(2 * k, device=dev, dtype=dt) - k
-    yy, xx = torch.meshgrid(idx, idx, indexing='ij')
-    dist = torch.sqrt((yy / (r * R))**2 + (xx / (r * R))**2)
+    grids = torch.meshgrid(*([idx] * nd), indexing='ij')
+    dist = torch.sqrt(sum((g / (r * R))**2 for g in grids))
     nb = b.shape[0]
     bdist = nb * dist
     ring = torch.clamp(torch.floor(bdist).long(), max=nb - 1)
     raw = _kf_torch(kf_slug, float(kf_params[0]), torch.remainder(bdist, 1.0))
     kern = (dist < 1).to(dt) * raw * b[ring]
     kern = kern / kern.sum()
-    H, W = world
-    ph, pw = (H - 2 * k) // 2, (W - 2 * k) // 2
-    full = torch.nn.functional.pad(kern, (pw, W - 2 * k - pw, ph, H - 2 * k - ph))
-    # fftshift of an even-sized world: index H/2 (the kernel centre) moves to 0
-    return torch.roll(full, shifts=(-(H // 2), -(W // 2)), dims=(0, 1))
+    pads = []
+    for ws in reversed(list(world)):  # F.pad lists the last axis first
+        need = ws - 2 * k
+        pads += [need // 2, need - need // 2]
+    full = torch.nn.functional.pad(kern, pads)
+    # fftshift (a roll by n // 2 along every axis, also for odd sides)
+    return torch.roll(full, shifts=tuple(ws // 2 for ws in world), dims=tuple(range(nd)))
 
 
 # ---------------------------------------------------------------------------
@@ -116,9 +150,11 @@ class LeniaRolloutFunction(torch.autograd.Function):
     """``final = LeniaRolloutFunction.apply(cells0, k_real, gf_params, weights,
     T, update_fn, steps, checkpoint_every, clip_grad)``
 
-    cells0 ``[Ns, Ni, 1, H, W]``; k_real ``[Ns, H, W]`` world-sized fftshifted
-    kernels; gf_params ``[Ns, 1, 2]``; weights ``[Ns, 1, 1]``; T ``[Ns]``.
-    Returns the state after ``steps`` steps ``[Ns, Ni, 1, H, W]``.
+    cells0 ``[Ns, Ni, C, *world]``; k_real ``[Ns, K, *world]`` (or
+    ``[Ns, *world]`` for one kernel): each true kernel's world-sized
+    fftshifted real kernel in leniax's channel-sorted order; gf_params
+    ``[Ns, K, 2]``; weights ``[Ns, C, K]``; T ``[Ns]``.  Returns the state
+    after ``steps`` steps ``[Ns, Ni, C, *world]``.
     """
 
     @staticmethod
@@ -127,9 +163,11 @@ class LeniaRolloutFunction(torch.autograd.Function):
         m = update_fn.model
         dev = cells0.device
         Ns, Ni = cells0.shape[:2]
-        k_half = kernel_spectrum(k_real.detach().float()).reshape(Ns, 1, 1, m.world[0], m.world[1] // 2 + 1)
-        gf = gf_params.detach().float().reshape(Ns, 1, 2).contiguous()
-        w = weights.detach().float().reshape(Ns, 1, 1).contiguous()
+        nd = len(m.world)
+        kr = k_real.detach().float().reshape((Ns, m.K) + m.world)
+        k_half = _engine_spectra(m, kernel_spectrum(kr, nd))
+        gf = gf_params.detach().float().reshape(Ns, m.K, 2).contiguous()
+        w = weights.detach().float().reshape(Ns, m.C, m.K).contiguous()
         Tt = torch.as_tensor(T, dtype=torch.float32, device=dev).reshape(-1).expand(Ns).contiguous()
         k = max(1, int(checkpoint_every))
         ckpts = [cells0.detach().contiguous()]
@@ -143,6 +181,7 @@ class LeniaRolloutFunction(torch.autograd.Function):
                 ckpts.append(cur)
         ctx.save_for_backward(k_half, gf, w, Tt, *ckpts)
         ctx.update_fn, ctx.steps, ctx.k, ctx.clip = update_fn, steps, k, CLIP_GRAD[clip_grad]
+        ctx.k_shape = tuple(k_real.shape)
         return cur
 
     @staticmethod
@@ -152,19 +191,22 @@ class LeniaRolloutFunction(torch.autograd.Function):
         m = update_fn.model
         dev = grad_final.device
         Ns, Ni = ckpts[0].shape[:2]
-        H, W = m.world
         lib = _bind(_lib.load())
-        nw = Ns * Ni
+        handle = m.plan.handle
         lam = grad_final.detach().float().contiguous().clone()
         lam_out = torch.empty_like(lam)
-        acc = torch.zeros((nw, H // 2, W), dtype=torch.complex64, device=dev)
-        g_gf = torch.zeros((Ns, 1, 2), dtype=torch.float32, device=dev)
-        g_w = torch.zeros((Ns, 1, 1), dtype=torch.float32, device=dev)
-        ws = workspace(lib.lgx_adjoint_workspace_bytes(update_fn.model.plan.handle, Ns, Ni), dev)
+        acc_bytes = lib.lgx_adjoint_kernel_grad_acc_bytes(handle, Ns, Ni)
+        ws_bytes = lib.lgx_adjoint_workspace_bytes(handle, Ns, Ni)
+        if acc_bytes == 0 or ws_bytes == 0:
+            raise _lib.LgxError(_lib.LGX_ERR_UNSUPPORTED, 'no adjoint for this model')
+        acc = torch.zeros(acc_bytes // 4, dtype=torch.float32, device=dev)
+        g_gf = torch.zeros((Ns, m.K, 2), dtype=torch.float32, device=dev)
+        g_w = torch.zeros((Ns, m.C, m.K), dtype=torch.float32, device=dev)
+        ws = workspace(ws_bytes, dev)
         seg_starts = list(range(0, steps, k))
         # Segment j - 1's trajectory is recomputed on a side stream while
-        # segment j's adjoint runs: the two persistent launches take
-        # different SMs when a batch fills fewer than half of them.
+        # segment j's adjoint runs: the two launches take different SMs when
+        # a batch fills fewer than half of them.
         main = torch.cuda.current_stream(dev)
         side = torch.cuda.Stream(device=dev)
         side.wait_stream(main)
@@ -176,6 +218,7 @@ class LeniaRolloutFunction(torch.autograd.Function):
                 ev.record(side)
             return tr, ev
 
+        kh = torch.view_as_real(k_half.contiguous())
         nxt = recompute(len(seg_starts) - 1)
         for j in reversed(range(len(seg_starts))):
             n = min(k, steps - seg_starts[j])
@@ -187,20 +230,19 @@ class LeniaRolloutFunction(torch.autograd.Function):
             tp.record_stream(main)
             job = AdjointJob()
             job.n_sols, job.n_init, job.steps = Ns, Ni, n
-            job.k_half, job.gf_params, job.weights, job.T = (k_half.data_ptr(), gf.data_ptr(), w.data_ptr(),
+            job.k_half, job.gf_params, job.weights, job.T = (kh.data_ptr(), gf.data_ptr(), w.data_ptr(),
                                                              Tt.data_ptr())
             job.traj_cells, job.traj_potential = tc.data_ptr(), tp.data_ptr()
             job.lambda_in, job.lambda_out = lam.data_ptr(), lam_out.data_ptr()
             job.kernel_grad_acc = acc.data_ptr()
             job.grad_gf, job.grad_weights = g_gf.data_ptr(), g_w.data_ptr()
             job.clip_grad = ctx.clip
-            _lib.check(lib.lgx_adjoint(update_fn.model.plan.handle, job, ws.data_ptr(), ws.numel(),
-                                       _stream_handle(dev)))
+            _lib.check(lib.lgx_adjoint(handle, job, ws.data_ptr(), ws.numel(), _stream_handle(dev)))
             lam, lam_out = lam_out, lam
-        g_k = torch.empty((Ns, H, W), dtype=torch.float32, device=dev)
-        _lib.check(lib.lgx_adjoint_kernel_grad(update_fn.model.plan.handle, Ns, Ni, acc.data_ptr(), g_k.data_ptr(),
-                                               ws.data_ptr(), ws.numel(), _stream_handle(dev)))
-        return lam, g_k, g_gf, g_w, None, None, None, None, None
+        g_k = torch.empty((Ns, m.K) + m.world, dtype=torch.float32, device=dev)
+        _lib.check(lib.lgx_adjoint_kernel_grad(handle, Ns, Ni, acc.data_ptr(), g_k.data_ptr(), ws.data_ptr(),
+                                               ws.numel(), _stream_handle(dev)))
+        return lam, g_k.reshape(ctx.k_shape), g_gf, g_w, None, None, None, None, None
 
 
 def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj):
@@ -219,8 +261,8 @@ def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj):
     job.final_cells = final.data_ptr()
     tc = tp = None
     if traj:
-        tc = torch.empty((n, Ns * Ni, 1) + m.world, dtype=torch.float32, device=dev)
-        tp = torch.empty_like(tc)
+        tc = torch.empty((n, Ns * Ni, m.C) + m.world, dtype=torch.float32, device=dev)
+        tp = torch.empty((n, Ns * Ni, m.K) + m.world, dtype=torch.float32, device=dev)
         job.traj_cells, job.traj_potential = tc.data_ptr(), tp.data_ptr()
     eng = _lib.ENGINES['auto']
     ws = workspace(lib.lgx_run_workspace_bytes(m.plan.handle, Ns, Ni, n, eng), dev)

@@ -67,3 +67,50 @@ def fd_grad(fn, x0, idx, h=1e-6):
         xm[i] -= h
         out.append((fn(xp.reshape(x0.shape)) - fn(xm.reshape(x0.shape))) / (2 * h))
     return np.array(out)
+
+
+# ---------------------------------------------------------------------------
+# Several channels and kernels, any number of world axes
+def rollout_general(cells0, k_real, gf, w, dt, steps, cin, slugs, clip='ste', mean=True, state_slug='v1'):
+    """The general graph of leniax's update (core.py:52-319): per kernel k the
+    potential real(ifftn(fftn(state[c_in(k)]) * fftn(k_real[k]))) over every
+    world axis, growth per kernel, the [C, K] weighting (weighted_mean divides
+    by the per-channel weight sums, weighted_sum does not; core.py:202-242),
+    then get_state.  cells0 [..., C, *world]; k_real [K, *world]; gf [K, 2];
+    w [C, K]; cin / slugs: the input channel and growth slug of each kernel.
+    Returns the state after `steps` steps."""
+    nd = k_real.dim() - 1
+    world = tuple(k_real.shape[1:])
+    axes = tuple(range(-nd, 0))
+    Kh = torch.fft.rfftn(k_real, dim=axes)  # [K, *half]
+    idx = torch.as_tensor(cin, dtype=torch.long)
+    x = cells0
+    for _ in range(steps):
+        X = torch.fft.rfftn(x, dim=axes)  # [..., C, *half]
+        U = torch.fft.irfftn(X.index_select(-(nd + 1), idx) * Kh, s=world, dim=axes)  # [..., K, *world]
+        G = torch.stack([growth(U.select(-(nd + 1), k), gf[k, 0], gf[k, 1], slugs[k]) for k in range(len(cin))],
+                        dim=-(nd + 1))
+        Gm = G.movedim(-(nd + 1), -1)  # [..., *world, K]
+        f = (Gm.unsqueeze(-2) * w).sum(-1)  # [..., *world, C]
+        if mean:
+            f = f / w.sum(-1)
+        f = f.movedim(-1, -(nd + 1))  # [..., C, *world]
+        if state_slug == 'v2':
+            x = x * (1 - dt) + dt * f
+        elif state_slug == 'simple':
+            x = x + dt * f
+        else:
+            n = x + dt * f
+            c = torch.clamp(n, 0., 1.)
+            x = (n - n.detach() + c.detach()) if clip == 'ste' else c
+    return x
+
+
+def loss_and_grads_general(cells0, k_real, gf, w, dt, steps, target, cin, slugs, **kw):
+    """MSE loss of the final state against `target` and its gradients with
+    respect to (cells0, k_real, gf, w), in the dtype of the inputs."""
+    leaves = [torch.as_tensor(v).clone().requires_grad_(True) for v in (cells0, k_real, gf, w)]
+    final = rollout_general(*leaves, dt, steps, cin, slugs, **kw)
+    loss = ((final - torch.as_tensor(target))**2).mean()
+    grads = torch.autograd.grad(loss, leaves)
+    return float(loss.detach()), [g.numpy() for g in grads]

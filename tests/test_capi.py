@@ -64,15 +64,38 @@ def test_3d_plans_select_the_cta_engine_and_size_workspaces():
     assert lib.lgx_select_engine(p.handle, 1, 2, 0) == _lib.ENGINES['cta']
     assert lib.lgx_update_workspace_bytes(p.handle, 3) > 0  # core.update on 3D worlds
     assert lib.lgx_run_workspace_bytes(p.handle, 1, 2, 4, 0) > 0
-    # several channels in 3D: no engine, no update workspace
+    # several channels in 3D: the general N-D engine
     p2 = _plan(nb_dims=3, world=(32, 32, 32), nb_channels=2, kernel_cin=[0, 1], kernel_slot=[0, 0], growth_ids=[1, 1])
-    assert lib.lgx_select_engine(p2.handle, 1, 2, 0) == -1
-    assert lib.lgx_update_workspace_bytes(p2.handle, 3) == 0
+    assert lib.lgx_select_engine(p2.handle, 1, 2, 0) == _lib.ENGINES['nd']
+    assert lib.lgx_update_workspace_bytes(p2.handle, 3) > 0
+
+
+@pytest.mark.parametrize('nb_dims,world', [(3, (48, 48, 48)), (3, (24, 40, 36)), (2, (100, 128)), (2, (45, 45)),
+                                           (2, (35, 64)), (3, (128, 128, 128))])
+def test_other_worlds_select_the_nd_engine_and_its_adjoint(nb_dims, world):
+    # leniax's get_potential_fft transforms any world shape (core.py:74-87):
+    # odd, non-square and 3D sides of factors 2, 3, 5, 7 run on the N-D engine
+    lib = _lib.load()
+    for attr in ('lgx_adjoint_workspace_bytes', 'lgx_adjoint_kernel_grad_acc_bytes'):
+        getattr(lib, attr).restype = ctypes.c_size_t
+        getattr(lib, attr).argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+    p = _plan(nb_dims=nb_dims, world=world, nb_channels=2, kernel_cin=[0, 1, 1], kernel_slot=[0, 0, 1],
+              growth_ids=[1, 0, 2], max_k=2)
+    assert lib.lgx_select_engine(p.handle, 1, 2, 0) == _lib.ENGINES['nd']
+    assert lib.lgx_run_workspace_bytes(p.handle, 1, 2, 4, 0) > 0
+    assert lib.lgx_update_workspace_bytes(p.handle, 3) > 0
+    assert lib.lgx_adjoint_workspace_bytes(p.handle, 2, 3) > 0
+    cells = 1
+    for w in world:
+        cells *= w
+    assert lib.lgx_adjoint_kernel_grad_acc_bytes(p.handle, 2, 3) == 2 * 3 * 3 * cells * 8
 
 
 @pytest.mark.parametrize('kw,code', [
-    (dict(world=(100, 128)), _lib.LGX_ERR_UNSUPPORTED),  # a side that is not a power of two: square only
     (dict(world=(66, 66)), _lib.LGX_ERR_UNSUPPORTED),    # 66 = 2 * 3 * 11: no radix-11 pass
+    (dict(world=(26, 32)), _lib.LGX_ERR_UNSUPPORTED),    # 26 = 2 * 13
+    (dict(world=(1024, 1024)), _lib.LGX_ERR_UNSUPPORTED),  # sides up to 512
+    (dict(nb_dims=3, world=(32, 22, 32)), _lib.LGX_ERR_UNSUPPORTED),
     (dict(nb_dims=4), _lib.LGX_ERR_INVALID),
     (dict(kernel_cin=[1]), _lib.LGX_ERR_INVALID),
     (dict(growth_ids=[42]), _lib.LGX_ERR_UNSUPPORTED),

@@ -111,7 +111,7 @@ def _oracle_rollout(kparams, world, C, R, T, cells, steps, dtype=np.float32, wit
                       keep_intermediary=False, with_box=with_box)
 
 
-@pytest.mark.parametrize('engine', ['resident', 'streamed', 'plain'])
+@pytest.mark.parametrize('engine', ['resident', 'streamed', 'plain', 'plain_streamed'])
 def test_rollout_matches_fp64_oracle(cuda, engine):
     # single world, 128^2, 128 steps: state max abs error and mass / centroid
     # relative error <= 1e-4 against the FP64 oracle
@@ -185,6 +185,42 @@ def test_mem_optimized_batch_matches_oracle_and_engines_agree(cuda):
             assert (np.abs(mass - st['mass']) / np.maximum(np.abs(st['mass']), 1e-3)).max() < 1e-4, engine
             cm = sd['channel_mass'][s].cpu().numpy()
             assert cm.shape == (steps, Ni, 1)
+
+
+@pytest.mark.parametrize('size', [32, 64, 128])
+def test_plain_engine_is_the_resident_step_one_launch_at_a_time(cuda, size):
+    # the one-world-per-launch engine runs the resident kernel for one world
+    # and one step per launch, chaining the carried shift through global
+    # memory: states, statistics, centroids and trajectories must equal the
+    # batched resident engine's bit for bit
+    dev = torch.device('cuda')
+    R, steps, Ns, Ni = {32: 6, 64: 10, 128: 13}[size], 12, 2, 3
+    cells = np.stack([patch_init(Ni, size, size // 3, seed=60 + s, scale_range=(0.6, 1.0)) for s in range(Ns)])
+    Ks, gfs, ws = [], [], []
+    upd = None
+    for s, (m, sg) in enumerate([(0.15, 0.015), (0.2, 0.03)]):
+        K, mp, u = engine_model(bump_kernel_params(m=m, s=sg), [size, size], 1, R, dev=dev)
+        upd = upd or u
+        Ks.append(K)
+        gfs.append(mp.get_gf_params(dev))
+        ws.append(mp.get_kernels_weight_per_channel(dev))
+    stats_fn = statistics.ComputeStatsFn([size, size], R, 10)
+    outs = {}
+    for engine in ('resident', 'plain'):
+        outs[engine] = runner.run_scan_mem_optimized(None, torch.from_numpy(cells).to(dev), torch.stack(Ks),
+                                                     torch.stack(gfs), torch.stack(ws), torch.tensor([10., 5.]), steps,
+                                                     R, upd, stats_fn, engine=engine, with_box=True,
+                                                     with_centroid=True)
+    (sd_r, fin_r), (sd_p, fin_p) = outs['resident'], outs['plain']
+    assert torch.equal(fin_r, fin_p)
+    for k in sd_r:
+        assert torch.equal(sd_r[k], sd_p[k]), k
+    traj = {}
+    for engine in ('resident', 'plain'):
+        traj[engine] = runner.run_scan(None, torch.from_numpy(cells[0]).to(dev), Ks[0], gfs[0], ws[0],
+                                       torch.tensor(10.), steps, R, upd, stats_fn, engine=engine)
+    for a, b in zip(traj['resident'][:3], traj['plain'][:3]):
+        assert torch.equal(a, b)
 
 
 def test_partial_items_and_zero_steps(cuda):
