@@ -214,7 +214,21 @@ typedef struct lgx_adjoint_job {
   float* grad_weights;          /* [Ns, C, K] dL/d(kernels_weight_per_channel), every
                                    entry (zero weights included), accumulated (+=)     */
   int clip_grad;                /* LGX_CLIP_GRAD_*                                    */
+  const float* cells_after;     /* [Ns*Ni, C, *world] state after the segment's last step
+                                   (the next checkpoint, or the rollout's result), or NULL.
+                                   With LGX_CLIP_GRAD_MASK the clip's mask is then read from
+                                   the forward's own outputs -- 1 where the next state lies
+                                   strictly inside (0, 1) -- so it is the exact derivative of
+                                   the map the forward computed; without it the mask is
+                                   re-derived from s + dt f                             */
 } lgx_adjoint_job;
+
+/* Adjoint engine of a plan: LGX_ENGINE_AUTO (default: the one-kernel adjoint
+ * for 2D C = K = 1 square worlds of 32..256, the general N-D adjoint
+ * otherwise) or LGX_ENGINE_ND (the general N-D adjoint for every model).  Set
+ * before the plan's adjoint calls: the workspace and accumulator sizes, the
+ * accumulator layout and lgx_adjoint_kernel_grad follow it. */
+LGX_API int lgx_plan_set_adjoint_engine(lgx_plan* plan, int engine);
 
 /* Workspace bytes of lgx_adjoint (and lgx_adjoint_kernel_grad) for a batch;
  * 0 when the model has no adjoint. */
@@ -357,6 +371,10 @@ typedef struct lgx_init_job {
   const uint64_t* seeds; /* [n_worlds] device */
   const float* gf_m;     /* [n_worlds] device: m of the first kernel (Perlin kinds) */
   float* out;            /* [n_worlds, nb_init, H, W] */
+  const float* angles;   /* Perlin kinds: [n_worlds, nb_init, res0, res1] gradient angles in
+                            radians, res0 = H // (3 ceil R), res1 = W // (2 ceil R) -- the
+                            `angles` input of perlin.py:16-71 -- or NULL to draw them
+                            uniformly in [0, 2 pi) from the seeds */
 } lgx_init_job;
 
 LGX_API int lgx_init_cells_workspace_bytes(const lgx_init_job* job, size_t* bytes);

@@ -37,7 +37,7 @@ EXPORTED = (
     'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update', 'lgx_fp32_probe',
     'lgx_batch_workspace_bytes', 'lgx_batch_run', 'lgx_workspace_status', 'lgx_ring_kernels_workspace_bytes',
     'lgx_ring_kernels', 'lgx_selftest_wait_timeout', 'lgx_adjoint_kernel_grad_acc_bytes', 'lgx_kernel_spectrum_nd',
-    'lgx_kernel_spectrum_nd_workspace_bytes'
+    'lgx_kernel_spectrum_nd_workspace_bytes', 'lgx_plan_set_adjoint_engine'
 )
 
 

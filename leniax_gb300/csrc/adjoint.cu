@@ -154,8 +154,8 @@ __global__ void __launch_bounds__(kT) adj_row_fwd_kernel(int planes, const float
 template <int N>
 __global__ void __launch_bounds__(kT) adj_rows_kernel(AdjParams p, const float* __restrict__ lam_in,
                                                       const float* __restrict__ s_t, const float* __restrict__ u_t,
-                                                      float* __restrict__ lam_next, float2* __restrict__ spec,
-                                                      float* __restrict__ pacc) {
+                                                      const float* __restrict__ s_next, float* __restrict__ lam_next,
+                                                      float2* __restrict__ spec, float* __restrict__ pacc) {
   constexpr int G = ACfg<N>::G;
   using GE = Geo<N, G>;
   constexpr int P = GE::P, Q = GE::Q, GPB = kT / G, BPP = (N / 2 + GPB - 1) / GPB;
@@ -188,7 +188,8 @@ __global__ void __launch_bounds__(kT) adj_rows_kernel(AdjParams p, const float* 
         growth_and_grads(p.gf_id, u, m, sg, g, gu, gm, gs);
         float mu = lam;
         if (p.state_fn == LGX_STATE_V1 && p.clip_mask) {
-          const float nn = sv + dt * (g * wf);
+          // the forward's clip was inactive where its output lies strictly inside (0, 1)
+          const float nn = s_next ? __ldg(s_next + off) : sv + dt * (g * wf);
           mu = (nn > 0.f && nn < 1.f) ? lam : 0.f;
         }
         lam_next[off] = p.state_fn == LGX_STATE_V2 ? mu * (1.f - dt) : mu;
@@ -540,7 +541,9 @@ cudaError_t adjoint_n(const AdjointSegment& j, cudaStream_t st) {
     float* lam_next = (s == 0) ? j.lambda_out : ((s & 1) ? j.lam_a : j.lam_b);
     const float* st_s = j.traj_cells + (size_t)s * nw * cells;
     const float* st_u = j.traj_potential + (size_t)s * nw * cells;
-    adj_rows_kernel<N><<<(unsigned)(nw * BPP), kT, smem, st>>>(p, lam_cur, st_s, st_u, lam_next, j.spec, j.partial);
+    const float* st_n = s + 1 < j.steps ? st_s + (size_t)nw * cells : j.cells_after;
+    adj_rows_kernel<N><<<(unsigned)(nw * BPP), kT, smem, st>>>(p, lam_cur, st_s, st_u, st_n, lam_next, j.spec,
+                                                               j.partial);
     col_adj_kernel<N><<<(unsigned)(nw * BPP), kT, smem, st>>>(nw, j.n_init, j.spec, j.kp, kp_sol, j.gk, j.prod);
     row_inv_add_kernel<N><<<(unsigned)(nw * BPP), kT, smem, st>>>(nw, j.prod, lam_next, 1.f, 1);
     lam_cur = lam_next;

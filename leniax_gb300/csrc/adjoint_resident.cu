@@ -257,6 +257,10 @@ __global__ void __launch_bounds__(512, 1) adjoint_resident_kernel(AdjResArgs a) 
         const size_t off = ((size_t)st * a.n_worlds + world) * plane + (size_t)(2 * grp) * N;
         const float* sp = a.traj_cells + off;
         const float* up = a.traj_pot + off;
+        // state after this step: the next trajectory entry, or the segment's result
+        const float* snp = st + 1 < a.steps ? sp + (size_t)a.n_worlds * plane
+                                            : (a.cells_after ? a.cells_after + world * plane + (size_t)(2 * grp) * N
+                                                             : nullptr);
         float2 za[P], zs[P];
 #pragma unroll
         for (int k1 = 0; k1 < P; ++k1) {
@@ -270,7 +274,8 @@ __global__ void __launch_bounds__(512, 1) adjoint_resident_kernel(AdjResArgs a) 
             growth_grads<GF>(a.gf_id, u, m, sg, g, gu, gm, gs);
             float mu = lamv;
             if (a.state_fn == LGX_STATE_V1 && a.clip_mask) {
-              const float nn = sv + dt * (g * wf);
+              // the forward's clip was inactive where its output lies strictly inside (0, 1)
+              const float nn = snp ? __ldg(snp + e * N + x) : sv + dt * (g * wf);
               mu = (nn > 0.f && nn < 1.f) ? lamv : 0.f;
             }
             le[e] = a.state_fn == LGX_STATE_V2 ? mu * (1.f - dt) : mu;

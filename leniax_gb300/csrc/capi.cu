@@ -15,6 +15,7 @@ using namespace lgx;
 
 struct lgx_plan {
   Model m;
+  int adjoint_engine;  // LGX_ENGINE_AUTO or LGX_ENGINE_ND (lgx_plan_set_adjoint_engine)
 };
 
 namespace {
@@ -260,6 +261,7 @@ int lgx_plan_create(const lgx_model_desc* d, lgx_plan** out) {
   lgx_plan* p = new (std::nothrow) lgx_plan;
   if (!p) return fail(LGX_ERR_INVALID, "out of host memory");
   p->m = m;
+  p->adjoint_engine = LGX_ENGINE_AUTO;
   *out = p;
   g_err.clear();
   return LGX_OK;
@@ -746,6 +748,10 @@ const Model* plan_model(const lgx_plan* plan) { return plan ? &plan->m : nullptr
 // ------------------------------------------------------------------ adjoint
 namespace {
 
+// The general N-D adjoint runs every model the one-kernel adjoint does not,
+// and every model when the plan asks for it.
+bool adjoint_is_nd(const lgx_plan& p) { return p.adjoint_engine == LGX_ENGINE_ND || !adjoint_supported(p.m); }
+
 size_t adjoint_ws(const Model& m, int n_sols, int n_init) {
   const size_t nw = (size_t)n_sols * n_init, cells = (size_t)m.H * m.W;
   size_t b = 0;
@@ -761,25 +767,35 @@ size_t adjoint_ws(const Model& m, int n_sols, int n_init) {
 
 extern "C" {
 
+int lgx_plan_set_adjoint_engine(lgx_plan* plan, int engine) {
+  if (!plan) return fail(LGX_ERR_INVALID, "lgx_plan_set_adjoint_engine: null plan");
+  if (engine != LGX_ENGINE_AUTO && engine != LGX_ENGINE_ND)
+    return fail(LGX_ERR_INVALID, "lgx_plan_set_adjoint_engine: LGX_ENGINE_AUTO or LGX_ENGINE_ND");
+  if (engine == LGX_ENGINE_ND && !nd_supported(plan->m))
+    return fail(LGX_ERR_UNSUPPORTED, "lgx_plan_set_adjoint_engine: no N-D adjoint for this model");
+  plan->adjoint_engine = engine;
+  g_err.clear();
+  return LGX_OK;
+}
+
 size_t lgx_adjoint_workspace_bytes(const lgx_plan* plan, int n_sols, int n_init) {
   if (!plan || n_sols < 1 || n_init < 1) return 0;
-  if (adjoint_supported(plan->m)) return adjoint_ws(plan->m, n_sols, n_init);
-  if (nd_supported(plan->m)) return nd_adjoint_workspace_bytes(plan->m, n_sols, n_init);
-  return 0;
+  if (!adjoint_is_nd(*plan)) return adjoint_supported(plan->m) ? adjoint_ws(plan->m, n_sols, n_init) : 0;
+  return nd_supported(plan->m) ? nd_adjoint_workspace_bytes(plan->m, n_sols, n_init) : 0;
 }
 
 size_t lgx_adjoint_kernel_grad_acc_bytes(const lgx_plan* plan, int n_sols, int n_init) {
   if (!plan || n_sols < 1 || n_init < 1) return 0;
   const Model& m = plan->m;
-  if (adjoint_supported(m)) return (size_t)n_sols * n_init * (m.H / 2) * m.W * sizeof(float2);
-  if (nd_supported(m)) return nd_kernel_grad_acc_bytes(m, n_sols, n_init);
-  return 0;
+  if (!adjoint_is_nd(*plan))
+    return adjoint_supported(m) ? (size_t)n_sols * n_init * (m.H / 2) * m.W * sizeof(float2) : 0;
+  return nd_supported(m) ? nd_kernel_grad_acc_bytes(m, n_sols, n_init) : 0;
 }
 
 int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t ws_bytes, void* stream) {
   if (!plan || !j) return fail(LGX_ERR_INVALID, "lgx_adjoint: null plan or job");
   const Model& m = plan->m;
-  if (!adjoint_supported(m) && !nd_supported(m))
+  if (!(adjoint_is_nd(*plan) ? nd_supported(m) : adjoint_supported(m)))
     return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint: no adjoint for this model");
   if (j->n_sols < 1 || j->n_init < 1 || j->steps < 1) return fail(LGX_ERR_INVALID, "lgx_adjoint: bad batch");
   if (!j->k_half || !j->gf_params || !j->weights || !j->T || !j->traj_cells || !j->traj_potential ||
@@ -788,10 +804,11 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   if (j->lambda_in == j->lambda_out) return fail(LGX_ERR_INVALID, "lgx_adjoint: lambda_out aliases lambda_in");
   if (j->clip_grad != LGX_CLIP_GRAD_STE && j->clip_grad != LGX_CLIP_GRAD_MASK)
     return fail(LGX_ERR_INVALID, "lgx_adjoint: unknown clip_grad %d", j->clip_grad);
+  const bool use_nd = adjoint_is_nd(*plan);
   const size_t need = lgx_adjoint_workspace_bytes(plan, j->n_sols, j->n_init);
   if (!ws || ws_bytes < need) return fail(LGX_ERR_WORKSPACE, "lgx_adjoint: workspace %zu < %zu bytes", ws_bytes, need);
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  if (!adjoint_supported(m)) {
+  if (use_nd) {
     // the general N-D adjoint: any channels and kernels, 2D and 3D worlds
     NdAdjoint a;
     a.n_sols = j->n_sols;
@@ -809,6 +826,7 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
     a.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
     a.grad_gf = j->grad_gf;
     a.grad_weights = j->grad_weights;
+    a.cells_after = j->cells_after;
     cudaError_t ce = launch_nd_adjoint(m, a, ws, st);
     if (ce != cudaSuccess) return cuda_fail(ce, "N-D adjoint segment");
     g_err.clear();
@@ -850,6 +868,7 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
   a.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
   a.grad_gf = j->grad_gf;
   a.grad_w = j->grad_weights;
+  a.cells_after = j->cells_after;
   if (resident) {
     // resident sizes: one persistent launch for the whole segment
     AdjResArgs r;
@@ -870,6 +889,7 @@ int lgx_adjoint(const lgx_plan* plan, const lgx_adjoint_job* j, void* ws, size_t
     r.lambda_out = j->lambda_out;
     r.gk = reinterpret_cast<float2*>(j->kernel_grad_acc);
     r.pacc = a.partial;
+    r.cells_after = j->cells_after;
     ce = cudaMemsetAsync(a.partial, 0, nw * 3 * sizeof(float), st);
     if (ce == cudaSuccess) ce = launch_adjoint_resident(m.H, r, st);
     if (ce == cudaSuccess) ce = launch_param_reduce(j->n_sols, j->n_init, 1, a.partial, j->grad_gf, j->grad_weights, st);
@@ -886,13 +906,13 @@ int lgx_adjoint_kernel_grad(const lgx_plan* plan, int n_sols, int n_init, const 
                             void* ws, size_t ws_bytes, void* stream) {
   if (!plan || !acc || !grad_kernel) return fail(LGX_ERR_INVALID, "lgx_adjoint_kernel_grad: null argument");
   const Model& m = plan->m;
-  if (!adjoint_supported(m) && !nd_supported(m))
+  if (lgx_adjoint_workspace_bytes(plan, 1, 1) == 0)
     return fail(LGX_ERR_UNSUPPORTED, "lgx_adjoint_kernel_grad: unsupported model");
   if (n_sols < 1 || n_init < 1) return fail(LGX_ERR_INVALID, "lgx_adjoint_kernel_grad: bad batch");
   const size_t need = lgx_adjoint_workspace_bytes(plan, n_sols, n_init);
   if (!ws || ws_bytes < need)
     return fail(LGX_ERR_WORKSPACE, "lgx_adjoint_kernel_grad: workspace %zu < %zu bytes", ws_bytes, need);
-  if (!adjoint_supported(m)) {
+  if (adjoint_is_nd(*plan)) {
     cudaError_t ce = launch_nd_kernel_grad(m, n_sols, n_init, reinterpret_cast<const float2*>(acc), grad_kernel, ws,
                                            static_cast<cudaStream_t>(stream));
     if (ce != cudaSuccess) return cuda_fail(ce, "kernel gradient");

@@ -221,6 +221,7 @@ struct NdAdjoint {
   float2* gk;                   // [nw, K, cells] kernel-gradient spectra (+=)
   float* grad_gf;               // [Ns, K, 2] (+=)
   float* grad_weights;          // [Ns, C, K] (+=)
+  const float* cells_after;     // [nw, C, cells] state after the last step, or null
 };
 size_t nd_adjoint_workspace_bytes(const Model& m, int n_sols, int n_init);
 size_t nd_kernel_grad_acc_bytes(const Model& m, int n_sols, int n_init);
@@ -252,6 +253,7 @@ struct AdjointSegment {
   float2* gk;                   // [nw, N/2, N] kernel-gradient accumulator (column domain)
   float* grad_gf;               // [Ns, 2]   +=
   float* grad_w;                // [Ns]      +=
+  const float* cells_after;     // [nw, N, N] state after the last step, or null
 };
 // Resident adjoint (adjoint_resident.cu): one launch per segment for the
 // resident sizes, lambda in registers across the segment's steps.
@@ -268,6 +270,7 @@ struct AdjResArgs {
   float* lambda_out;            // [nw, N, N]
   float2* gk;                   // [nw, N/2, N] kernel-gradient accumulator (+=)
   float* pacc;                  // [nw, 3] parameter partials (+=)
+  const float* cells_after;     // [nw, N, N] state after the last step, or null
 };
 bool adjoint_resident_supported(const Model& m);
 cudaError_t launch_adjoint_resident(int N, const AdjResArgs& a, cudaStream_t st);

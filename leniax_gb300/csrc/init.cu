@@ -51,18 +51,20 @@ struct InitArgs {
   const uint64_t* seeds;
   const float* gf_m;
   float* out;
+  const float* angles;  // [n_worlds, nb_init, res0, res1] or null (drawn from the seeds)
 };
 
 // Perlin value at (y, x) of init `i` (perlin.py:16-71 with leniax's
 // repeat-and-slice gradient lookup, which stays valid when the shape is not a
 // multiple of the periods).
-__device__ __forceinline__ float perlin_at(const InitArgs& a, uint64_t seed, int i, int y, int x) {
+__device__ __forceinline__ float perlin_at(const InitArgs& a, uint64_t seed, int world, int i, int y, int x) {
   const float gy = fmodf((float)y * ((float)a.res0 / (float)a.H), 1.f);
   const float gx = fmodf((float)x * ((float)a.res1 / (float)a.W), 1.f);
   const int y0 = y / a.d0, y1 = ((y + a.diff0) / a.d0) % a.res0;  // row a.res0 wraps to 0
   const int x0 = x / a.d1, x1 = ((x + a.diff1) / a.d1) % a.res1;
   auto grad = [&](int cy, int cx, float& c, float& s) {
-    const float ang = 6.283185307179586f * uniform01(seed, 1 + i, (uint64_t)cy * a.res1 + cx);
+    const float ang = a.angles ? __ldg(a.angles + (((size_t)world * a.nb_init + i) * a.res0 + cy) * a.res1 + cx)
+                               : 6.283185307179586f * uniform01(seed, 1 + i, (uint64_t)cy * a.res1 + cx);
     sincosf(ang, &s, &c);
   };
   float c00, s00, c10, s10, c01, s01, c11, s11;
@@ -98,7 +100,7 @@ __global__ void init_kernel(InitArgs a) {
   // Perlin (initializations.py:35-77): noise, per-init min / max normalisation, scaling
   float lo = 3.4e38f, hi = -3.4e38f;
   for (long c = threadIdx.x; c < cells; c += blockDim.x) {
-    const float v = perlin_at(a, seed, i, (int)(c / a.W), (int)(c % a.W));
+    const float v = perlin_at(a, seed, world, i, (int)(c / a.W), (int)(c % a.W));
     out[c] = v;
     lo = fminf(lo, v);
     hi = fmaxf(hi, v);
@@ -191,6 +193,7 @@ int lgx_init_cells(const lgx_init_job* j, void* ws, size_t ws_bytes, void* strea
   a.seeds = reinterpret_cast<const uint64_t*>(j->seeds);
   a.gf_m = j->gf_m;
   a.out = j->out;
+  a.angles = j->angles;
   a.res0 = a.res1 = a.d0 = a.d1 = 1;
   a.diff0 = a.diff1 = 0;
   int kr = 0;

@@ -440,6 +440,7 @@ __global__ void nd_reduce_kernel(NdTab t, int n_worlds, int n_init, int bpw, con
 struct AdjArgs {
   int n_worlds, n_init, clip_mask;
   const float* s;      // [nw, C, cells] state entering the step
+  const float* s_next;  // [nw, C, cells] state after the step, or null
   const float* u;      // [nw, K, cells] potentials of the step
   const float* lam;    // [nw, C, cells] dL/d(state after the step)
   float* lam_out;      // [nw, C, cells] direct part of dL/d(state before the step)
@@ -519,7 +520,8 @@ __global__ void __launch_bounds__(kNT) nd_adj_point_kernel(NdTab t, AdjArgs a) {
       const float sv = __ldg(a.s + off);
       float dsds, dsdf;  // d state' / d state and d state' / d field (core.py:245-319)
       if (t.state_fn == LGX_STATE_V1) {
-        const float n = sv + dt * f[c];
+        // mask: the forward's clip was inactive where its output lies strictly inside (0, 1)
+        const float n = a.s_next ? __ldg(a.s_next + off) : fmaf(dt, f[c], sv);
         const float cg = a.clip_mask ? ((n > 0.f && n < 1.f) ? 1.f : 0.f) : 1.f;  // mask or straight-through
         dsds = cg;
         dsdf = dt * cg;
@@ -799,6 +801,7 @@ cudaError_t launch_nd_adjoint(const Model& m, const NdAdjoint& j, void* ws, cuda
     a.n_init = j.n_init;
     a.clip_mask = j.clip_mask;
     a.s = j.traj_cells + (size_t)step * nw * plane_c;
+    a.s_next = step + 1 < j.steps ? a.s + (size_t)nw * plane_c : j.cells_after;
     a.u = j.traj_potential + (size_t)step * nw * plane_k;
     a.lam = lam_in;
     a.lam_out = lam_out;

@@ -31,6 +31,7 @@ from . import _lib
 from .core import UpdateFn, _require_cuda, _stream_handle, workspace
 
 CLIP_GRAD = {'ste': 0, 'mask': 1}
+ENGINES = ('auto', 'nd')  # 'nd': the general N-D engine for the forward segments and the adjoint
 
 
 def _bind(lib):
@@ -54,6 +55,8 @@ def _bind(lib):
     lib.lgx_kernel_spectrum_nd.restype = ctypes.c_int
     lib.lgx_adjoint_kernel_grad_acc_bytes.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
     lib.lgx_adjoint_kernel_grad_acc_bytes.restype = ctypes.c_size_t
+    lib.lgx_plan_set_adjoint_engine.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    lib.lgx_plan_set_adjoint_engine.restype = ctypes.c_int
     lib._lgx_grad_bound = True
     return lib
 
@@ -64,7 +67,7 @@ class AdjointJob(ctypes.Structure):
         ('n_sols', ctypes.c_int), ('n_init', ctypes.c_int), ('steps', ctypes.c_int), ('k_half', _fp),
         ('gf_params', _fp), ('weights', _fp), ('T', _fp), ('traj_cells', _fp), ('traj_potential', _fp),
         ('lambda_in', _fp), ('lambda_out', _fp), ('kernel_grad_acc', _fp), ('grad_gf', _fp), ('grad_weights', _fp),
-        ('clip_grad', ctypes.c_int)
+        ('clip_grad', ctypes.c_int), ('cells_after', _fp)
     ]
 
 
@@ -148,18 +151,20 @@ def ring_kernel(R: float, r: float, b: torch.Tensor, kf_slug: str, kf_params: Se
 # ---------------------------------------------------------------------------
 class LeniaRolloutFunction(torch.autograd.Function):
     """``final = LeniaRolloutFunction.apply(cells0, k_real, gf_params, weights,
-    T, update_fn, steps, checkpoint_every, clip_grad)``
+    T, update_fn, steps, checkpoint_every, clip_grad, engine)``
 
     cells0 ``[Ns, Ni, C, *world]``; k_real ``[Ns, K, *world]`` (or
     ``[Ns, *world]`` for one kernel): each true kernel's world-sized
     fftshifted real kernel in leniax's channel-sorted order; gf_params
     ``[Ns, K, 2]``; weights ``[Ns, C, K]``; T ``[Ns]``.  Returns the state
-    after ``steps`` steps ``[Ns, Ni, C, *world]``.
+    after ``steps`` steps ``[Ns, Ni, C, *world]``.  ``engine`` ``'auto'`` runs
+    the engines lgx_run and lgx_adjoint pick; ``'nd'`` runs the general N-D
+    engine for both (any model).
     """
 
     @staticmethod
     def forward(ctx, cells0, k_real, gf_params, weights, T, update_fn: UpdateFn, steps: int, checkpoint_every: int,
-                clip_grad: str):
+                clip_grad: str, engine: str = 'auto'):
         m = update_fn.model
         dev = cells0.device
         Ns, Ni = cells0.shape[:2]
@@ -175,24 +180,30 @@ class LeniaRolloutFunction(torch.autograd.Function):
         done = 0
         while done < steps:
             n = min(k, steps - done)
-            cur = _segment(update_fn, cur, k_half, gf, w, Tt, n, traj=False)
+            cur = _segment(update_fn, cur, k_half, gf, w, Tt, n, traj=False, engine=engine)
             done += n
             if done < steps:
                 ckpts.append(cur)
-        ctx.save_for_backward(k_half, gf, w, Tt, *ckpts)
+        ctx.save_for_backward(k_half, gf, w, Tt, *ckpts, cur)
         ctx.update_fn, ctx.steps, ctx.k, ctx.clip = update_fn, steps, k, CLIP_GRAD[clip_grad]
         ctx.k_shape = tuple(k_real.shape)
+        ctx.engine = engine
         return cur
 
     @staticmethod
     def backward(ctx, grad_final):
-        k_half, gf, w, Tt, *ckpts = ctx.saved_tensors
+        k_half, gf, w, Tt, *ckpts, final = ctx.saved_tensors
+        after = ckpts[1:] + [final]  # the state after each segment
         update_fn, steps, k = ctx.update_fn, ctx.steps, ctx.k
+        if steps == 0:
+            return grad_final, torch.zeros(ctx.k_shape, device=grad_final.device), torch.zeros_like(gf), \
+                torch.zeros_like(w), None, None, None, None, None, None
         m = update_fn.model
         dev = grad_final.device
         Ns, Ni = ckpts[0].shape[:2]
         lib = _bind(_lib.load())
         handle = m.plan.handle
+        _lib.check(lib.lgx_plan_set_adjoint_engine(handle, _lib.ENGINES[ctx.engine]))
         lam = grad_final.detach().float().contiguous().clone()
         lam_out = torch.empty_like(lam)
         acc_bytes = lib.lgx_adjoint_kernel_grad_acc_bytes(handle, Ns, Ni)
@@ -213,7 +224,8 @@ class LeniaRolloutFunction(torch.autograd.Function):
 
         def recompute(j):
             with torch.cuda.stream(side):
-                tr = _segment(update_fn, ckpts[j], k_half, gf, w, Tt, min(k, steps - seg_starts[j]), traj=True)
+                tr = _segment(update_fn, ckpts[j], k_half, gf, w, Tt, min(k, steps - seg_starts[j]), traj=True,
+                              engine=ctx.engine)
                 ev = torch.cuda.Event()
                 ev.record(side)
             return tr, ev
@@ -237,15 +249,16 @@ class LeniaRolloutFunction(torch.autograd.Function):
             job.kernel_grad_acc = acc.data_ptr()
             job.grad_gf, job.grad_weights = g_gf.data_ptr(), g_w.data_ptr()
             job.clip_grad = ctx.clip
+            job.cells_after = after[j].data_ptr()
             _lib.check(lib.lgx_adjoint(handle, job, ws.data_ptr(), ws.numel(), _stream_handle(dev)))
             lam, lam_out = lam_out, lam
         g_k = torch.empty((Ns, m.K) + m.world, dtype=torch.float32, device=dev)
         _lib.check(lib.lgx_adjoint_kernel_grad(handle, Ns, Ni, acc.data_ptr(), g_k.data_ptr(), ws.data_ptr(),
                                                ws.numel(), _stream_handle(dev)))
-        return lam, g_k.reshape(ctx.k_shape), g_gf, g_w, None, None, None, None, None
+        return lam, g_k.reshape(ctx.k_shape), g_gf, g_w, None, None, None, None, None, None
 
 
-def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj):
+def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj, engine='auto'):
     """n Euler steps from `cells` through lgx_run (no statistics needed)."""
     m = update_fn.model
     dev = cells.device
@@ -264,7 +277,7 @@ def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj):
         tc = torch.empty((n, Ns * Ni, m.C) + m.world, dtype=torch.float32, device=dev)
         tp = torch.empty((n, Ns * Ni, m.K) + m.world, dtype=torch.float32, device=dev)
         job.traj_cells, job.traj_potential = tc.data_ptr(), tp.data_ptr()
-    eng = _lib.ENGINES['auto']
+    eng = _lib.ENGINES[engine]
     ws = workspace(lib.lgx_run_workspace_bytes(m.plan.handle, Ns, Ni, n, eng), dev)
     job.engine = eng
     _lib.check(lib.lgx_run(m.plan.handle, job, ws.data_ptr(), ws.numel(), _stream_handle(dev)))
@@ -272,9 +285,11 @@ def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj):
 
 
 def rollout(cells0, k_real, gf_params, weights, T, update_fn: UpdateFn, steps: int, checkpoint_every: int = 16,
-            clip_grad: str = 'ste'):
+            clip_grad: str = 'ste', engine: str = 'auto'):
     """Differentiable rollout (see :class:`LeniaRolloutFunction`)."""
     if clip_grad not in CLIP_GRAD:
         raise ValueError("clip_grad must be 'ste' or 'mask'")
+    if engine not in ENGINES:
+        raise ValueError(f'engine must be one of {ENGINES}')
     return LeniaRolloutFunction.apply(cells0, k_real, gf_params, weights, T, update_fn, steps, checkpoint_every,
-                                      clip_grad)
+                                      clip_grad, engine)

@@ -11,6 +11,7 @@ leniax threads a JAX PRNG key through these functions; here a key is a
 not JAX's threefry stream (``next_key`` plays the role of ``jax.random.split``).
 """
 import ctypes
+import math
 from typing import List, Sequence, Tuple
 
 import torch
@@ -25,7 +26,7 @@ _MASK64 = (1 << 64) - 1
 class InitJobC(ctypes.Structure):
     _fields_ = [('kind', ctypes.c_int), ('n_worlds', ctypes.c_int), ('nb_init', ctypes.c_int), ('H', ctypes.c_int),
                 ('W', ctypes.c_int), ('R', ctypes.c_float), ('compressible', ctypes.c_int), ('seeds', ctypes.c_void_p),
-                ('gf_m', ctypes.c_void_p), ('out', ctypes.c_void_p)]
+                ('gf_m', ctypes.c_void_p), ('out', ctypes.c_void_p), ('angles', ctypes.c_void_p)]
 
 
 def _bind(lib):
@@ -46,11 +47,21 @@ def next_key(seed: int) -> int:
     return z ^ (z >> 31)
 
 
+def perlin_res(world_size: Sequence[int], R: float) -> Tuple[int, int]:
+    """Perlin periods of a world (initializations.py:57-58)."""
+    kr = math.ceil(R)
+    return int(world_size[0]) // (kr * 3), int(world_size[1]) // (kr * 2)
+
+
 def generate(kind: str, seeds: Sequence[int], nb_init: int, world_size: Sequence[int], R: float,
-             gf_m: Sequence[float] = None, compressible: bool = True, device=None) -> torch.Tensor:
+             gf_m: Sequence[float] = None, compressible: bool = True, device=None,
+             angles: torch.Tensor = None) -> torch.Tensor:
     """``[len(seeds), nb_init, H, W]`` float32 initial states on the GPU, one
     block of ``nb_init`` states per seed.  ``gf_m`` (the m of each world's
-    first kernel) sets the Perlin scaling."""
+    first kernel) sets the Perlin scaling.  ``angles`` ``[len(seeds), nb_init,
+    *perlin_res(world_size, R)]`` (radians) supplies the Perlin gradient field
+    as leniax's ``generate_perlin_noise_2d`` takes it (perlin.py:16-71);
+    without it the angles are drawn from the seeds."""
     if kind not in KINDS:
         raise ValueError(f'unknown initialisation {kind!r}')
     if len(world_size) != 2:
@@ -68,6 +79,14 @@ def generate(kind: str, seeds: Sequence[int], nb_init: int, world_size: Sequence
     job.kind, job.n_worlds, job.nb_init, job.H, job.W = KINDS[kind], n, int(nb_init), H, W
     job.R, job.compressible = float(R), int(bool(compressible))
     job.seeds, job.gf_m, job.out = sd.data_ptr(), gm.data_ptr(), out.data_ptr()
+    if angles is not None:
+        if kind == 'random_uniform':
+            raise ValueError('angles apply to the Perlin initialisations')
+        want = (n, int(nb_init)) + perlin_res(world_size, R)
+        if tuple(angles.shape) != want:
+            raise ValueError(f'angles has shape {tuple(angles.shape)}, expected {want}')
+        angles = angles.to(device=device, dtype=torch.float32).contiguous()
+        job.angles = angles.data_ptr()
     lib = _bind(_lib.load())
     nbytes = ctypes.c_size_t(0)
     _lib.check(lib.lgx_init_cells_workspace_bytes(ctypes.byref(job), ctypes.byref(nbytes)))

@@ -854,3 +854,81 @@ def create_init_cells(world_size, nb_channels, raw_cells):
         if len(c) != 0:
             cells = merge_cells(cells, c)
     return cells[np.newaxis]
+
+
+# ---------------------------------------------------------------------------
+# Initial states -- leniax/perlin.py, leniax/initializations.py, loader.py
+# ---------------------------------------------------------------------------
+def perlin_interpolant(t):
+    """perlin.py:12-13: 6t^5 - 15t^4 + 10t^3."""
+    return t * t * t * (t * (t * 6 - 15) + 10)
+
+
+def perlin_noise_2d(angles, shape, res):
+    """perlin.py:16-71 (generate_perlin_noise_2d): 2D Perlin noise of
+    ``angles.shape[0]`` states from the gradient angles ``[n, res0, res1]``.
+    The gradients at the lattice points are (cos a, sin a), wrapped by one
+    period, repeated ``shape // res`` times along each axis and sliced at the
+    four corners; ramps are the fractional grid coordinates (taken here as
+    ``arange(shape) * (res / shape) % 1``); the quintic interpolant blends the
+    four corner dot products; the result is scaled by sqrt(2)."""
+    angles = np.asarray(angles, dtype=np.float64)
+    grads = np.stack([np.cos(angles), np.sin(angles)], axis=-1)  # [n, r0, r1, 2]
+    grads = np.pad(grads, [(0, 0), (0, 1), (0, 1), (0, 0)], mode='wrap')
+    d = (shape[0] // res[0], shape[1] // res[1])
+    grads = grads.repeat(d[0], 1).repeat(d[1], 2)
+    diff = [grads.shape[1] - shape[0], grads.shape[2] - shape[1]]
+    g00 = grads[:, :-diff[0], :-diff[1]]
+    g10 = grads[:, diff[0]:, :-diff[1]]
+    g01 = grads[:, :-diff[0], diff[1]:]
+    g11 = grads[:, diff[0]:, diff[1]:]
+    gy = (np.arange(shape[0]) * (res[0] / shape[0])) % 1
+    gx = (np.arange(shape[1]) * (res[1] / shape[1])) % 1
+    grid = np.stack(np.meshgrid(gy, gx, indexing='ij'), axis=-1)[np.newaxis]  # [1, H, W, 2]
+    n00 = (np.stack([grid[..., 0], grid[..., 1]], -1) * g00).sum(3)
+    n10 = (np.stack([grid[..., 0] - 1, grid[..., 1]], -1) * g10).sum(3)
+    n01 = (np.stack([grid[..., 0], grid[..., 1] - 1], -1) * g01).sum(3)
+    n11 = (np.stack([grid[..., 0] - 1, grid[..., 1] - 1], -1) * g11).sum(3)
+    t = perlin_interpolant(grid)
+    n0 = n00 * (1 - t[..., 0]) + t[..., 0] * n10
+    n1 = n01 * (1 - t[..., 0]) + t[..., 0] * n11
+    return np.sqrt(2) * ((1 - t[..., 1]) * n0 + t[..., 1] * n1)
+
+
+def perlin_res(world_size, R):
+    """initializations.py:57-58: Perlin periods of a world."""
+    kr = math.ceil(R)
+    return [world_size[0] // (kr * 3), world_size[1] // (kr * 2)]
+
+
+def make_array_compressible(cells):
+    """loader.py:16-30: round to the NB_CHARS**2 - 1 grid (numpy's round is
+    half to even, as jnp.round)."""
+    max_val = NB_CHARS**2 - 1
+    return (np.round(cells * max_val).astype(np.int32) / max_val).astype(np.float32)
+
+
+def perlin_init(angles, world_size, R, m, compressible=True):
+    """initializations.py:35-77 given the gradient angles ``[nb_init, *res]``:
+    noise normalised per state to [0, 1], scaled by m + i / nb_init *
+    (min(1, 3 m) - m), made compressible.  -> ``[nb_init, 1, *world]``."""
+    nb_init = angles.shape[0]
+    cells = perlin_noise_2d(angles, tuple(world_size), tuple(perlin_res(world_size, R)))
+    cells = cells - cells.min(axis=(1, 2), keepdims=True)
+    cells = cells / cells.max(axis=(1, 2), keepdims=True)
+    hi = min(1, 3 * m)
+    scaling = np.array([m + i / nb_init * (hi - m) for i in range(nb_init)])[:, None, None]
+    cells = (cells * scaling)[:, np.newaxis]
+    return make_array_compressible(cells) if compressible else cells.astype(np.float32)
+
+
+def cropped_perlin_init(angles, world_size, R, m, compressible=True):
+    """initializations.py:80-116: the Perlin state's 2 ceil(R) square at rows
+    and columns [24, 24 + 2 ceil(R)) centred on a zero 128 x 128 world."""
+    cells = perlin_init(angles, world_size, R, m, compressible)
+    size = math.ceil(R) * 2
+    pad_left = (128 - size) // 2
+    pad_right = pad_left + 1 if pad_left * 2 + size != 128 else pad_left
+    out = np.pad(cells[:, :, 24:24 + size, 24:24 + size], ((0, 0), (0, 0), (pad_left, pad_right),
+                                                           (pad_left, pad_right)))
+    return make_array_compressible(out) if compressible else out

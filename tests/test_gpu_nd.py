@@ -79,7 +79,10 @@ def test_nd_single_step_matches_oracle(cuda, world, C, per, R, mean):
 @pytest.mark.parametrize('world,C,per,R,mean', [CASES[1], CASES[4]])
 def test_nd_run_scan_trajectories_and_stats(cuda, world, C, per, R, mean):
     # run_scan (runner.py:119-164) on the N-D engine: per-step cells, field,
-    # potential, the 12 statistics and N against the FP32 oracle
+    # potential, the 12 statistics and N against the oracle.  Statistics are
+    # held to 1e-4 or to 8x the oracle's own FP32-vs-FP64 spread, whichever is
+    # larger: mass_angle_speed is the angle of a centroid displacement, ill
+    # conditioned when the centroid barely moves
     dev = cuda
     kp = _model(world, C, per, R, mean, seed=4)
     K, mp = kernels.get_kernels_and_mapping([dict(p) for p in kp], list(world), C, R, True, dev)
@@ -95,10 +98,14 @@ def test_nd_run_scan_trajectories_and_stats(cuda, world, C, per, R, mean):
     assert np.abs(cs.cpu().numpy() - cs_o).max() < 2e-5
     assert np.abs(ps.cpu().numpy() - ps_o).max() < 5e-6
     assert np.abs(fs.cpu().numpy() - fs_o).max() < 5e-4
+    Ko64, mpo64 = O.get_kernels_and_mapping([dict(p) for p in kp], list(world), C, R, True, np.float64)
+    *_, st64 = O.run_scan(cells.astype(np.float64), Ko64, mpo64['gf_params'], mpo64['weights'], 5, steps, R,
+                          O.Model(mpo64, 'v1', mean))
     for k in statistics.STAT_KEYS:
-        a, b = st[k].cpu().numpy(), st_o[k]
+        a, b, b32 = st[k].cpu().numpy(), st64[k], st_o[k]
         atol = 8 / R**2 if k.endswith('volume') or k.endswith('density') else 1e-4
-        assert np.allclose(a, b, rtol=1e-4, atol=atol), (k, np.abs(a - b).max())
+        tol = np.maximum(atol + 1e-4 * np.abs(b), 8 * np.abs(b32 - b))
+        assert (np.abs(a - b) <= tol).all(), (k, np.abs(a - b).max())
     assert np.abs(st['N'].cpu().numpy() - st_o['N']).max() == 0
 
 

@@ -8,6 +8,7 @@ import torch
 
 from leniax_gb300 import helpers, initializations, kernels, qd, runner, statistics
 from leniax_gb300.constant import NB_CHARS
+from oracle import lenia_oracle as O
 
 pytestmark = pytest.mark.gpu
 
@@ -26,6 +27,33 @@ def qd_config(init_slug='perlin', steps=48, nb_init_search=4):
                      {'key': 'kernels_params.0.gf_params.1', 'domain': [0.01, 0.05], 'type': 'float'}],
         'phenotype': ['behaviours.mass', 'behaviours.mass_volume'],
     }
+
+
+@pytest.mark.parametrize('kind', ['perlin', 'cropped_perlin'])
+@pytest.mark.parametrize('world,R', [([128, 128], 13), ([96, 160], 7.5)])
+def test_perlin_states_match_oracle_for_a_given_gradient_field(cuda, kind, world, R):
+    # the device construction (noise, per-state normalisation, scaling,
+    # compressible rounding, crop) against the oracle's restatement of
+    # perlin.py:16-71 / initializations.py:35-116 from the same angles
+    if kind == 'cropped_perlin' and world != [128, 128]:
+        pytest.skip('cropped_perlin is defined on 128 x 128 worlds')
+    nb_init, ms = 5, [0.15, 0.3]
+    res = O.perlin_res(world, R)
+    rng = np.random.Generator(np.random.PCG64(9))
+    ang = (rng.random((2, nb_init) + tuple(res)) * 2 * np.pi).astype(np.float32)
+    ref_fn = O.perlin_init if kind == 'perlin' else O.cropped_perlin_init
+    for comp in (False, True):
+        got = initializations.generate(kind, [1, 2], nb_init, world, R, ms, compressible=comp,
+                                       angles=torch.from_numpy(ang)).cpu().numpy()
+        for w in range(2):
+            ref = ref_fn(ang[w].astype(np.float64), world, R, ms[w], compressible=comp)[:, 0]
+            if not comp:
+                assert np.abs(got[w] - ref).max() <= 2e-6, (kind, world, w)
+            else:
+                # a value within rounding distance of a half-quantum may round the other way
+                quantum = 1 / (NB_CHARS**2 - 1)
+                d = np.abs(got[w] - ref)
+                assert d.max() <= quantum * 1.001 and (d > 1e-6).mean() < 1e-3, (kind, world, w)
 
 
 @pytest.mark.parametrize('kind', ['random_uniform', 'perlin', 'cropped_perlin'])
