@@ -300,6 +300,7 @@ def run_ours(args, rank, world_size):
     plain_value = plain['plain']
 
     adjoint = measure_adjoint(dev, fp32_peak=fp32_peak)
+    adjoint['variant_3d'] = measure_adjoint_3d(dev)
     multichannel = measure_multichannel(dev, fp32_peak=fp32_peak)
     uneven = measure_uneven(dev, fp32_peak=fp32_peak)
 
@@ -410,6 +411,51 @@ def measure_adjoint(dev, worlds=64, steps=256, ckpt=16, reps=3, fp32_peak=None):
             'b': bool(torch.isfinite(b.grad).all())
         }
     }
+
+
+def measure_adjoint_3d(dev, size=48, steps=256, ckpt=16, reps=2):
+    """The differentiation workload's 3D variant: one 48x48x48 world (bump
+    kernel R=8, gaussian growth m=0.15 s=0.03, dt=0.1, uniform[0,1) central
+    16^3 patch), 256 steps with checkpoints every 16, MSE of the final state
+    against a target made at m=0.16 s=0.033; gradients with respect to the
+    initial cells, the kernel and (m, s) on the general N-D engine (forward
+    and adjoint).  fwd+bwd world-steps/s timed with CUDA events."""
+    import torch
+    from leniax_gb300 import grad as lgrad
+    from leniax_gb300 import helpers, kernels
+    R, T = 8.0, 10.0
+    kp = [dict(KPARAMS[0], gf_params=[0.15, 0.03])]
+    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in kp], [size] * 3, 1, R, True, dev)
+    upd = helpers.build_update_fn(K.shape, mp)
+    rng = np.random.Generator(np.random.PCG64(5))
+    c = np.zeros((1, 1, 1, size, size, size), np.float32)
+    lo, p = (size - size // 3) // 2, size // 3
+    c[..., lo:lo + p, lo:lo + p, lo:lo + p] = rng.random((p, p, p), dtype=np.float32)
+    cells = torch.from_numpy(c).to(dev)
+    kr = lgrad.ring_kernel(R, 1.0, torch.tensor([1.0], device=dev), 'gauss_bump', [1.0], [size] * 3)[None]
+    with torch.no_grad():
+        target = lgrad.rollout(cells, kr, torch.tensor([[[0.16, 0.033]]], device=dev), torch.ones((1, 1, 1), device=dev),
+                               torch.tensor([T]), upd, steps, ckpt)
+    times = []
+    for i in range(reps + 1):
+        c0 = cells.clone().requires_grad_(True)
+        k0 = kr.clone().requires_grad_(True)
+        gf = torch.tensor([[[0.15, 0.03]]], device=dev, requires_grad=True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        fin = lgrad.rollout(c0, k0, gf, torch.ones((1, 1, 1), device=dev), torch.tensor([T]), upd, steps, ckpt)
+        ((fin - target)**2).mean().backward()
+        e1.record()
+        torch.cuda.synchronize()
+        if i > 0:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    t = pystats.median(times)
+    return {'metric': 'fwd+bwd world-steps/s', 'value': steps / t, 'unit': 'world-steps/s', 'seconds': t,
+            'engine': 'nd (forward and adjoint)',
+            'config': f'1 world x {size}^3, {steps} steps, checkpoint every {ckpt}, grads wrt cells0, kernel, m, s',
+            'grads_finite': bool(torch.isfinite(c0.grad).all() and torch.isfinite(k0.grad).all()
+                                 and torch.isfinite(gf.grad).all())}
 
 
 def _timed(fn, stream, flush, reps):
@@ -538,7 +584,9 @@ def profile_case(args):
       uneven256 / uneven3d : --profile-worlds worlds of 256x256 / 64x64x64 in one uneven-batch launch
                      (--profile-steps steps)
       adjoint      : the differentiation workload (forward + backward) on --profile-worlds worlds of
-                     128x128 over --profile-steps steps, checkpoints every 16"""
+                     128x128 over --profile-steps steps, checkpoints every 16
+      nd48         : --profile-worlds worlds of 48x48x48 (bump kernel R=8, gaussian growth) on the
+                     general N-D engine, --profile-steps steps with statistics"""
     import torch
     from leniax_gb300 import helpers, kernels, runner, statistics
     dev = torch.device('cuda', 0)
@@ -569,6 +617,22 @@ def profile_case(args):
     elif name == 'adjoint':
         r = measure_adjoint(dev, worlds=nw, steps=ns, reps=1)
         info = {'fwd_bwd_world_steps_per_s': r['value']}
+    elif name == 'nd48':
+        size, Rn = 48, 8.0
+        kp = [dict(KPARAMS[0], gf_params=[0.15, 0.03])]
+        K, mp = kernels.get_kernels_and_mapping([dict(p) for p in kp], [size] * 3, 1, Rn, True, dev)
+        upd = helpers.build_update_fn(K.shape, mp)
+        stats_fn = statistics.ComputeStatsFn([size] * 3, Rn, T_RATE)
+        rng = np.random.Generator(np.random.PCG64(5))
+        c = np.zeros((1, nw, 1, size, size, size), np.float32)
+        lo, p = (size - size // 3) // 2, size // 3
+        c[..., lo:lo + p, lo:lo + p, lo:lo + p] = rng.random((nw, 1, p, p, p), dtype=np.float32)
+        cells = torch.from_numpy(c).to(dev)
+        gf, w, Tt = mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([T_RATE])
+        for _ in range(2):
+            sd, fin = runner.run_scan_mem_optimized(None, cells, K[None], gf, w, Tt, ns, Rn, upd, stats_fn,
+                                                    with_box=True)
+        info = {'mean_N_box': float(sd['N_box'].mean())}
     else:
         from leniax_gb300 import batch as lbatch
         from leniax_gb300 import workloads
@@ -602,7 +666,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--profile-case', nargs='?', const='resident', default=None,
-                    choices=['resident', 'multichannel', 'uneven256', 'uneven3d', 'adjoint'],
+                    choices=['resident', 'multichannel', 'uneven256', 'uneven3d', 'adjoint', 'nd48'],
                     help='profiling case for ncu: one warm-up and one rollout of --profile-worlds worlds x '
                          '--profile-steps Euler steps of the named workload, nothing else')
     ap.add_argument('--profile-worlds', type=int, default=2048)
