@@ -105,21 +105,33 @@ __global__ void __launch_bounds__(kNT) nd_pass_kernel(Pass a, GPlan p) {
   }
   fill_twiddles(tw, L);
   const int pts = nl * L;
-  for (int idx = threadIdx.x; idx < pts; idx += blockDim.x) {
-    int l, j;
-    if (a.I == 1) {
-      l = idx / L;
-      j = idx - l * L;
-    } else {
-      j = idx / nl;
-      l = idx - j * nl;
+  // kLoadBatch independent global loads in flight per thread before their
+  // shared-memory stores (one load per iteration would serialise on latency)
+  constexpr int kLoadBatch = 8;
+  for (int base = threadIdx.x; base < pts; base += kLoadBatch * blockDim.x) {
+    float2 v[kLoadBatch];
+    int dst[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = base + u * blockDim.x;
+      int l, j;
+      if (a.I == 1) {
+        l = idx / L;
+        j = idx - l * L;
+      } else {
+        j = idx / nl;
+        l = idx - j * nl;
+      }
+      dst[u] = idx < pts ? l * L + j : -1;
+      v[u] = make_float2(0.f, 0.f);
+      if (idx < pts && l < lines) {
+        const long off = (a.I == 1 ? (g0 + l) * a.gstride : g0 * a.gstride + i0 + l) + (long)j * a.stride;
+        v[u] = a.in_real ? make_float2(__ldg(a.src_real + off), 0.f) : a.data[off];
+      }
     }
-    float2 v = make_float2(0.f, 0.f);
-    if (l < lines) {
-      const long off = (a.I == 1 ? (g0 + l) * a.gstride : g0 * a.gstride + i0 + l) + (long)j * a.stride;
-      v = a.in_real ? make_float2(__ldg(a.src_real + off), 0.f) : a.data[off];
-    }
-    A[l * L + j] = v;
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u)
+      if (dst[u] >= 0) A[dst[u]] = v[u];
   }
   __syncthreads();
   const float2* res = fft_line<INV>(A, B, p, tw, nl);
