@@ -586,7 +586,9 @@ def profile_case(args):
       adjoint      : the differentiation workload (forward + backward) on --profile-worlds worlds of
                      128x128 over --profile-steps steps, checkpoints every 16
       nd48         : --profile-worlds worlds of 48x48x48 (bump kernel R=8, gaussian growth) on the
-                     general N-D engine, --profile-steps steps with statistics"""
+                     general N-D engine, --profile-steps steps with statistics
+      adjoint3d    : the differentiation workload's 3D variant (one 48x48x48 world, forward + backward
+                     on the N-D engine) over --profile-steps steps, checkpoints every 16"""
     import torch
     from leniax_gb300 import helpers, kernels, runner, statistics
     dev = torch.device('cuda', 0)
@@ -616,6 +618,9 @@ def profile_case(args):
         info = {'mean_N': float(sd['N'].float().mean())}
     elif name == 'adjoint':
         r = measure_adjoint(dev, worlds=nw, steps=ns, reps=1)
+        info = {'fwd_bwd_world_steps_per_s': r['value']}
+    elif name == 'adjoint3d':
+        r = measure_adjoint_3d(dev, steps=ns, reps=1)
         info = {'fwd_bwd_world_steps_per_s': r['value']}
     elif name == 'nd48':
         size, Rn = 48, 8.0
@@ -666,7 +671,7 @@ def main():
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--profile-case', nargs='?', const='resident', default=None,
-                    choices=['resident', 'multichannel', 'uneven256', 'uneven3d', 'adjoint', 'nd48'],
+                    choices=['resident', 'multichannel', 'uneven256', 'uneven3d', 'adjoint', 'nd48', 'adjoint3d'],
                     help='profiling case for ncu: one warm-up and one rollout of --profile-worlds worlds x '
                          '--profile-steps Euler steps of the named workload, nothing else')
     ap.add_argument('--profile-worlds', type=int, default=2048)

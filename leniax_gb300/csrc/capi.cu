@@ -165,8 +165,8 @@ NdLayout nd_layout(const Model& m, int n_sols, int n_init, int steps) {
   off += al256(nw * m.C * m.cells * sizeof(float));
   L.sb = off;
   off += al256(nw * m.C * m.cells * sizeof(float));
-  L.shift = off;
-  off += al256(nw * 3 * sizeof(int));
+  L.shift = off;  // [nw, 3] carried shifts, then [nw] block counters of the N-D epilogue
+  off += al256(nw * 4 * sizeof(int));
   L.step = off;
   off += nd_step_workspace_bytes(m, (int)nw);
   L.end = off;
@@ -356,19 +356,15 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     float* sb = reinterpret_cast<float*>(base + L.sb);
     int* shift = reinterpret_cast<int*>(base + L.shift);
     ce = launch_nd_prepare(m, j->n_sols, reinterpret_cast<const float2*>(j->k_half), kf, st);
-    if (ce == cudaSuccess) ce = cudaMemsetAsync(shift, 0, (size_t)nw * 3 * sizeof(int), st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(shift, 0, (size_t)nw * 4 * sizeof(int), st);
     if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
     const long raws = raw_stride(m.C);
     const float* cur = j->cells0;
     if (j->main_events[0]) cudaEventRecord(static_cast<cudaEvent_t>(j->main_events[0]), st);
     for (int s = 0; s < j->steps; ++s) {
       float* out = (s == j->steps - 1 && j->final_cells) ? j->final_cells : ((s & 1) ? sb : sa);
-      if (j->traj_cells) {
-        ce = cudaMemcpyAsync(j->traj_cells + (size_t)s * nw * plane, cur, (size_t)nw * plane * sizeof(float),
-                             cudaMemcpyDeviceToDevice, st);
-        if (ce != cudaSuccess) return cuda_fail(ce, "trajectory copy");
-      }
       NdStep ns;
+      ns.state_copy = j->traj_cells ? j->traj_cells + (size_t)s * nw * plane : nullptr;
       ns.m = &m;
       ns.n_worlds = nw;
       ns.n_init = j->n_init;
@@ -388,6 +384,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
       ns.raw_world_stride = raws;
       ns.raw_sol_stride = (long)j->steps * j->n_init * raws;
       ns.shift = shift;
+      ns.done = shift + 3 * nw;
       ns.ws = base + L.step;
       ce = launch_nd_step(ns, st);
       if (ce != cudaSuccess) return cuda_fail(ce, "N-D step");
@@ -657,9 +654,11 @@ int lgx_update(const lgx_plan* plan, int n, const float* state, const float* k_h
     int* shift = reinterpret_cast<int*>(base + L.shift);
     ce = cudaMemsetAsync(ws, 0, sizeof(int), st);
     if (ce == cudaSuccess) ce = launch_nd_prepare(m, 1, reinterpret_cast<const float2*>(k_half), kf, st);
-    if (ce == cudaSuccess) ce = cudaMemsetAsync(shift, 0, (size_t)n * 3 * sizeof(int), st);
+    if (ce == cudaSuccess) ce = cudaMemsetAsync(shift, 0, (size_t)n * 4 * sizeof(int), st);
     if (ce != cudaSuccess) return cuda_fail(ce, "prepare spectrum");
     NdStep ns;
+    ns.state_copy = nullptr;
+    ns.done = shift + 3 * n;
     ns.m = &m;
     ns.n_worlds = n;
     ns.n_init = n;

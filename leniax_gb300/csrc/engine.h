@@ -181,7 +181,7 @@ cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const f
 // mixed-radix line passes over full complex spectra in HBM (nd.cu).
 bool nd_side_ok(int n);
 bool nd_supported(const Model& m);
-int nd_blocks_per_world(const Model& m);
+int nd_blocks_per_world(const Model& m, long n_worlds);
 // Prepared spectra [Ns, C, max_k, cells] complex: the Hermitian half
 // [Ns, C, max_k, D, H, W/2+1] extended to the full spectrum, scaled by 1/cells.
 size_t nd_prepared_bytes(const Model& m, int n_sols);
@@ -204,6 +204,8 @@ struct NdStep {
   float* raw;           // raw moments of this step, or null
   long raw_world_stride, raw_sol_stride;
   int* shift;           // [n_worlds, 3] carried torus shift (read, then advanced)
+  int* done;            // [n_worlds] per-world block counters, zero before the first step (kept zero)
+  float* state_copy;    // [n_worlds, C, cells] copy of the entering state (trajectory), or null
   void* ws;             // nd_step_workspace_bytes
 };
 size_t nd_step_workspace_bytes(const Model& m, int n_worlds);

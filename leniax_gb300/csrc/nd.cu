@@ -38,6 +38,10 @@ namespace {
 
 constexpr int kNT = 256;          // threads per block
 constexpr int kMaxPts = 4096;     // complex points of one pass tile (two buffers in shared memory)
+// Launches smaller than this many blocks (four on each of GB300's 152 SMs)
+// get smaller tiles / chunks so that one small world still spreads over the
+// whole GPU; large batches keep the full-size tiles.
+constexpr long kFillBlocks = 4 * 152;
 constexpr int kRawMax = RAW_CM + kMaxChannels;
 
 struct NdTab {  // kernel table of a model, passed by value
@@ -201,7 +205,12 @@ cudaError_t run_pass(bool inv, int axis, const NdTab& t, long planes, float2* da
   const GPlan p = make_plan(a.L);
   if (p.stages == 0) return cudaErrorInvalidValue;
   const int cap = std::max(1, kMaxPts / a.L);
-  a.nl = (int)std::min<long>(cap, a.I == 1 ? a.G : a.I);
+  // lines per tile: the full tile, or fewer when the pass has too few lines
+  // to fill the GPU (at least 4 adjacent lines of a strided pass, so each
+  // load still covers a 32-byte sector)
+  const long fill = (a.G * a.I + kFillBlocks - 1) / kFillBlocks;
+  const long want = std::max<long>(a.I == 1 ? 1 : 4, fill);
+  a.nl = (int)std::min<long>(std::min<long>(cap, want), a.I == 1 ? a.G : a.I);
   const long tiles = a.I == 1 ? (a.G + a.nl - 1) / a.nl : a.G * ((a.I + a.nl - 1) / a.nl);
   const size_t smem = (size_t)(a.L + 2 * a.nl * a.L) * sizeof(float2);
   cudaError_t e = allow_pass_smem();
@@ -271,19 +280,191 @@ __global__ void nd_half_kernel(long planes, int D, int H, int W, const float2* _
 
 inline int grid_for(long total) { return (int)std::max(1L, std::min<long>((total + kNT - 1) / kNT, 1L << 16)); }
 
-// P[w, k] = S[w, c_in(k)] * prepared[sol(w), c_in(k), slot(k)]
-__global__ void nd_multiply_kernel(NdTab t, int n_worlds, int n_init, const float2* __restrict__ S,
-                                   const float2* __restrict__ kf, long kf_sol_stride, float2* __restrict__ P) {
-  const long total = (long)n_worlds * t.K * t.cells;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const long cell = i % t.cells;
-    const long wk = i / t.cells;
-    const int k = (int)(wk % t.K), w = (int)(wk / t.K);
-    const int sol = w / n_init, c = t.cin[k];
-    const float2 s = S[((long)w * t.C + c) * t.cells + cell];
-    const float2 kk = __ldg(kf + sol * kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + cell);
-    P[i] = cmul(s, kk);
+// ------------------------------------------------------------------ fused convolution pass
+// Along the last world axis (z in 3D, y in 2D) line i of a plane holds the
+// points i + j I, j < L, with I = cells / L lines per plane.  One block takes
+// a tile of nl adjacent lines of one world: the forward transform along the
+// axis of each channel, the spectrum products, the inverse transform of each
+// product -- the last forward pass, the multiply and the first inverse pass
+// in one launch, with the channel spectra kept in shared memory.  The
+// arithmetic is that of the separate passes, in the same order.
+struct ConvArgs {
+  int n_init, L, nl, tiles;  // points per line, lines per tile, tiles per plane
+  long I;                    // lines per plane (= point stride along the axis)
+  const float2* kf;          // prepared full spectra [Ns, C, max_k, cells]
+  long kf_sol_stride;
+  const float2* S;           // forward: [nw, C] planes, the other axes transformed
+  float2* P;                 // forward: [nw, K] product planes out
+  const float2* A;           // adjoint: [nw, K] planes of a = dL/du, the other axes transformed
+  float2* gk;                // adjoint: [nw, K] kernel-gradient spectra (accumulated)
+  float2* Q;                 // adjoint: [nw, C] correlation planes out
+};
+
+// nl lines of a plane (points src[l + j I]) into a line-major tile (lines
+// past `lines` read as zero); kLoadBatch loads in flight per thread
+__device__ __forceinline__ void load_lines(float2* dst, const float2* __restrict__ src, long I, int L, int nl,
+                                           int lines) {
+  const int pts = nl * L;
+  constexpr int kLoadBatch = 8;
+  for (int base = threadIdx.x; base < pts; base += kLoadBatch * blockDim.x) {
+    float2 v[kLoadBatch];
+    int d[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = base + u * blockDim.x;
+      const int j = idx / nl, l = idx - j * nl;
+      d[u] = idx < pts ? l * L + j : -1;
+      v[u] = make_float2(0.f, 0.f);
+      if (idx < pts && l < lines) v[u] = src[l + (long)j * I];
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u)
+      if (d[u] >= 0) dst[d[u]] = v[u];
   }
+}
+
+__device__ __forceinline__ void store_lines(float2* __restrict__ dst, const float2* src, long I, int L, int nl,
+                                            int lines) {
+  for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
+    const int j = idx / nl, l = idx - j * nl;
+    if (l < lines) dst[l + (long)j * I] = src[l * L + j];
+  }
+}
+
+// forward: P[w, k] = IFFT_axis(FFT_axis(S[w, c_in(k)]) * prepared[sol, c_in(k), slot(k)])
+__global__ void __launch_bounds__(kNT) nd_conv_kernel(NdTab t, ConvArgs a, GPlan p) {
+  extern __shared__ __align__(16) float2 ndsm[];
+  const int L = a.L, nl = a.nl, pts = nl * L;
+  float2* tw = ndsm;
+  float2* Sc = tw + L;  // [C][pts] channel spectra along the axis
+  float2* A = Sc + (size_t)t.C * pts;
+  float2* B = A + pts;
+  const int w = blockIdx.x / a.tiles;
+  const long i0 = (long)(blockIdx.x % a.tiles) * nl;
+  const int lines = (int)min((long)nl, a.I - i0);
+  const int sol = w / a.n_init;
+  fill_twiddles(tw, L);
+  for (int c = 0; c < t.C; ++c) {
+    load_lines(A, a.S + ((long)w * t.C + c) * t.cells + i0, a.I, L, nl, lines);
+    __syncthreads();
+    const float2* r = fft_line<false>(A, B, p, tw, nl);
+    for (int x = threadIdx.x; x < pts; x += blockDim.x) Sc[c * pts + x] = r[x];
+    __syncthreads();
+  }
+  for (int k = 0; k < t.K; ++k) {
+    const int c = t.cin[k];
+    load_lines(A, a.kf + sol * a.kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + i0, a.I, L, nl, lines);
+    __syncthreads();
+    for (int x = threadIdx.x; x < pts; x += blockDim.x) A[x] = cmul(Sc[c * pts + x], A[x]);
+    __syncthreads();
+    const float2* r = fft_line<true>(A, B, p, tw, nl);
+    store_lines(a.P + ((long)w * t.K + k) * t.cells + i0, r, a.I, L, nl, lines);
+    __syncthreads();
+  }
+}
+
+// adjoint: with A_k = FFT(a_k), S_c = FFT(state_c) along the axis,
+// gk[w, k] += A_k conj(S_c_in(k)) and Q[w, c] = IFFT_axis(sum_{k: c_in(k) = c}
+// A_k conj(prepared_k)) -- the last forward passes of a and of the state, the
+// spectral products and the first inverse pass of Q in one launch
+__global__ void __launch_bounds__(kNT) nd_adj_conv_kernel(NdTab t, ConvArgs a, GPlan p) {
+  extern __shared__ __align__(16) float2 ndsm[];
+  const int L = a.L, nl = a.nl, pts = nl * L;
+  float2* tw = ndsm;
+  float2* Sc = tw + L;                    // [C][pts]
+  float2* Qc = Sc + (size_t)t.C * pts;    // [C][pts]
+  float2* A = Qc + (size_t)t.C * pts;
+  float2* B = A + pts;
+  const int w = blockIdx.x / a.tiles;
+  const long i0 = (long)(blockIdx.x % a.tiles) * nl;
+  const int lines = (int)min((long)nl, a.I - i0);
+  const int sol = w / a.n_init;
+  fill_twiddles(tw, L);
+  for (int c = 0; c < t.C; ++c) {
+    load_lines(A, a.S + ((long)w * t.C + c) * t.cells + i0, a.I, L, nl, lines);
+    __syncthreads();
+    const float2* r = fft_line<false>(A, B, p, tw, nl);
+    for (int x = threadIdx.x; x < pts; x += blockDim.x) {
+      Sc[c * pts + x] = r[x];
+      Qc[c * pts + x] = make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+  }
+  for (int k = 0; k < t.K; ++k) {
+    const int c = t.cin[k];
+    load_lines(A, a.A + ((long)w * t.K + k) * t.cells + i0, a.I, L, nl, lines);
+    __syncthreads();
+    const float2* r = fft_line<false>(A, B, p, tw, nl);
+    float2* o = r == A ? B : A;  // the free buffer takes the prepared spectrum's lines
+    load_lines(o, a.kf + sol * a.kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + i0, a.I, L, nl,
+               lines);
+    __syncthreads();
+    float2* g = a.gk + ((long)w * t.K + k) * t.cells + i0;
+    for (int idx = threadIdx.x; idx < pts; idx += blockDim.x) {
+      const int j = idx / nl, l = idx - j * nl;
+      if (l >= lines) continue;
+      const int x = l * L + j;
+      const float2 ak = r[x];
+      float2* gp = g + l + (long)j * a.I;
+      *gp = cadd(*gp, cmulc(ak, Sc[c * pts + x]));
+      Qc[c * pts + x] = cadd(Qc[c * pts + x], cmulc(ak, o[x]));
+    }
+    __syncthreads();
+  }
+  for (int c = 0; c < t.C; ++c) {
+    for (int x = threadIdx.x; x < pts; x += blockDim.x) A[x] = Qc[c * pts + x];
+    __syncthreads();
+    const float2* r = fft_line<true>(A, B, p, tw, nl);
+    store_lines(a.Q + ((long)w * t.C + c) * t.cells + i0, r, a.I, L, nl, lines);
+    __syncthreads();
+  }
+}
+
+// Tile and shared memory of a fused convolution pass; `bufs` complex tiles
+// besides the twiddles (C + 2 forward, 2C + 2 adjoint).
+constexpr long kConvSmemPts = 96 * 1024 / 8;  // 96 KB of tiles: two blocks per SM
+
+cudaError_t run_conv(bool adjoint, const NdTab& t, long nw, ConvArgs a, cudaStream_t st) {
+  a.L = t.nd == 3 ? t.D : t.H;
+  a.I = t.cells / a.L;
+  const GPlan p = make_plan(a.L);
+  if (p.stages == 0) return cudaErrorInvalidValue;
+  const long bufs = adjoint ? 2L * t.C + 2 : (long)t.C + 2;
+  const long cap_pts = std::min<long>(kMaxPts, (kConvSmemPts - a.L) / bufs);
+  const long cap = std::max<long>(1, cap_pts / a.L);
+  const long fill = (nw * a.I + kFillBlocks - 1) / kFillBlocks;
+  a.nl = (int)std::min<long>(std::min<long>(cap, std::max<long>(4, fill)), a.I);
+  a.tiles = (int)((a.I + a.nl - 1) / a.nl);
+  const size_t smem = (size_t)(a.L + bufs * a.nl * a.L) * sizeof(float2);
+  const long blocks = nw * a.tiles;
+  if (blocks >= (1L << 31)) return cudaErrorInvalidConfiguration;
+  cudaError_t e;
+  if (adjoint) {
+    e = cudaFuncSetAttribute(nd_adj_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    nd_adj_conv_kernel<<<(unsigned)blocks, kNT, smem, st>>>(t, a, p);
+  } else {
+    e = cudaFuncSetAttribute(nd_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    nd_conv_kernel<<<(unsigned)blocks, kNT, smem, st>>>(t, a, p);
+  }
+  return cudaGetLastError();
+}
+
+// The axis passes before and after the fused one: forward x (real input)
+// and, in 3D, y; inverse y (3D) and x (real part out).
+cudaError_t forward_real_head(const NdTab& t, long planes, const float* src, float2* dst, cudaStream_t st) {
+  cudaError_t e = run_pass(false, 0, t, planes, dst, src, nullptr, false, 1.f, st);
+  if (e == cudaSuccess && t.D > 1) e = run_pass(false, 1, t, planes, dst, nullptr, nullptr, false, 1.f, st);
+  return e;
+}
+
+cudaError_t inverse_real_tail(const NdTab& t, long planes, float2* data, float* dst, bool accumulate, float scale,
+                              cudaStream_t st) {
+  cudaError_t e = cudaSuccess;
+  if (t.D > 1) e = run_pass(true, 1, t, planes, data, nullptr, nullptr, false, 1.f, st);
+  if (e == cudaSuccess) e = run_pass(true, 0, t, planes, data, nullptr, dst, accumulate, scale, st);
+  return e;
 }
 
 // ------------------------------------------------------------------ forward epilogue
@@ -298,8 +479,12 @@ struct EpiArgs {
   long w_sol_stride;
   const float* dt;
   float* field_out;     // [nw, C, cells] or null
-  const int* shift;     // [nw, 3]
+  float* state_copy;    // [nw, C, cells] copy of the entering state (trajectory), or null
+  int* shift;           // [nw, 3] read by every block, advanced by the world's last block
+  int* done;            // [nw] blocks finished this step (zero between steps)
   float* partial;       // [nw, bpw, RAWS]
+  float* raw;           // the step's raw record, or null
+  long raw_sol_stride, raw_init_stride;
 };
 
 // per-cell centred coordinate on one axis (statistics.py:64-81 on the world
@@ -361,6 +546,7 @@ __global__ void __launch_bounds__(kNT) nd_epilogue_kernel(NdTab t, EpiArgs a) {
       const float sv = __ldg(a.state + off);
       a.state_out[off] = state_fn(t.state_fn, sv, f, dt);
       if (a.field_out) a.field_out[off] = f;
+      if (a.state_copy) a.state_copy[off] = sv;
       const float fp = fmaxf(f, 0.f);
       m00 += sv;
       g00 += fp;
@@ -407,44 +593,49 @@ __global__ void __launch_bounds__(kNT) nd_epilogue_kernel(NdTab t, EpiArgs a) {
   }
   __syncthreads();
   const int RAWS = raw_stride(C);
+  float* pw = a.partial + (long)w * a.bpw * RAWS;
   if (threadIdx.x < RAWS) {
     float s = 0.f;
     for (int i = 0; i < NWARP; ++i) s += red[i][threadIdx.x];
     if (threadIdx.x == RAW_BORDER) s = s > 0.f ? 1.f : 0.f;
-    a.partial[((long)w * a.bpw + b) * RAWS + threadIdx.x] = s;
+    pw[b * RAWS + threadIdx.x] = s;
+    __threadfence();
   }
-}
-
-// Per world: block moments -> the step's raw record (with the shift that
-// centred it), then the carried shift advances by the integer part of the
-// centred-frame centroid (statistics.py:117-124).
-__global__ void nd_reduce_kernel(NdTab t, int n_worlds, int n_init, int bpw, const float* __restrict__ partial,
-                                 float* __restrict__ raw, long raw_sol_stride, long raw_init_stride,
-                                 int* __restrict__ shift) {
-  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int lane = threadIdx.x & 31;
-  if (w >= n_worlds) return;
-  const int RAWS = raw_stride(t.C);
-  const int sol = w / n_init, init = w - sol * n_init;
-  float* rw = raw ? raw + sol * raw_sol_stride + init * raw_init_stride : nullptr;
-  const int sh[3] = {shift[3 * w], shift[3 * w + 1], shift[3 * w + 2]};
-  float m00 = 0.f, mx[3] = {0.f, 0.f, 0.f};
+  // The world's last block to finish (a ticket on the world's counter; no
+  // block waits) reduces all of the world's block moments in a fixed order
+  // into the step's raw record (with the shift that centred it), then
+  // advances the carried shift by the integer part of the centred-frame
+  // centroid (statistics.py:117-124).
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(a.done + w, 1) == a.bpw - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
   for (int s = lane; s < RAWS; s += 32) {
     float v = 0.f;
-    for (int b = 0; b < bpw; ++b) v += partial[((long)w * bpw + b) * RAWS + s];
-    if (s == RAW_BORDER) v = v > 0.f ? 1.f : 0.f;
-    if (s >= RAW_SHIFT && s < RAW_SHIFT + 3) v = (float)sh[s - RAW_SHIFT];
-    if (rw) rw[s] = v;
+    for (int bb = wid; bb < a.bpw; bb += NWARP) v += __ldcg(pw + bb * RAWS + s);
+    red[wid][s] = v;
   }
-  __syncwarp();
-  if (lane == 0) {
-    for (int b = 0; b < bpw; ++b) {
-      const float* pp = partial + ((long)w * bpw + b) * RAWS;
-      m00 += pp[RAW_M00];
-      for (int i = 0; i < 3; ++i) mx[i] += pp[RAW_MX + i];
-    }
-    const int n[3] = {t.nd == 2 ? t.H : t.D, t.nd == 2 ? t.W : t.H, t.W};
-    for (int i = 0; i < t.nd; ++i) shift[3 * w + i] = pmod(sh[i] + (int)(mx[i] / (m00 + kEps)), n[i]);
+  __syncthreads();
+  __shared__ float tot[kRawMax];
+  if (threadIdx.x < RAWS) {
+    const int s = threadIdx.x;
+    float v = 0.f;
+    for (int i = 0; i < NWARP; ++i) v += red[i][s];
+    if (s == RAW_BORDER) v = v > 0.f ? 1.f : 0.f;
+    if (s == RAW_SHIFT) v = (float)s0;
+    if (s == RAW_SHIFT + 1) v = (float)s1;
+    if (s == RAW_SHIFT + 2) v = (float)s2;
+    tot[s] = v;
+    if (a.raw) a.raw[sol * a.raw_sol_stride + (w - sol * a.n_init) * a.raw_init_stride + s] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int n[3] = {nd == 2 ? t.H : t.D, nd == 2 ? t.W : t.H, t.W};
+    const int sh[3] = {s0, s1, s2};
+    for (int i = 0; i < nd; ++i) a.shift[3 * w + i] = pmod(sh[i] + (int)(tot[RAW_MX + i] / (tot[RAW_M00] + kEps)), n[i]);
+    a.done[w] = 0;
   }
 }
 
@@ -459,6 +650,7 @@ struct AdjArgs {
   float* a;            // [nw, K, cells] dL/du_k
   float* bf;           // [nw, C, cells] dL/df_c
   float* ff;           // [nw, C, cells] f_c
+  float* s_copy;       // [nw, C, cells] copy of s, stored right after a
   const float* gf;     // [Ns, K, 2]
   const float* w;      // [Ns, C, K]
   const float* T;      // [Ns]
@@ -495,16 +687,29 @@ __device__ __forceinline__ float growth_du(int id, float u, float m, float s, fl
   return 0.f;  // step, staircase: piecewise constant
 }
 
-__global__ void __launch_bounds__(kNT) nd_adj_point_kernel(NdTab t, AdjArgs a) {
-  const long total = (long)a.n_worlds * t.cells;
-  const int C = t.C, K = t.K;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const int w = (int)(i / t.cells);
-    const long cell = i - (long)w * t.cells;
-    const int sol = w / a.n_init;
-    const float dt = 1.f / __ldg(a.T + sol);
-    const float* gf = a.gf + (long)sol * 2 * K;
-    const float* wt = a.w + (long)sol * C * K;
+// Pointwise part of the reverse step, one block per (world, chunk of cells):
+// the clip / state-function gradient, dL/df per channel, dL/dg per kernel
+// (the weighted merge's transpose) and the growth derivative give
+// a_k = dL/du_k; the entering state is copied beside a (both are
+// transformed by the same passes).  With FK > 0 the model has exactly FK
+// kernels and FC channels and the block also adds its parameter partials
+// (those of nd_adj_param_kernel) into its slots of pacc.
+template <int FK, int FC>
+__global__ void __launch_bounds__(kNT) nd_adj_point_kernel(NdTab t, AdjArgs a, int pb, float* __restrict__ pacc) {
+  constexpr bool kFused = FK > 0;
+  const int C = kFused ? FC : t.C, K = kFused ? FK : t.K;
+  const int w = blockIdx.x / pb, b = blockIdx.x % pb;
+  const long chunk = (t.cells + pb - 1) / pb;
+  const long c0 = (long)b * chunk, c1 = min(t.cells, c0 + chunk);
+  const int sol = w / a.n_init;
+  const float dt = 1.f / __ldg(a.T + sol);
+  const float* gf = a.gf + (long)sol * 2 * K;
+  const float* wt = a.w + (long)sol * C * K;
+  constexpr int kAcc = kFused ? FK * (2 + FC) : 1;
+  float acc[kAcc];
+#pragma unroll
+  for (int j = 0; j < kAcc; ++j) acc[j] = 0.f;
+  for (long cell = c0 + threadIdx.x; cell < c1; cell += blockDim.x) {
     float f[kMaxChannels], bb[kMaxChannels], ws[kMaxChannels];
 #pragma unroll
     for (int c = 0; c < kMaxChannels; ++c) {
@@ -530,6 +735,7 @@ __global__ void __launch_bounds__(kNT) nd_adj_point_kernel(NdTab t, AdjArgs a) {
       const long off = ((long)w * C + c) * t.cells + cell;
       const float lam = __ldg(a.lam + off);
       const float sv = __ldg(a.s + off);
+      a.s_copy[off] = sv;
       float dsds, dsdf;  // d state' / d state and d state' / d field (core.py:245-319)
       if (t.state_fn == LGX_STATE_V1) {
         // mask: the forward's clip was inactive where its output lies strictly inside (0, 1)
@@ -550,9 +756,11 @@ __global__ void __launch_bounds__(kNT) nd_adj_point_kernel(NdTab t, AdjArgs a) {
       a.ff[off] = f[c];
     }
     for (int k = 0; k < K; ++k) {
+      const int id = t.gf[k];
       const float u = __ldg(a.u + ((long)w * K + k) * t.cells + cell);
+      const float m = __ldg(gf + 2 * k), sg = __ldg(gf + 2 * k + 1);
       float g;
-      const float gu = growth_du(t.gf[k], u, __ldg(gf + 2 * k), __ldg(gf + 2 * k + 1), &g);
+      const float gu = growth_du(id, u, m, sg, &g);
       float dg = 0.f;  // dL/dg_k = sum_c dL/df_c * w_ck (/ sum_j w_cj in mean mode)
 #pragma unroll
       for (int c = 0; c < kMaxChannels; ++c) {
@@ -560,20 +768,52 @@ __global__ void __launch_bounds__(kNT) nd_adj_point_kernel(NdTab t, AdjArgs a) {
         const float wk = __ldg(wt + c * K + k);
         dg = fmaf(bb[c], t.mean ? wk / ws[c] : wk, dg);
       }
-      a.a[((long)w * K + k) * t.cells + cell] = dg * gu;
+      const float ak = dg * gu;
+      a.a[((long)w * K + k) * t.cells + cell] = ak;
+      if constexpr (kFused) {
+        if (k < FK) {
+          float* pk = acc + k * (2 + FC);
+          if (id != LGX_GF_IDENTITY) {
+            pk[0] -= ak;
+            pk[1] -= ak * (u - m) / sg;
+          }
+#pragma unroll
+          for (int c = 0; c < FC; ++c) pk[2 + c] = fmaf(bb[c], t.mean ? (g - f[c]) / ws[c] : g, pk[2 + c]);
+        }
+      }
+    }
+  }
+  if constexpr (kFused) {
+    __shared__ float red[kNT / 32][kAcc];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int j = 0; j < kAcc; ++j) acc[j] = warp_sum(acc[j]);
+    if (lane == 0)
+#pragma unroll
+      for (int j = 0; j < kAcc; ++j) red[wid][j] = acc[j];
+    __syncthreads();
+    if (threadIdx.x < kAcc) {
+      float v = 0.f;
+      for (int i = 0; i < kNT / 32; ++i) v += red[i][threadIdx.x];
+      const int k = threadIdx.x / (2 + FC), j = threadIdx.x % (2 + FC);
+      pacc[(((long)w * FK + k) * pb + b) * (2 + FC) + j] += v;
     }
   }
 }
 
-// Per (world, kernel): dL/dm_k = -sum a_k, dL/ds_k = -sum a_k (u_k - m) / s,
-// dL/dw_ck = sum dL/df_c * (g_k - f_c) / sum_j w_cj (mean) or dL/df_c * g_k
-// (sum), accumulated into pacc[w] ([2K] growth parameters, then [C, K]).
-__global__ void __launch_bounds__(kNT) nd_adj_param_kernel(NdTab t, int n_init, const float* __restrict__ u,
+// Per (world, kernel, chunk of cells): dL/dm_k = -sum a_k,
+// dL/ds_k = -sum a_k (u_k - m) / s, dL/dw_ck = sum dL/df_c * (g_k - f_c) /
+// sum_j w_cj (mean) or dL/df_c * g_k (sum), added into the block's own slot
+// pacc[w, k, b] = {dm, ds, dw_0k .. dw_(C-1)k} (each block owns its slot
+// across the reverse steps, so the sums are race-free and deterministic).
+__global__ void __launch_bounds__(kNT) nd_adj_param_kernel(NdTab t, int n_init, int pb, const float* __restrict__ u,
                                                            const float* __restrict__ a, const float* __restrict__ bf,
                                                            const float* __restrict__ ff, const float* __restrict__ gfp,
                                                            const float* __restrict__ wts, float* __restrict__ pacc) {
   const int C = t.C, K = t.K;
-  const int w = blockIdx.x / K, k = blockIdx.x % K;
+  const int w = blockIdx.x / (K * pb), k = (blockIdx.x / pb) % K, b = blockIdx.x % pb;
+  const long chunk = (t.cells + pb - 1) / pb;
+  const long c0 = (long)b * chunk, c1 = min(t.cells, c0 + chunk);
   const int sol = w / n_init;
   const float m = __ldg(gfp + ((long)sol * K + k) * 2), s = __ldg(gfp + ((long)sol * K + k) * 2 + 1);
   const int id = t.gf[k];
@@ -587,7 +827,7 @@ __global__ void __launch_bounds__(kNT) nd_adj_param_kernel(NdTab t, int n_init, 
   float dm = 0.f, ds = 0.f, dw[kMaxChannels];
 #pragma unroll
   for (int c = 0; c < kMaxChannels; ++c) dw[c] = 0.f;
-  for (long cell = threadIdx.x; cell < t.cells; cell += blockDim.x) {
+  for (long cell = c0 + threadIdx.x; cell < c1; cell += blockDim.x) {
     const float uu = __ldg(u + ((long)w * K + k) * t.cells + cell);
     const float ak = __ldg(a + ((long)w * K + k) * t.cells + cell);
     if (id != LGX_GF_IDENTITY) {
@@ -618,56 +858,23 @@ __global__ void __launch_bounds__(kNT) nd_adj_param_kernel(NdTab t, int n_init, 
   if (threadIdx.x < 2 + C) {
     float v = 0.f;
     for (int i = 0; i < kNT / 32; ++i) v += red[i][threadIdx.x];
-    float* pw = pacc + (long)w * (2 * K + C * K);
-    if (threadIdx.x < 2) pw[2 * k + threadIdx.x] += v;
-    else pw[2 * K + (threadIdx.x - 2) * K + k] += v;
+    pacc[(((long)w * K + k) * pb + b) * (2 + C) + threadIdx.x] += v;
   }
 }
 
-// Spectral part of the reverse step: gk[w, k] += A_k conj(S_cin(k)) (kernel
-// gradient), Q[w, c] = sum_{k: c_in(k) = c} A_k conj(prepared K_k).
-__global__ void nd_adj_spectral_kernel(NdTab t, int n_worlds, int n_init, const float2* __restrict__ A,
-                                       const float2* __restrict__ S, const float2* __restrict__ kf,
-                                       long kf_sol_stride, float2* __restrict__ gk, float2* __restrict__ Q) {
-  const long total = (long)n_worlds * t.cells;
-  const int C = t.C, K = t.K;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
-    const int w = (int)(i / t.cells);
-    const long cell = i - (long)w * t.cells;
-    const int sol = w / n_init;
-    float2 q[kMaxChannels];
-#pragma unroll
-    for (int c = 0; c < kMaxChannels; ++c) q[c] = make_float2(0.f, 0.f);
-    for (int k = 0; k < K; ++k) {
-      const int c = t.cin[k];
-      const float2 ak = A[((long)w * K + k) * t.cells + cell];
-      const float2 sc = S[((long)w * C + c) * t.cells + cell];
-      float2* g = gk + ((long)w * K + k) * t.cells + cell;
-      *g = cadd(*g, cmulc(ak, sc));
-      const float2 kk = __ldg(kf + sol * kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + cell);
-      const float2 pr = cmulc(ak, kk);
-#pragma unroll
-      for (int cc = 0; cc < kMaxChannels; ++cc)
-        if (cc == c) q[cc] = cadd(q[cc], pr);
-    }
-#pragma unroll
-    for (int c = 0; c < kMaxChannels; ++c) {
-      if (c >= C) break;
-      Q[((long)w * C + c) * t.cells + cell] = q[c];
-    }
-  }
-}
-
-// per solution: grad_gf[s] += sum over its inits of pacc[..., :2K],
-// grad_w[s] += sum of pacc[..., 2K:]
-__global__ void nd_param_reduce_kernel(int n_sols, int n_init, int K, int C, const float* __restrict__ pacc,
+// per solution: grad_gf[s, k] += sum over its inits and chunks of
+// pacc[w, k, b, 0:2], grad_w[s, c, k] += sum of pacc[w, k, b, 2 + c]
+__global__ void nd_param_reduce_kernel(int n_sols, int n_init, int K, int C, int pb, const float* __restrict__ pacc,
                                        float* __restrict__ grad_gf, float* __restrict__ grad_w) {
   const int per = 2 * K + C * K;
   const long total = (long)n_sols * per;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
     const int sol = (int)(i / per), j = (int)(i % per);
+    const int k = j < 2 * K ? j / 2 : (j - 2 * K) % K;
+    const int slot = j < 2 * K ? j % 2 : 2 + (j - 2 * K) / K;
     float v = 0.f;
-    for (int n = 0; n < n_init; ++n) v += pacc[((long)sol * n_init + n) * per + j];
+    for (int n = 0; n < n_init; ++n)
+      for (int b = 0; b < pb; ++b) v += pacc[((((long)sol * n_init + n) * K + k) * pb + b) * (2 + C) + slot];
     if (j < 2 * K) grad_gf[(long)sol * 2 * K + j] += v;
     else grad_w[(long)sol * C * K + (j - 2 * K)] += v;
   }
@@ -701,14 +908,25 @@ bool nd_supported(const Model& m) {
   return true;
 }
 
-int nd_blocks_per_world(const Model& m) {
-  return (int)std::max(1L, std::min<long>(256, (m.cells + (long)kNT * 16 - 1) / ((long)kNT * 16)));
+int nd_blocks_per_world(const Model& m, long n_worlds) {
+  // 16 cells per thread, or more blocks when the batch is too small to fill
+  // the GPU (at least one cell per thread, at most 256 blocks)
+  const long by_cells = (m.cells + (long)kNT * 16 - 1) / ((long)kNT * 16);
+  const long fill = (kFillBlocks + n_worlds - 1) / std::max(1L, n_worlds);
+  const long useful = (m.cells + kNT - 1) / kNT;
+  return (int)std::max(1L, std::min<long>(256, std::min(useful, std::max(by_cells, fill))));
 }
+
+namespace {
+// chunks of cells per world of the adjoint's pointwise kernel, and per
+// (world, kernel) of its parameter reduction
+int nd_param_blocks(const Model& m, long n_worlds) { return nd_blocks_per_world(m, n_worlds); }
+}  // namespace
 
 size_t nd_step_workspace_bytes(const Model& m, int n_worlds) {
   const size_t nw = (size_t)n_worlds, cells = (size_t)m.cells;
   return al256(nw * m.C * cells * sizeof(float2)) + al256(nw * m.K * cells * sizeof(float2)) +
-         al256(nw * m.K * cells * sizeof(float)) + al256(nw * nd_blocks_per_world(m) * raw_stride(m.C) * sizeof(float));
+         al256(nw * m.K * cells * sizeof(float)) + al256(nw * nd_blocks_per_world(m, (long)nw) * raw_stride(m.C) * sizeof(float));
 }
 
 size_t nd_prepared_bytes(const Model& m, int n_sols) {
@@ -726,7 +944,7 @@ cudaError_t launch_nd_step(const NdStep& s, cudaStream_t st) {
   const Model& m = *s.m;
   const NdTab t = make_tab(m, s.dt_mode);
   const size_t nw = (size_t)s.n_worlds, cells = (size_t)m.cells;
-  const int bpw = nd_blocks_per_world(m);
+  const int bpw = nd_blocks_per_world(m, (long)nw);
   char* p = static_cast<char*>(s.ws);
   float2* S = reinterpret_cast<float2*>(p);
   p += al256(nw * m.C * cells * sizeof(float2));
@@ -736,12 +954,16 @@ cudaError_t launch_nd_step(const NdStep& s, cudaStream_t st) {
   p += al256(nw * m.K * cells * sizeof(float));
   float* partial = reinterpret_cast<float*>(p);
   float* pot = s.pot_out ? s.pot_out : U;
-  cudaError_t e = forward_real(t, (long)nw * m.C, s.state, S, st);
+  cudaError_t e = forward_real_head(t, (long)nw * m.C, s.state, S, st);
   if (e != cudaSuccess) return e;
-  nd_multiply_kernel<<<grid_for((long)nw * m.K * cells), kNT, 0, st>>>(t, s.n_worlds, s.n_init, S, s.kf,
-                                                                        s.kf_sol_stride, P);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if ((e = inverse_real(t, (long)nw * m.K, P, pot, false, 1.f, st)) != cudaSuccess) return e;
+  ConvArgs ca{};
+  ca.n_init = s.n_init;
+  ca.kf = s.kf;
+  ca.kf_sol_stride = s.kf_sol_stride;
+  ca.S = S;
+  ca.P = P;
+  if ((e = run_conv(false, t, (long)nw, ca, st)) != cudaSuccess) return e;
+  if ((e = inverse_real_tail(t, (long)nw * m.K, P, pot, false, 1.f, st)) != cudaSuccess) return e;
   EpiArgs a;
   a.n_worlds = s.n_worlds;
   a.n_init = s.n_init;
@@ -755,23 +977,24 @@ cudaError_t launch_nd_step(const NdStep& s, cudaStream_t st) {
   a.w_sol_stride = s.w_sol_stride;
   a.dt = s.dt;
   a.field_out = s.field_out;
+  a.state_copy = s.state_copy;
   a.shift = s.shift;
+  a.done = s.done;
   a.partial = partial;
+  a.raw = s.raw;
+  a.raw_sol_stride = s.raw_sol_stride;
+  a.raw_init_stride = s.raw_world_stride;
   nd_epilogue_kernel<<<(unsigned)(nw * bpw), kNT, 0, st>>>(t, a);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  const int wpb = 4;
-  nd_reduce_kernel<<<(unsigned)((nw + wpb - 1) / wpb), 32 * wpb, 0, st>>>(
-      t, s.n_worlds, s.n_init, bpw, partial, s.raw, s.raw_sol_stride, s.raw_world_stride, s.shift);
   return cudaGetLastError();
 }
 
 size_t nd_adjoint_workspace_bytes(const Model& m, int n_sols, int n_init) {
-  const size_t nw = (size_t)n_sols * n_init, cells = (size_t)m.cells;
-  return nd_prepared_bytes(m, n_sols) + al256(nw * m.K * cells * sizeof(float2)) +  // kf, A
-         2 * al256(nw * m.C * cells * sizeof(float2)) +                              // S, Q
-         al256(nw * m.K * cells * sizeof(float)) +                                   // a
-         3 * al256(nw * m.C * cells * sizeof(float)) +                               // bf, ff, lambda ping-pong
-         al256(nw * (2 * m.K + m.C * m.K) * sizeof(float));                          // parameter partials
+  const size_t nw = (size_t)n_sols * n_init, cells = (size_t)m.cells, KC = (size_t)(m.K + m.C);
+  return nd_prepared_bytes(m, n_sols) + al256(nw * KC * cells * sizeof(float2)) +  // kf, [A | S]
+         al256(nw * m.C * cells * sizeof(float2)) +                                // Q
+         al256(nw * KC * cells * sizeof(float)) +                                  // [a | state copy]
+         3 * al256(nw * m.C * cells * sizeof(float)) +                             // bf, ff, lambda ping-pong
+         al256(nw * m.K * nd_param_blocks(m, (long)nw) * (2 + m.C) * sizeof(float));  // parameter partials
 }
 
 size_t nd_kernel_grad_acc_bytes(const Model& m, int n_sols, int n_init) {
@@ -785,14 +1008,14 @@ cudaError_t launch_nd_adjoint(const Model& m, const NdAdjoint& j, void* ws, cuda
   char* p = static_cast<char*>(ws);
   float2* kf = reinterpret_cast<float2*>(p);
   p += nd_prepared_bytes(m, j.n_sols);
-  float2* A = reinterpret_cast<float2*>(p);
-  p += al256((size_t)nw * m.K * cells * sizeof(float2));
-  float2* S = reinterpret_cast<float2*>(p);
-  p += al256((size_t)nw * m.C * cells * sizeof(float2));
+  const size_t KC = (size_t)(m.K + m.C);
+  float2* A = reinterpret_cast<float2*>(p);  // the K planes of a, then the C planes of the state
+  float2* S = A + (size_t)nw * m.K * cells;
+  p += al256((size_t)nw * KC * cells * sizeof(float2));
   float2* Q = reinterpret_cast<float2*>(p);
   p += al256((size_t)nw * m.C * cells * sizeof(float2));
-  float* ar = reinterpret_cast<float*>(p);
-  p += al256((size_t)nw * m.K * cells * sizeof(float));
+  float* ar = reinterpret_cast<float*>(p);  // a, then the state copy: one real input for the head passes
+  p += al256((size_t)nw * KC * cells * sizeof(float));
   float* bf = reinterpret_cast<float*>(p);
   p += al256((size_t)nw * m.C * cells * sizeof(float));
   float* ff = reinterpret_cast<float*>(p);
@@ -801,8 +1024,10 @@ cudaError_t launch_nd_adjoint(const Model& m, const NdAdjoint& j, void* ws, cuda
   p += al256((size_t)nw * m.C * cells * sizeof(float));
   float* pacc = reinterpret_cast<float*>(p);
   const long kf_sol = (long)m.C * m.max_k * m.cells;
+  const int pb = nd_param_blocks(m, nw);
+  const bool fused = m.K == 1 && m.C == 1;  // parameter partials inside the pointwise kernel
   cudaError_t e = launch_nd_prepare(m, j.n_sols, j.k_half, kf, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(pacc, 0, (size_t)nw * (2 * m.K + m.C * m.K) * sizeof(float), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(pacc, 0, (size_t)nw * m.K * pb * (2 + m.C) * sizeof(float), st);
   if (e != cudaSuccess) return e;
   const size_t plane_c = (size_t)m.C * cells, plane_k = (size_t)m.K * cells;
   const float* lam_in = j.lambda_in;
@@ -823,20 +1048,32 @@ cudaError_t launch_nd_adjoint(const Model& m, const NdAdjoint& j, void* ws, cuda
     a.gf = j.gf_params;
     a.w = j.weights;
     a.T = j.T;
-    nd_adj_point_kernel<<<grid_for((long)nw * cells), kNT, 0, st>>>(t, a);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    nd_adj_param_kernel<<<(unsigned)(nw * m.K), kNT, 0, st>>>(t, j.n_init, a.u, ar, bf, ff, j.gf_params, j.weights,
-                                                                pacc);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = forward_real(t, (long)nw * m.K, ar, A, st)) != cudaSuccess) return e;
-    if ((e = forward_real(t, (long)nw * m.C, a.s, S, st)) != cudaSuccess) return e;
-    nd_adj_spectral_kernel<<<grid_for((long)nw * cells), kNT, 0, st>>>(t, nw, j.n_init, A, S, kf, kf_sol, j.gk, Q);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if ((e = inverse_real(t, (long)nw * m.C, Q, lam_out, true, 1.f, st)) != cudaSuccess) return e;
+    a.s_copy = ar + (size_t)nw * m.K * cells;
+    if (fused) {
+      nd_adj_point_kernel<1, 1><<<(unsigned)(nw * pb), kNT, 0, st>>>(t, a, pb, pacc);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    } else {
+      nd_adj_point_kernel<0, 0><<<(unsigned)(nw * pb), kNT, 0, st>>>(t, a, pb, pacc);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      nd_adj_param_kernel<<<(unsigned)(nw * m.K * pb), kNT, 0, st>>>(t, j.n_init, pb, a.u, ar, bf, ff, j.gf_params,
+                                                                       j.weights, pacc);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if ((e = forward_real_head(t, (long)nw * KC, ar, A, st)) != cudaSuccess) return e;
+    ConvArgs ca{};
+    ca.n_init = j.n_init;
+    ca.kf = kf;
+    ca.kf_sol_stride = kf_sol;
+    ca.S = S;
+    ca.A = A;
+    ca.gk = j.gk;
+    ca.Q = Q;
+    if ((e = run_conv(true, t, (long)nw, ca, st)) != cudaSuccess) return e;
+    if ((e = inverse_real_tail(t, (long)nw * m.C, Q, lam_out, true, 1.f, st)) != cudaSuccess) return e;
     lam_in = lam_out;
   }
   nd_param_reduce_kernel<<<grid_for((long)j.n_sols * (2 * m.K + m.C * m.K)), kNT, 0, st>>>(
-      j.n_sols, j.n_init, m.K, m.C, pacc, j.grad_gf, j.grad_weights);
+      j.n_sols, j.n_init, m.K, m.C, pb, pacc, j.grad_gf, j.grad_weights);
   return cudaGetLastError();
 }
 
