@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 
@@ -41,6 +42,31 @@ int cuda_fail(cudaError_t e, const char* where) {
 int lgx::api_error(int code, const char* msg) {
   g_err = msg;
   return code;
+}
+
+// Unique id of the current driver context (cuCtxGetCurrent + cuCtxGetId,
+// fetched through the runtime's driver entry points, so the library does not
+// link the driver library itself).  Returns false when it cannot be read.
+bool lgx::current_context_id(unsigned long long* id) {
+  typedef int (*GetCurrent)(void**);
+  typedef int (*GetId)(void*, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag looked_up;
+  std::call_once(looked_up, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(f);
+  });
+  void* ctx = nullptr;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx) return false;
+  return get_id(ctx, id) == 0;
 }
 
 namespace {

@@ -28,6 +28,9 @@ struct Model {
 // Record `msg` as the calling thread's lgx_last_error() and return `code`.
 int api_error(int code, const char* msg);
 
+// Unique id of the calling thread's current CUDA context (false if none).
+bool current_context_id(unsigned long long* id);
+
 // The model a plan was built from (capi.cu).
 const Model* plan_model(const lgx_plan* plan);
 

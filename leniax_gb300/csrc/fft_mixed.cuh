@@ -54,22 +54,29 @@ __device__ __forceinline__ void fill_twiddles(float2* tw, int N) {
 // by W_{Ns R}^{q (j mod Ns)}, takes the R-point DFT and writes
 // out[(j / Ns) Ns R + (j mod Ns) + t Ns].
 template <bool INV, int R>
-__device__ __forceinline__ void stockham_stage(const float2* in_all, float2* out_all, int N, int Ns, const float2* tw,
-                                               int nl) {
-  const int nb = N / R, stride = N / (Ns * R);
-  for (int jj = threadIdx.x; jj < nl * nb; jj += blockDim.x) {
-    const int line = jj / nb, j = jj - line * nb;  // lines of N points, contiguous
-    const float2* in = in_all + line * N;
-    float2* out = out_all + line * N;
-    const int k = j % Ns;
-    float2 v[R];
+__device__ __forceinline__ void stockham_butterfly(const float2* in, float2* out, int nb, int Ns, int j, int k,
+                                                   int stride, const float2* tw) {
+  float2 v[R];
 #pragma unroll
-    for (int q = 0; q < R; ++q) {
-      const float2 x = in[j + q * nb];
-      const float2 w = tw[q * k * stride];  // q k stride < N
-      v[q] = q == 0 ? x : (INV ? cmulc(x, w) : cmul(x, w));
-    }
-    float2 y[R];
+  for (int q = 0; q < R; ++q) {
+    const float2 x = in[j + q * nb];
+    const float2 w = tw[q * k * stride];  // q k stride < N
+    v[q] = q == 0 ? x : (INV ? cmulc(x, w) : cmul(x, w));
+  }
+  float2 y[R];
+  if constexpr (R == 2) {
+    y[0] = cadd(v[0], v[1]);
+    y[1] = csub(v[0], v[1]);
+  } else if constexpr (R == 4) {
+    // W_4 = -i forward, +i inverse: the products are swaps and sign flips
+    const float2 s02 = cadd(v[0], v[2]), d02 = csub(v[0], v[2]);
+    const float2 s13 = cadd(v[1], v[3]), d13 = csub(v[1], v[3]);
+    const float2 rot = INV ? make_float2(-d13.y, d13.x) : make_float2(d13.y, -d13.x);
+    y[0] = cadd(s02, s13);
+    y[1] = cadd(d02, rot);
+    y[2] = csub(s02, s13);
+    y[3] = csub(d02, rot);
+  } else {
 #pragma unroll
     for (int t = 0; t < R; ++t) {
       float2 acc = v[0];
@@ -80,9 +87,19 @@ __device__ __forceinline__ void stockham_stage(const float2* in_all, float2* out
       }
       y[t] = acc;
     }
-    const int base = (j / Ns) * Ns * R + k;
+  }
+  const int base = (j - k) * R + k;  // (j / Ns) Ns R + k
 #pragma unroll
-    for (int t = 0; t < R; ++t) out[base + t * Ns] = y[t];
+  for (int t = 0; t < R; ++t) out[base + t * Ns] = y[t];
+}
+
+template <bool INV, int R>
+__device__ __forceinline__ void stockham_stage(const float2* in_all, float2* out_all, int N, int Ns, const float2* tw,
+                                               int nl) {
+  const int nb = N / R, stride = N / (Ns * R);
+  for (int jj = threadIdx.x; jj < nl * nb; jj += blockDim.x) {
+    const int line = jj / nb, j = jj - line * nb;  // lines of N points, contiguous
+    stockham_butterfly<INV, R>(in_all + line * N, out_all + line * N, nb, Ns, j, j % Ns, stride, tw);
   }
 }
 

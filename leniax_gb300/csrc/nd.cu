@@ -28,6 +28,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
+#include <vector>
 
 #include "common.cuh"
 #include "engine.h"
@@ -38,10 +40,13 @@ namespace {
 
 constexpr int kNT = 256;          // threads per block
 constexpr int kMaxPts = 4096;     // complex points of one pass tile (two buffers in shared memory)
-// Launches smaller than this many blocks (four on each of GB300's 152 SMs)
+// Launches smaller than this many blocks (two on each of GB300's 152 SMs)
 // get smaller tiles / chunks so that one small world still spreads over the
-// whole GPU; large batches keep the full-size tiles.
-constexpr long kFillBlocks = 4 * 152;
+// whole GPU; large batches keep the full-size tiles.  Measured on one 48^3
+// world (forward + adjoint): 1, 2, 4 and 8 blocks per SM gave 8.45, 8.7,
+// 6.25 and 5.6 thousand fwd+bwd world-steps/s (more, smaller blocks pay
+// more per-block start-up than they gain in parallelism).
+constexpr long kFillBlocks = 2 * 152;
 constexpr int kRawMax = RAW_CM + kMaxChannels;
 
 struct NdTab {  // kernel table of a model, passed by value
@@ -78,18 +83,37 @@ NdTab make_tab(const Model& m, int dt_mode) {
 // Lines of a pass: line (g, i) starts at g * gstride + i and has L points
 // `stride` apart; g < G, i < I.  I == 1: a tile is nl consecutive groups
 // (rows of the x pass, contiguous); I > 1: nl consecutive i of one group.
+// n / d for 0 <= n < 2^31 by a multiply-high and a shift (the round-up
+// method of Granlund and Montgomery, "Division by invariant integers using
+// multiplication", 1994): s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> s.
+struct FastDiv {
+  unsigned m, s;
+};
+inline FastDiv make_fastdiv(unsigned d) {
+  FastDiv f;
+  f.s = 0;
+  while ((1ull << f.s) < d) ++f.s;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << f.s) - d)) / d + 1);
+  return f;
+}
+__device__ __forceinline__ int fdiv(int n, FastDiv f) {
+  return (int)((__umulhi((unsigned)n, f.m) + (unsigned)n) >> f.s);
+}
+
 struct Pass {
   float2* data;          // complex planes (in and out, in place)
   const float* src_real;  // IN_REAL: real input of the same geometry
   float* dst_real;        // OUT_REAL: Re(result) * scale (stored, or added when accumulate)
   long G, I, gstride, stride;
   int L, nl;
+  FastDiv fnl;            // division by nl
   int in_real, out_real, accumulate;
   float scale;
 };
 
 template <bool INV>
-__global__ void __launch_bounds__(kNT) nd_pass_kernel(Pass a, GPlan p) {
+__global__ void __launch_bounds__(kNT, 3) nd_pass_kernel(Pass a, GPlan p) {
   extern __shared__ __align__(16) float2 ndsm[];
   const int L = a.L, nl = a.nl;
   float2* tw = ndsm;
@@ -109,6 +133,13 @@ __global__ void __launch_bounds__(kNT) nd_pass_kernel(Pass a, GPlan p) {
   }
   fill_twiddles(tw, L);
   const int pts = nl * L;
+  // A tile of the x pass is nl whole rows, contiguous in memory and in the
+  // tile (point idx at row-block offset idx); a strided pass's tile holds
+  // nl adjacent lines, point idx = j nl + l of the global walk landing at
+  // l L + j in the tile.
+  const bool rows = a.I == 1;
+  const long gbase = rows ? g0 * a.gstride : g0 * a.gstride + i0;
+  const int valid = rows ? lines * L : pts;
   // kLoadBatch independent global loads in flight per thread before their
   // shared-memory stores (one load per iteration would serialise on latency)
   constexpr int kLoadBatch = 8;
@@ -118,20 +149,20 @@ __global__ void __launch_bounds__(kNT) nd_pass_kernel(Pass a, GPlan p) {
 #pragma unroll
     for (int u = 0; u < kLoadBatch; ++u) {
       const int idx = base + u * blockDim.x;
-      int l, j;
-      if (a.I == 1) {
-        l = idx / L;
-        j = idx - l * L;
+      long off;
+      bool in;
+      if (rows) {
+        dst[u] = idx < pts ? idx : -1;
+        in = idx < valid;
+        off = gbase + idx;
       } else {
-        j = idx / nl;
-        l = idx - j * nl;
+        const int j = fdiv(idx, a.fnl), l = idx - j * nl;
+        dst[u] = idx < pts ? l * L + j : -1;
+        in = idx < pts && l < lines;
+        off = gbase + l + (long)j * a.stride;
       }
-      dst[u] = idx < pts ? l * L + j : -1;
       v[u] = make_float2(0.f, 0.f);
-      if (idx < pts && l < lines) {
-        const long off = (a.I == 1 ? (g0 + l) * a.gstride : g0 * a.gstride + i0 + l) + (long)j * a.stride;
-        v[u] = a.in_real ? make_float2(__ldg(a.src_real + off), 0.f) : a.data[off];
-      }
+      if (in) v[u] = a.in_real ? make_float2(__ldg(a.src_real + off), 0.f) : a.data[off];
     }
 #pragma unroll
     for (int u = 0; u < kLoadBatch; ++u)
@@ -139,18 +170,19 @@ __global__ void __launch_bounds__(kNT) nd_pass_kernel(Pass a, GPlan p) {
   }
   __syncthreads();
   const float2* res = fft_line<INV>(A, B, p, tw, nl);
-  for (int idx = threadIdx.x; idx < pts; idx += blockDim.x) {
-    int l, j;
-    if (a.I == 1) {
-      l = idx / L;
-      j = idx - l * L;
+  for (int idx = threadIdx.x; idx < valid; idx += blockDim.x) {
+    long off;
+    int src;
+    if (rows) {
+      off = gbase + idx;
+      src = idx;
     } else {
-      j = idx / nl;
-      l = idx - j * nl;
+      const int j = fdiv(idx, a.fnl), l = idx - j * nl;
+      if (l >= lines) continue;
+      off = gbase + l + (long)j * a.stride;
+      src = l * L + j;
     }
-    if (l >= lines) continue;
-    const long off = (a.I == 1 ? (g0 + l) * a.gstride : g0 * a.gstride + i0 + l) + (long)j * a.stride;
-    const float2 v = res[l * L + j];
+    const float2 v = res[src];
     if (a.out_real) {
       const float r = v.x * a.scale;
       a.dst_real[off] = a.accumulate ? a.dst_real[off] + r : r;
@@ -160,15 +192,10 @@ __global__ void __launch_bounds__(kNT) nd_pass_kernel(Pass a, GPlan p) {
   }
 }
 
-// Opt the pass kernels into their shared-memory tile (set on the current
-// device; cheap, so it is set before every pass).
-cudaError_t allow_pass_smem() {
-  const int bytes = (int)((2 * kMaxPts + kGMaxN) * sizeof(float2));
-  cudaError_t e = cudaFuncSetAttribute(nd_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(nd_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  return e;
-}
+// Raise the N-D kernels' dynamic shared-memory limits once per CUDA context
+// (the attribute belongs to the context: a context created later, after a
+// device reset for example, gets them again).
+cudaError_t allow_nd_smem();
 
 // One axis pass over `planes` planes of D x H x W points.  axis 0 = x
 // (contiguous), 1 = y, 2 = z.
@@ -211,9 +238,10 @@ cudaError_t run_pass(bool inv, int axis, const NdTab& t, long planes, float2* da
   const long fill = (a.G * a.I + kFillBlocks - 1) / kFillBlocks;
   const long want = std::max<long>(a.I == 1 ? 1 : 4, fill);
   a.nl = (int)std::min<long>(std::min<long>(cap, want), a.I == 1 ? a.G : a.I);
+  a.fnl = make_fastdiv((unsigned)a.nl);
   const long tiles = a.I == 1 ? (a.G + a.nl - 1) / a.nl : a.G * ((a.I + a.nl - 1) / a.nl);
   const size_t smem = (size_t)(a.L + 2 * a.nl * a.L) * sizeof(float2);
-  cudaError_t e = allow_pass_smem();
+  cudaError_t e = allow_nd_smem();
   if (e != cudaSuccess) return e;
   if (tiles >= (1L << 31)) return cudaErrorInvalidConfiguration;
   if (inv) nd_pass_kernel<true><<<(unsigned)tiles, kNT, smem, st>>>(a, p);
@@ -290,6 +318,7 @@ inline int grid_for(long total) { return (int)std::max(1L, std::min<long>((total
 // arithmetic is that of the separate passes, in the same order.
 struct ConvArgs {
   int n_init, L, nl, tiles;  // points per line, lines per tile, tiles per plane
+  FastDiv fnl;               // division by nl
   long I;                    // lines per plane (= point stride along the axis)
   const float2* kf;          // prepared full spectra [Ns, C, max_k, cells]
   long kf_sol_stride;
@@ -303,7 +332,7 @@ struct ConvArgs {
 // nl lines of a plane (points src[l + j I]) into a line-major tile (lines
 // past `lines` read as zero); kLoadBatch loads in flight per thread
 __device__ __forceinline__ void load_lines(float2* dst, const float2* __restrict__ src, long I, int L, int nl,
-                                           int lines) {
+                                           FastDiv fnl, int lines) {
   const int pts = nl * L;
   constexpr int kLoadBatch = 8;
   for (int base = threadIdx.x; base < pts; base += kLoadBatch * blockDim.x) {
@@ -312,7 +341,7 @@ __device__ __forceinline__ void load_lines(float2* dst, const float2* __restrict
 #pragma unroll
     for (int u = 0; u < kLoadBatch; ++u) {
       const int idx = base + u * blockDim.x;
-      const int j = idx / nl, l = idx - j * nl;
+      const int j = fdiv(idx, fnl), l = idx - j * nl;
       d[u] = idx < pts ? l * L + j : -1;
       v[u] = make_float2(0.f, 0.f);
       if (idx < pts && l < lines) v[u] = src[l + (long)j * I];
@@ -324,9 +353,9 @@ __device__ __forceinline__ void load_lines(float2* dst, const float2* __restrict
 }
 
 __device__ __forceinline__ void store_lines(float2* __restrict__ dst, const float2* src, long I, int L, int nl,
-                                            int lines) {
+                                            FastDiv fnl, int lines) {
   for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
-    const int j = idx / nl, l = idx - j * nl;
+    const int j = fdiv(idx, fnl), l = idx - j * nl;
     if (l < lines) dst[l + (long)j * I] = src[l * L + j];
   }
 }
@@ -345,7 +374,7 @@ __global__ void __launch_bounds__(kNT) nd_conv_kernel(NdTab t, ConvArgs a, GPlan
   const int sol = w / a.n_init;
   fill_twiddles(tw, L);
   for (int c = 0; c < t.C; ++c) {
-    load_lines(A, a.S + ((long)w * t.C + c) * t.cells + i0, a.I, L, nl, lines);
+    load_lines(A, a.S + ((long)w * t.C + c) * t.cells + i0, a.I, L, nl, a.fnl, lines);
     __syncthreads();
     const float2* r = fft_line<false>(A, B, p, tw, nl);
     for (int x = threadIdx.x; x < pts; x += blockDim.x) Sc[c * pts + x] = r[x];
@@ -353,12 +382,12 @@ __global__ void __launch_bounds__(kNT) nd_conv_kernel(NdTab t, ConvArgs a, GPlan
   }
   for (int k = 0; k < t.K; ++k) {
     const int c = t.cin[k];
-    load_lines(A, a.kf + sol * a.kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + i0, a.I, L, nl, lines);
+    load_lines(A, a.kf + sol * a.kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + i0, a.I, L, nl, a.fnl, lines);
     __syncthreads();
     for (int x = threadIdx.x; x < pts; x += blockDim.x) A[x] = cmul(Sc[c * pts + x], A[x]);
     __syncthreads();
     const float2* r = fft_line<true>(A, B, p, tw, nl);
-    store_lines(a.P + ((long)w * t.K + k) * t.cells + i0, r, a.I, L, nl, lines);
+    store_lines(a.P + ((long)w * t.K + k) * t.cells + i0, r, a.I, L, nl, a.fnl, lines);
     __syncthreads();
   }
 }
@@ -381,7 +410,7 @@ __global__ void __launch_bounds__(kNT) nd_adj_conv_kernel(NdTab t, ConvArgs a, G
   const int sol = w / a.n_init;
   fill_twiddles(tw, L);
   for (int c = 0; c < t.C; ++c) {
-    load_lines(A, a.S + ((long)w * t.C + c) * t.cells + i0, a.I, L, nl, lines);
+    load_lines(A, a.S + ((long)w * t.C + c) * t.cells + i0, a.I, L, nl, a.fnl, lines);
     __syncthreads();
     const float2* r = fft_line<false>(A, B, p, tw, nl);
     for (int x = threadIdx.x; x < pts; x += blockDim.x) {
@@ -392,16 +421,16 @@ __global__ void __launch_bounds__(kNT) nd_adj_conv_kernel(NdTab t, ConvArgs a, G
   }
   for (int k = 0; k < t.K; ++k) {
     const int c = t.cin[k];
-    load_lines(A, a.A + ((long)w * t.K + k) * t.cells + i0, a.I, L, nl, lines);
+    load_lines(A, a.A + ((long)w * t.K + k) * t.cells + i0, a.I, L, nl, a.fnl, lines);
     __syncthreads();
     const float2* r = fft_line<false>(A, B, p, tw, nl);
     float2* o = r == A ? B : A;  // the free buffer takes the prepared spectrum's lines
-    load_lines(o, a.kf + sol * a.kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + i0, a.I, L, nl,
+    load_lines(o, a.kf + sol * a.kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + i0, a.I, L, nl, a.fnl,
                lines);
     __syncthreads();
     float2* g = a.gk + ((long)w * t.K + k) * t.cells + i0;
     for (int idx = threadIdx.x; idx < pts; idx += blockDim.x) {
-      const int j = idx / nl, l = idx - j * nl;
+      const int j = fdiv(idx, a.fnl), l = idx - j * nl;
       if (l >= lines) continue;
       const int x = l * L + j;
       const float2 ak = r[x];
@@ -415,7 +444,7 @@ __global__ void __launch_bounds__(kNT) nd_adj_conv_kernel(NdTab t, ConvArgs a, G
     for (int x = threadIdx.x; x < pts; x += blockDim.x) A[x] = Qc[c * pts + x];
     __syncthreads();
     const float2* r = fft_line<true>(A, B, p, tw, nl);
-    store_lines(a.Q + ((long)w * t.C + c) * t.cells + i0, r, a.I, L, nl, lines);
+    store_lines(a.Q + ((long)w * t.C + c) * t.cells + i0, r, a.I, L, nl, a.fnl, lines);
     __syncthreads();
   }
 }
@@ -423,6 +452,8 @@ __global__ void __launch_bounds__(kNT) nd_adj_conv_kernel(NdTab t, ConvArgs a, G
 // Tile and shared memory of a fused convolution pass; `bufs` complex tiles
 // besides the twiddles (C + 2 forward, 2C + 2 adjoint).
 constexpr long kConvSmemPts = 96 * 1024 / 8;  // 96 KB of tiles: two blocks per SM
+// the largest tile set: one 512-point line, 2 x 16 + 2 buffers, twiddles
+constexpr int kConvSmemMax = (kGMaxN + (2 * kMaxChannels + 2) * kGMaxN) * (int)sizeof(float2);
 
 cudaError_t run_conv(bool adjoint, const NdTab& t, long nw, ConvArgs a, cudaStream_t st) {
   a.L = t.nd == 3 ? t.D : t.H;
@@ -435,20 +466,40 @@ cudaError_t run_conv(bool adjoint, const NdTab& t, long nw, ConvArgs a, cudaStre
   const long fill = (nw * a.I + kFillBlocks - 1) / kFillBlocks;
   a.nl = (int)std::min<long>(std::min<long>(cap, std::max<long>(4, fill)), a.I);
   a.tiles = (int)((a.I + a.nl - 1) / a.nl);
+  a.fnl = make_fastdiv((unsigned)a.nl);
   const size_t smem = (size_t)(a.L + bufs * a.nl * a.L) * sizeof(float2);
   const long blocks = nw * a.tiles;
   if (blocks >= (1L << 31)) return cudaErrorInvalidConfiguration;
-  cudaError_t e;
-  if (adjoint) {
-    e = cudaFuncSetAttribute(nd_adj_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    nd_adj_conv_kernel<<<(unsigned)blocks, kNT, smem, st>>>(t, a, p);
-  } else {
-    e = cudaFuncSetAttribute(nd_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    nd_conv_kernel<<<(unsigned)blocks, kNT, smem, st>>>(t, a, p);
-  }
+  if (smem > (size_t)kConvSmemMax) return cudaErrorInvalidConfiguration;
+  cudaError_t e = allow_nd_smem();
+  if (e != cudaSuccess) return e;
+  if (adjoint) nd_adj_conv_kernel<<<(unsigned)blocks, kNT, smem, st>>>(t, a, p);
+  else nd_conv_kernel<<<(unsigned)blocks, kNT, smem, st>>>(t, a, p);
   return cudaGetLastError();
+}
+
+cudaError_t allow_nd_smem() {
+  static std::mutex mu;
+  static std::vector<unsigned long long> done;  // contexts already set up
+  unsigned long long ctx = 0;
+  const bool known = current_context_id(&ctx);
+  if (known) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), ctx) != done.end()) return cudaSuccess;
+  }
+  const int pass_bytes = (int)((2 * kMaxPts + kGMaxN) * sizeof(float2));
+  cudaError_t e = cudaFuncSetAttribute(nd_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_adj_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
+  if (e == cudaSuccess && known) {
+    std::lock_guard<std::mutex> lk(mu);
+    done.push_back(ctx);
+  }
+  return e;
 }
 
 // The axis passes before and after the fused one: forward x (real input)
@@ -489,9 +540,13 @@ struct EpiArgs {
 
 // per-cell centred coordinate on one axis (statistics.py:64-81 on the world
 // rolled by the carried shift): ((i - shift) mod n) - n // 2
-__device__ __forceinline__ float centred(int i, int sh, int n) { return (float)(pmod(i - sh, n) - n / 2); }
+// (for 0 <= i, sh < n: a carried shift is always reduced mod n)
+__device__ __forceinline__ float centred_in(int i, int sh, int n) {
+  const int d = i - sh;
+  return (float)((d < 0 ? d + n : d) - n / 2);
+}
 
-__global__ void __launch_bounds__(kNT) nd_epilogue_kernel(NdTab t, EpiArgs a) {
+__global__ void __launch_bounds__(kNT, 3) nd_epilogue_kernel(NdTab t, EpiArgs a) {
   constexpr int NWARP = kNT / 32;
   __shared__ float red[NWARP][kRawMax];
   const int w = blockIdx.x / a.bpw, b = blockIdx.x % a.bpw;
@@ -514,19 +569,21 @@ __global__ void __launch_bounds__(kNT) nd_epilogue_kernel(NdTab t, EpiArgs a) {
 #pragma unroll
   for (int c = 0; c < kMaxChannels; ++c) cm[c] = 0.f;
   bool border = false;
-  for (long cell = c0 + threadIdx.x; cell < c1; cell += blockDim.x) {
-    const int x = (int)(cell % t.W);
-    const long r = cell / t.W;
-    const int y = (int)(r % t.H), z = (int)(r / t.H);
+  // (x, y, z) of the thread's cell, advanced by the block's stride of kNT
+  // cells with one carry per axis (no divisions inside the loop)
+  long cell = c0 + threadIdx.x;
+  int x = (int)(cell % t.W), y = (int)((cell / t.W) % t.H), z = (int)(cell / ((long)t.W * t.H));
+  const int sx = kNT % t.W, sy = (kNT / t.W) % t.H, sz = (int)(kNT / ((long)t.W * t.H));
+  for (; cell < c1; cell += kNT) {
     float ca, cb, cc;  // centred coordinates along the moment axes
     if (nd == 2) {
-      ca = centred(y, s0, t.H);
-      cb = centred(x, s1, t.W);
+      ca = centred_in(y, s0, t.H);
+      cb = centred_in(x, s1, t.W);
       cc = 0.f;
     } else {
-      ca = centred(z, s0, t.D);
-      cb = centred(y, s1, t.H);
-      cc = centred(x, s2, t.W);
+      ca = centred_in(z, s0, t.D);
+      cb = centred_in(y, s1, t.H);
+      cc = centred_in(x, s2, t.W);
     }
     const bool edge = x == 0 || x == t.W - 1 || y == 0 || y == t.H - 1 || (nd == 3 && (z == 0 || z == t.D - 1));
     for (int k = 0; k < K; ++k) cpot += __ldg(a.pot + ((long)w * K + k) * t.cells + cell) > kEps ? 1.f : 0.f;
@@ -565,6 +622,17 @@ __global__ void __launch_bounds__(kNT) nd_epilogue_kernel(NdTab t, EpiArgs a) {
       cgrow += fp > kEps ? 1.f : 0.f;
       border |= live && edge;
     }
+    x += sx;
+    if (x >= t.W) {
+      x -= t.W;
+      ++y;
+    }
+    y += sy;
+    if (y >= t.H) {
+      y -= t.H;
+      ++z;
+    }
+    z += sz;
   }
   float v[14] = {m00, g00, cpot, cmass, cgrow, mx0, mx1, mx2, gx0, gx1, gx2, q0, q1, q2};
 #pragma unroll

@@ -42,32 +42,6 @@ int na_fail(int code, const char* msg) {
   return code;
 }
 
-// Unique id of the current driver context (cuCtxGetCurrent + cuCtxGetId,
-// fetched through the runtime's driver entry points, so the library does not
-// link the driver library itself).  Returns false when it cannot be read.
-bool current_context_id(unsigned long long* id) {
-  typedef int (*GetCurrent)(void**);
-  typedef int (*GetId)(void*, unsigned long long*);
-  static GetCurrent get_current = nullptr;
-  static GetId get_id = nullptr;
-  static bool looked_up = false;
-  if (!looked_up) {  // under g_mu
-    void* f = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_current = reinterpret_cast<GetCurrent>(f);
-    f = nullptr;
-    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      get_id = reinterpret_cast<GetId>(f);
-    looked_up = true;
-  }
-  void* ctx = nullptr;
-  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx) return false;
-  return get_id(ctx, id) == 0;
-}
-
 // Device address of the scratch array in the current device's current
 // context.  Resolved with that device current the first time a device (or a
 // new context on it) is seen; in host code g_noalloc_scratch names a host-side
