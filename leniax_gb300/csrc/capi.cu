@@ -105,7 +105,10 @@ int select_engine(const Model& m, int requested) {
   if (requested == LGX_ENGINE_ND) return nd_supported(m) ? LGX_ENGINE_ND : -1;
   if (requested != LGX_ENGINE_AUTO) return -1;
   if (resident_supported(m)) return LGX_ENGINE_RESIDENT;
-  if (streamed_supported(m)) return LGX_ENGINE_STREAMED;
+  // even sides that are not powers of two: the N-D engine measured 1.1-1.7x
+  // the mixed-radix streamed step at C = K = 1 (48^2, 72^2, 112^2) and the
+  // same at C = 3, K = 15 (96^2); the streamed step stays available on request
+  if (streamed_supported(m) && !(generic_size(m.H) && nd_supported(m))) return LGX_ENGINE_STREAMED;
   if (cta_supported(m)) return LGX_ENGINE_CTA;
   if (nd_supported(m)) return LGX_ENGINE_ND;
   return -1;

@@ -50,12 +50,16 @@ def test_plan_accepts_valid_models():
 
 
 @pytest.mark.parametrize('side', [48, 72, 100, 112, 480])
-def test_sides_that_are_not_powers_of_two_take_the_streamed_engine(side):
+def test_sides_that_are_not_powers_of_two_take_the_nd_engine(side):
+    # even sides of factors 2, 3, 5, 7: the N-D engine by default, the
+    # mixed-radix streamed step on request
     lib = _lib.load()
     p = _plan(world=(side, side))
-    assert lib.lgx_select_engine(p.handle, 1, 2, 0) == _lib.ENGINES['streamed']
+    assert lib.lgx_select_engine(p.handle, 1, 2, 0) == _lib.ENGINES['nd']
+    assert lib.lgx_select_engine(p.handle, 1, 2, _lib.ENGINES['streamed']) == _lib.ENGINES['streamed']
     assert lib.lgx_update_workspace_bytes(p.handle, 3) > 0
     assert lib.lgx_run_workspace_bytes(p.handle, 1, 2, 4, 0) > 0
+    assert lib.lgx_run_workspace_bytes(p.handle, 1, 2, 4, _lib.ENGINES['streamed']) > 0
 
 
 def test_3d_plans_select_the_cta_engine_and_size_workspaces():

@@ -37,7 +37,10 @@ def test_single_step_multichannel(cuda, average):
     assert np.abs(f - fo).max() < 5e-4
 
 
-def test_rollout_statistics_and_stop_counts(cuda):
+@pytest.mark.parametrize('engine', ['auto', 'streamed'])
+def test_rollout_statistics_and_stop_counts(cuda, engine):
+    # 'auto' takes the N-D engine for these sides, 'streamed' the mixed-radix
+    # streamed step
     dev = torch.device('cuda')
     size, R, steps = 72, 11.0, 24
     K, mp, upd = engine_model(bump_kernel_params(s=0.02), [size, size], 1, R, dev=dev)
@@ -45,7 +48,7 @@ def test_rollout_statistics_and_stop_counts(cuda):
     cells = patch_init(3, size, 30, seed=17, scale_range=(0.6, 1.0))
     cs, fs, ps, st = runner.run_scan(None, torch.from_numpy(cells).to(dev), K, mp.get_gf_params(dev),
                                      mp.get_kernels_weight_per_channel(dev), torch.tensor(10.), steps, R, upd,
-                                     statistics.ComputeStatsFn([size, size], R, 10))
+                                     statistics.ComputeStatsFn([size, size], R, 10), engine=engine)
     cs_o, fs_o, ps_o, st_o = O.run_scan(cells, Ko, mpo['gf_params'], mpo['weights'], 10, steps, R, model)
     assert np.abs(cs[:4].cpu().numpy() - cs_o[:4]).max() < 4 * STEP_TOL
     assert np.abs(ps[:4].cpu().numpy() - ps_o[:4]).max() < 2e-5
