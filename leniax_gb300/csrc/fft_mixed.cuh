@@ -10,6 +10,24 @@
 
 namespace lgx {
 
+// n / d for 0 <= n < 2^31 by a multiply-high and a shift (the round-up
+// method of Granlund and Montgomery, "Division by invariant integers using
+// multiplication", 1994): s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1,
+// n / d = (umulhi(n, m) + n) >> s.
+struct FastDivU {
+  unsigned m, s;
+  __device__ __forceinline__ int div(int n) const {
+    return (int)((__umulhi((unsigned)n, m) + (unsigned)n) >> s);
+  }
+};
+inline FastDivU make_fastdiv(unsigned d) {
+  FastDivU f;
+  f.s = 0;
+  while ((1ull << f.s) < d) ++f.s;
+  f.m = (unsigned)(((1ull << 32) * ((1ull << f.s) - d)) / d + 1);
+  return f;
+}
+
 constexpr int kGMaxStages = 12;
 constexpr int kGMaxN = 512;
 
@@ -53,13 +71,15 @@ __device__ __forceinline__ void fill_twiddles(float2* tw, int N) {
 // One Stockham stage of radix R: butterfly j reads in[j + q N/R], twiddles
 // by W_{Ns R}^{q (j mod Ns)}, takes the R-point DFT and writes
 // out[(j / Ns) Ns R + (j mod Ns) + t Ns].
+// Point i of the line is in[i * pitch] / out[i * pitch] (pitch 1: a
+// contiguous line; the row pitch: a column of a row-major tile).
 template <bool INV, int R>
 __device__ __forceinline__ void stockham_butterfly(const float2* in, float2* out, int nb, int Ns, int j, int k,
-                                                   int stride, const float2* tw) {
+                                                   int stride, const float2* tw, int pitch = 1) {
   float2 v[R];
 #pragma unroll
   for (int q = 0; q < R; ++q) {
-    const float2 x = in[j + q * nb];
+    const float2 x = in[(j + q * nb) * pitch];
     const float2 w = tw[q * k * stride];  // q k stride < N
     v[q] = q == 0 ? x : (INV ? cmulc(x, w) : cmul(x, w));
   }
@@ -90,7 +110,7 @@ __device__ __forceinline__ void stockham_butterfly(const float2* in, float2* out
   }
   const int base = (j - k) * R + k;  // (j / Ns) Ns R + k
 #pragma unroll
-  for (int t = 0; t < R; ++t) out[base + t * Ns] = y[t];
+  for (int t = 0; t < R; ++t) out[(base + t * Ns) * pitch] = y[t];
 }
 
 template <bool INV, int R>
@@ -101,6 +121,46 @@ __device__ __forceinline__ void stockham_stage(const float2* in_all, float2* out
     const int line = jj / nb, j = jj - line * nb;  // lines of N points, contiguous
     stockham_butterfly<INV, R>(in_all + line * N, out_all + line * N, nb, Ns, j, j % Ns, stride, tw);
   }
+}
+
+// The same stage over ncols columns of a row-major tile (N rows, row pitch
+// `pitch`): consecutive threads take consecutive columns, so every access of
+// a warp is to consecutive addresses.  cdiv divides by ncols.
+template <bool INV, int R>
+__device__ __forceinline__ void stockham_stage_cols(const float2* in_all, float2* out_all, int N, int Ns,
+                                                    const float2* tw, int ncols, int pitch, const FastDivU& cdiv) {
+  const int nb = N / R, stride = N / (Ns * R);
+  for (int jj = threadIdx.x; jj < ncols * nb; jj += blockDim.x) {
+    const int j = cdiv.div(jj), col = jj - j * ncols;
+    stockham_butterfly<INV, R>(in_all + col, out_all + col, nb, Ns, j, j % Ns, stride, tw, pitch);
+  }
+}
+
+// N-point FFTs of the ncols columns of a row-major tile in a (N rows, row
+// pitch `pitch`), into a or b (returned); unnormalised for INV.  Every thread
+// of the block calls it; it ends on a barrier.
+template <bool INV>
+__device__ __forceinline__ float2* fft_cols(float2* a, float2* b, const GPlan& p, const float2* tw, int ncols,
+                                            int pitch, const FastDivU& cdiv) {
+  const int N = p.n;
+  float2* in = a;
+  float2* out = b;
+  int Ns = 1;
+  for (int s = 0; s < p.stages; ++s) {
+    switch (p.r[s]) {
+      case 2: stockham_stage_cols<INV, 2>(in, out, N, Ns, tw, ncols, pitch, cdiv); break;
+      case 3: stockham_stage_cols<INV, 3>(in, out, N, Ns, tw, ncols, pitch, cdiv); break;
+      case 4: stockham_stage_cols<INV, 4>(in, out, N, Ns, tw, ncols, pitch, cdiv); break;
+      case 5: stockham_stage_cols<INV, 5>(in, out, N, Ns, tw, ncols, pitch, cdiv); break;
+      default: stockham_stage_cols<INV, 7>(in, out, N, Ns, tw, ncols, pitch, cdiv); break;
+    }
+    __syncthreads();
+    Ns *= p.r[s];
+    float2* t = in;
+    in = out;
+    out = t;
+  }
+  return in;
 }
 
 // N-point FFTs of the block's nl contiguous lines in a into a or b

@@ -83,31 +83,13 @@ NdTab make_tab(const Model& m, int dt_mode) {
 // Lines of a pass: line (g, i) starts at g * gstride + i and has L points
 // `stride` apart; g < G, i < I.  I == 1: a tile is nl consecutive groups
 // (rows of the x pass, contiguous); I > 1: nl consecutive i of one group.
-// n / d for 0 <= n < 2^31 by a multiply-high and a shift (the round-up
-// method of Granlund and Montgomery, "Division by invariant integers using
-// multiplication", 1994): s = ceil(log2 d), m = floor(2^32 (2^s - d) / d) + 1,
-// n / d = (umulhi(n, m) + n) >> s.
-struct FastDiv {
-  unsigned m, s;
-};
-inline FastDiv make_fastdiv(unsigned d) {
-  FastDiv f;
-  f.s = 0;
-  while ((1ull << f.s) < d) ++f.s;
-  f.m = (unsigned)(((1ull << 32) * ((1ull << f.s) - d)) / d + 1);
-  return f;
-}
-__device__ __forceinline__ int fdiv(int n, FastDiv f) {
-  return (int)((__umulhi((unsigned)n, f.m) + (unsigned)n) >> f.s);
-}
-
 struct Pass {
   float2* data;          // complex planes (in and out, in place)
   const float* src_real;  // IN_REAL: real input of the same geometry
   float* dst_real;        // OUT_REAL: Re(result) * scale (stored, or added when accumulate)
   long G, I, gstride, stride;
   int L, nl;
-  FastDiv fnl;            // division by nl
+  FastDivU fnl;            // division by nl
   int in_real, out_real, accumulate;
   float scale;
 };
@@ -156,7 +138,7 @@ __global__ void __launch_bounds__(kNT, 3) nd_pass_kernel(Pass a, GPlan p) {
         in = idx < valid;
         off = gbase + idx;
       } else {
-        const int j = fdiv(idx, a.fnl), l = idx - j * nl;
+        const int j = a.fnl.div(idx), l = idx - j * nl;
         dst[u] = idx < pts ? l * L + j : -1;
         in = idx < pts && l < lines;
         off = gbase + l + (long)j * a.stride;
@@ -177,7 +159,7 @@ __global__ void __launch_bounds__(kNT, 3) nd_pass_kernel(Pass a, GPlan p) {
       off = gbase + idx;
       src = idx;
     } else {
-      const int j = fdiv(idx, a.fnl), l = idx - j * nl;
+      const int j = a.fnl.div(idx), l = idx - j * nl;
       if (l >= lines) continue;
       off = gbase + l + (long)j * a.stride;
       src = l * L + j;
@@ -249,10 +231,113 @@ cudaError_t run_pass(bool inv, int axis, const NdTab& t, long planes, float2* da
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------- plane passes
+// 3D worlds whose z-planes fit one tile (H W <= kMaxPts): the x and y
+// transforms of a plane in one block -- rows as contiguous lines, then the
+// columns of the same row-major tile -- one global read and write per plane
+// instead of one per axis.  The line transforms and their order are those of
+// the axis passes: x then y forward, y then x inverse.
+struct PlaneArgs {
+  float2* data;           // complex planes (in and out, in place)
+  const float* src_real;  // forward: real input of the same geometry, or null
+  float* dst_real;        // inverse: Re(result) * scale (stored, or added when accumulate), or null
+  int accumulate;
+  float scale;
+  int H, W;
+  FastDivU wdiv;  // division by W
+};
+
+template <bool INV>
+__global__ void __launch_bounds__(kNT, 3) nd_plane_kernel(PlaneArgs a, GPlan px, GPlan py) {
+  extern __shared__ __align__(16) float2 ndsm[];
+  const int H = a.H, W = a.W, pts = H * W;
+  float2* twx = ndsm;
+  float2* twy = twx + W;
+  float2* A = twy + H;
+  float2* B = A + pts;
+  const long base = (long)blockIdx.x * pts;
+  fill_twiddles(twx, W);
+  fill_twiddles(twy, H);
+  constexpr int kLoadBatch = 8;
+  for (int b0 = threadIdx.x; b0 < pts; b0 += kLoadBatch * blockDim.x) {
+    float2 v[kLoadBatch];
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = b0 + u * blockDim.x;
+      v[u] = make_float2(0.f, 0.f);
+      if (idx < pts) v[u] = a.src_real ? make_float2(__ldg(a.src_real + base + idx), 0.f) : a.data[base + idx];
+    }
+#pragma unroll
+    for (int u = 0; u < kLoadBatch; ++u) {
+      const int idx = b0 + u * blockDim.x;
+      if (idx < pts) A[idx] = v[u];
+    }
+  }
+  __syncthreads();
+  float2* r;
+  if (!INV) {
+    r = fft_line<false>(A, B, px, twx, H);                          // x: H rows of W points
+    r = fft_cols<false>(r, r == A ? B : A, py, twy, W, W, a.wdiv);  // y: W columns of H points
+  } else {
+    r = fft_cols<true>(A, B, py, twy, W, W, a.wdiv);
+    r = fft_line<true>(r, r == A ? B : A, px, twx, H);
+  }
+  for (int idx = threadIdx.x; idx < pts; idx += blockDim.x) {
+    const float2 v = r[idx];
+    if (a.dst_real) {
+      const float x = v.x * a.scale;
+      a.dst_real[base + idx] = a.accumulate ? a.dst_real[base + idx] + x : x;
+    } else {
+      a.data[base + idx] = v;
+    }
+  }
+}
+
+bool plane_ok(const NdTab& t) { return t.D > 1 && (long)t.H * t.W <= kMaxPts; }
+
+// Shared memory of the fused plane epilogue (twiddles, two tiles, the
+// channels' fields), or 0 when the world does not take it.
+constexpr size_t kPlaneEpiSmemMax = 200 * 1024;
+size_t plane_epi_smem(const NdTab& t) {
+  if (!plane_ok(t)) return 0;
+  const size_t pts = (size_t)t.H * t.W;
+  const size_t bytes = (t.W + t.H + 2 * pts) * sizeof(float2) + (size_t)t.C * pts * sizeof(float);
+  return bytes <= kPlaneEpiSmemMax ? bytes : 0;
+}
+
+// The x and y transforms of `planes` 3D planes (each D z-planes of H x W).
+cudaError_t run_plane(bool inv, const NdTab& t, long planes, float2* data, const float* src_real, float* dst_real,
+                      bool accumulate, float scale, cudaStream_t st) {
+  PlaneArgs a;
+  a.data = data;
+  a.src_real = src_real;
+  a.dst_real = dst_real;
+  a.accumulate = accumulate ? 1 : 0;
+  a.scale = scale;
+  a.H = t.H;
+  a.W = t.W;
+  a.wdiv = make_fastdiv((unsigned)t.W);
+  const GPlan px = make_plan(t.W), py = make_plan(t.H);
+  if (px.stages == 0 || py.stages == 0) return cudaErrorInvalidValue;
+  const long blocks = planes * t.D;
+  if (blocks >= (1L << 31)) return cudaErrorInvalidConfiguration;
+  const size_t smem = (size_t)(t.W + t.H + 2L * t.H * t.W) * sizeof(float2);
+  cudaError_t e = allow_nd_smem();
+  if (e != cudaSuccess) return e;
+  if (inv) nd_plane_kernel<true><<<(unsigned)blocks, kNT, smem, st>>>(a, px, py);
+  else nd_plane_kernel<false><<<(unsigned)blocks, kNT, smem, st>>>(a, px, py);
+  return cudaGetLastError();
+}
+
 // Full forward transform of real planes (src) into complex planes (dst).
 cudaError_t forward_real(const NdTab& t, long planes, const float* src, float2* dst, cudaStream_t st) {
-  cudaError_t e = run_pass(false, 0, t, planes, dst, src, nullptr, false, 1.f, st);
-  if (e == cudaSuccess) e = run_pass(false, 1, t, planes, dst, nullptr, nullptr, false, 1.f, st);
+  cudaError_t e;
+  if (plane_ok(t)) {
+    e = run_plane(false, t, planes, dst, src, nullptr, false, 1.f, st);
+  } else {
+    e = run_pass(false, 0, t, planes, dst, src, nullptr, false, 1.f, st);
+    if (e == cudaSuccess) e = run_pass(false, 1, t, planes, dst, nullptr, nullptr, false, 1.f, st);
+  }
   if (e == cudaSuccess && t.D > 1) e = run_pass(false, 2, t, planes, dst, nullptr, nullptr, false, 1.f, st);
   return e;
 }
@@ -263,7 +348,9 @@ cudaError_t inverse_real(const NdTab& t, long planes, float2* data, float* dst, 
                          cudaStream_t st) {
   cudaError_t e = cudaSuccess;
   if (t.D > 1) e = run_pass(true, 2, t, planes, data, nullptr, nullptr, false, 1.f, st);
-  if (e == cudaSuccess) e = run_pass(true, 1, t, planes, data, nullptr, nullptr, false, 1.f, st);
+  if (e != cudaSuccess) return e;
+  if (plane_ok(t)) return run_plane(true, t, planes, data, nullptr, dst, accumulate, scale, st);
+  e = run_pass(true, 1, t, planes, data, nullptr, nullptr, false, 1.f, st);
   if (e == cudaSuccess) e = run_pass(true, 0, t, planes, data, nullptr, dst, accumulate, scale, st);
   return e;
 }
@@ -318,7 +405,7 @@ inline int grid_for(long total) { return (int)std::max(1L, std::min<long>((total
 // arithmetic is that of the separate passes, in the same order.
 struct ConvArgs {
   int n_init, L, nl, tiles;  // points per line, lines per tile, tiles per plane
-  FastDiv fnl;               // division by nl
+  FastDivU fnl;               // division by nl
   long I;                    // lines per plane (= point stride along the axis)
   const float2* kf;          // prepared full spectra [Ns, C, max_k, cells]
   long kf_sol_stride;
@@ -332,7 +419,7 @@ struct ConvArgs {
 // nl lines of a plane (points src[l + j I]) into a line-major tile (lines
 // past `lines` read as zero); kLoadBatch loads in flight per thread
 __device__ __forceinline__ void load_lines(float2* dst, const float2* __restrict__ src, long I, int L, int nl,
-                                           FastDiv fnl, int lines) {
+                                           FastDivU fnl, int lines) {
   const int pts = nl * L;
   constexpr int kLoadBatch = 8;
   for (int base = threadIdx.x; base < pts; base += kLoadBatch * blockDim.x) {
@@ -341,7 +428,7 @@ __device__ __forceinline__ void load_lines(float2* dst, const float2* __restrict
 #pragma unroll
     for (int u = 0; u < kLoadBatch; ++u) {
       const int idx = base + u * blockDim.x;
-      const int j = fdiv(idx, fnl), l = idx - j * nl;
+      const int j = fnl.div(idx), l = idx - j * nl;
       d[u] = idx < pts ? l * L + j : -1;
       v[u] = make_float2(0.f, 0.f);
       if (idx < pts && l < lines) v[u] = src[l + (long)j * I];
@@ -353,9 +440,9 @@ __device__ __forceinline__ void load_lines(float2* dst, const float2* __restrict
 }
 
 __device__ __forceinline__ void store_lines(float2* __restrict__ dst, const float2* src, long I, int L, int nl,
-                                            FastDiv fnl, int lines) {
+                                            FastDivU fnl, int lines) {
   for (int idx = threadIdx.x; idx < nl * L; idx += blockDim.x) {
-    const int j = fdiv(idx, fnl), l = idx - j * nl;
+    const int j = fnl.div(idx), l = idx - j * nl;
     if (l < lines) dst[l + (long)j * I] = src[l * L + j];
   }
 }
@@ -430,7 +517,7 @@ __global__ void __launch_bounds__(kNT) nd_adj_conv_kernel(NdTab t, ConvArgs a, G
     __syncthreads();
     float2* g = a.gk + ((long)w * t.K + k) * t.cells + i0;
     for (int idx = threadIdx.x; idx < pts; idx += blockDim.x) {
-      const int j = fdiv(idx, a.fnl), l = idx - j * nl;
+      const int j = a.fnl.div(idx), l = idx - j * nl;
       if (l >= lines) continue;
       const int x = l * L + j;
       const float2 ak = r[x];
@@ -478,33 +565,11 @@ cudaError_t run_conv(bool adjoint, const NdTab& t, long nw, ConvArgs a, cudaStre
   return cudaGetLastError();
 }
 
-cudaError_t allow_nd_smem() {
-  static std::mutex mu;
-  static std::vector<unsigned long long> done;  // contexts already set up
-  unsigned long long ctx = 0;
-  const bool known = current_context_id(&ctx);
-  if (known) {
-    std::lock_guard<std::mutex> lk(mu);
-    if (std::find(done.begin(), done.end(), ctx) != done.end()) return cudaSuccess;
-  }
-  const int pass_bytes = (int)((2 * kMaxPts + kGMaxN) * sizeof(float2));
-  cudaError_t e = cudaFuncSetAttribute(nd_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(nd_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(nd_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(nd_adj_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
-  if (e == cudaSuccess && known) {
-    std::lock_guard<std::mutex> lk(mu);
-    done.push_back(ctx);
-  }
-  return e;
-}
 
 // The axis passes before and after the fused one: forward x (real input)
 // and, in 3D, y; inverse y (3D) and x (real part out).
 cudaError_t forward_real_head(const NdTab& t, long planes, const float* src, float2* dst, cudaStream_t st) {
+  if (plane_ok(t)) return run_plane(false, t, planes, dst, src, nullptr, false, 1.f, st);
   cudaError_t e = run_pass(false, 0, t, planes, dst, src, nullptr, false, 1.f, st);
   if (e == cudaSuccess && t.D > 1) e = run_pass(false, 1, t, planes, dst, nullptr, nullptr, false, 1.f, st);
   return e;
@@ -512,6 +577,7 @@ cudaError_t forward_real_head(const NdTab& t, long planes, const float* src, flo
 
 cudaError_t inverse_real_tail(const NdTab& t, long planes, float2* data, float* dst, bool accumulate, float scale,
                               cudaStream_t st) {
+  if (plane_ok(t)) return run_plane(true, t, planes, data, nullptr, dst, accumulate, scale, st);
   cudaError_t e = cudaSuccess;
   if (t.D > 1) e = run_pass(true, 1, t, planes, data, nullptr, nullptr, false, 1.f, st);
   if (e == cudaSuccess) e = run_pass(true, 0, t, planes, data, nullptr, dst, accumulate, scale, st);
@@ -524,6 +590,7 @@ struct EpiArgs {
   const float* state;   // [nw, C, cells]
   float* state_out;     // [nw, C, cells]
   const float* pot;     // [nw, K, cells]
+  float* pot_out;       // [nw, K, cells] potential trajectory (fused plane epilogue), or null
   const float* gf;      // [Ns, K, 2] (sol stride gf_sol_stride)
   long gf_sol_stride;
   const float* w;       // [Ns, C, K]
@@ -546,29 +613,140 @@ __device__ __forceinline__ float centred_in(int i, int sh, int n) {
   return (float)((d < 0 ? d + n : d) - n / 2);
 }
 
-__global__ void __launch_bounds__(kNT, 3) nd_epilogue_kernel(NdTab t, EpiArgs a) {
+// Per-thread statistics moments of one block of cells (statistics.py:64-100
+// in the centred frame), then the block's partial and, in the world's last
+// block, the step's raw record and the carried shift.
+struct Moments {
+  float m00 = 0.f, g00 = 0.f, cpot = 0.f, cmass = 0.f, cgrow = 0.f;
+  float mx0 = 0.f, mx1 = 0.f, mx2 = 0.f, gx0 = 0.f, gx1 = 0.f, gx2 = 0.f, q0 = 0.f, q1 = 0.f, q2 = 0.f;
+  float cm[kMaxChannels];
+  bool border = false;
+  __device__ Moments() {
+#pragma unroll
+    for (int c = 0; c < kMaxChannels; ++c) cm[c] = 0.f;
+  }
+  // one channel of one cell: entering state sv, field f, centred coordinates
+  __device__ __forceinline__ void add(int c, float sv, float f, float ca, float cb, float cc, bool edge) {
+    const float fp = fmaxf(f, 0.f);
+    m00 += sv;
+    g00 += fp;
+    cm[c] += sv;
+    mx0 = fmaf(ca, sv, mx0);
+    mx1 = fmaf(cb, sv, mx1);
+    mx2 = fmaf(cc, sv, mx2);
+    gx0 = fmaf(ca, fp, gx0);
+    gx1 = fmaf(cb, fp, gx1);
+    gx2 = fmaf(cc, fp, gx2);
+    q0 = fmaf(ca * ca, sv, q0);
+    q1 = fmaf(cb * cb, sv, q1);
+    q2 = fmaf(cc * cc, sv, q2);
+    const bool live = sv > kEps;
+    cmass += live ? 1.f : 0.f;
+    cgrow += fp > kEps ? 1.f : 0.f;
+    border |= live && edge;
+  }
+};
+
+// Block b of world w: reduce the threads' moments into the block's partial;
+// the world's last block to finish (a ticket on the world's counter; no block
+// waits) reduces all of the world's block partials in a fixed order into the
+// step's raw record (with the shift s0..s2 that centred it), then advances
+// the carried shift by the integer part of the centred-frame centroid
+// (statistics.py:117-124).  Every thread of the block calls it.
+__device__ __forceinline__ void epi_finish(const NdTab& t, const EpiArgs& a, int w, int b, int bpw, Moments& mo,
+                                           int s0, int s1, int s2) {
   constexpr int NWARP = kNT / 32;
   __shared__ float red[NWARP][kRawMax];
-  const int w = blockIdx.x / a.bpw, b = blockIdx.x % a.bpw;
+  __shared__ int last;
+  __shared__ float tot[kRawMax];
+  const int C = t.C, nd = t.nd;
   const int sol = w / a.n_init, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  float v[14] = {mo.m00, mo.g00, mo.cpot, mo.cmass, mo.cgrow, mo.mx0, mo.mx1,
+                 mo.mx2, mo.gx0, mo.gx1, mo.gx2, mo.q0,   mo.q1,   mo.q2};
+#pragma unroll
+  for (int i = 0; i < 14; ++i) v[i] = warp_sum(v[i]);
+  const bool anyb = __any_sync(0xffffffffu, mo.border);
+#pragma unroll
+  for (int c = 0; c < kMaxChannels; ++c) {
+    if (c >= C) break;
+    mo.cm[c] = warp_sum(mo.cm[c]);
+  }
+  if (lane == 0) {
+    float* rd = red[wid];
+    rd[RAW_M00] = v[0];
+    rd[RAW_G00] = v[1];
+    rd[RAW_CNT_POT] = v[2];
+    rd[RAW_CNT_MASS] = v[3];
+    rd[RAW_CNT_GROW] = v[4];
+    for (int i = 0; i < 3; ++i) {
+      rd[RAW_MX + i] = v[5 + i];
+      rd[RAW_GX + i] = v[8 + i];
+      rd[RAW_MX2 + i] = v[11 + i];
+    }
+    rd[RAW_BORDER] = anyb ? 1.f : 0.f;
+    for (int i = 0; i < 3; ++i) rd[RAW_SHIFT + i] = 0.f;
+    for (int c = 0; c < C; ++c) rd[RAW_CM + c] = mo.cm[c];
+  }
+  __syncthreads();
+  const int RAWS = raw_stride(C);
+  float* pw = a.partial + (long)w * bpw * RAWS;
+  if (threadIdx.x < RAWS) {
+    float s = 0.f;
+    for (int i = 0; i < NWARP; ++i) s += red[i][threadIdx.x];
+    if (threadIdx.x == RAW_BORDER) s = s > 0.f ? 1.f : 0.f;
+    pw[b * RAWS + threadIdx.x] = s;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(a.done + w, 1) == bpw - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int s = lane; s < RAWS; s += 32) {
+    float acc = 0.f;
+    for (int bb = wid; bb < bpw; bb += NWARP) acc += __ldcg(pw + bb * RAWS + s);
+    red[wid][s] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x < RAWS) {
+    const int s = threadIdx.x;
+    float acc = 0.f;
+    for (int i = 0; i < NWARP; ++i) acc += red[i][s];
+    if (s == RAW_BORDER) acc = acc > 0.f ? 1.f : 0.f;
+    if (s == RAW_SHIFT) acc = (float)s0;
+    if (s == RAW_SHIFT + 1) acc = (float)s1;
+    if (s == RAW_SHIFT + 2) acc = (float)s2;
+    tot[s] = acc;
+    if (a.raw) a.raw[sol * a.raw_sol_stride + (w - sol * a.n_init) * a.raw_init_stride + s] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int n[3] = {nd == 2 ? t.H : t.D, nd == 2 ? t.W : t.H, t.W};
+    const int sh[3] = {s0, s1, s2};
+    for (int i = 0; i < nd; ++i) a.shift[3 * w + i] = pmod(sh[i] + (int)(tot[RAW_MX + i] / (tot[RAW_M00] + kEps)), n[i]);
+    a.done[w] = 0;
+  }
+}
+
+__device__ __forceinline__ float step_dt(const NdTab& t, const EpiArgs& a, int w, int sol) {
+  if (t.dt_mode == 0) return __ldg(a.dt);
+  if (t.dt_mode == 1) return __ldg(a.dt + w);
+  return 1.f / __ldg(a.dt + sol);
+}
+
+__global__ void __launch_bounds__(kNT, 3) nd_epilogue_kernel(NdTab t, EpiArgs a) {
+  const int w = blockIdx.x / a.bpw, b = blockIdx.x % a.bpw;
+  const int sol = w / a.n_init;
   const int C = t.C, K = t.K;
   const float* gf = a.gf + sol * a.gf_sol_stride;
   const float* wt = a.w + sol * a.w_sol_stride;
-  float dt;
-  if (t.dt_mode == 0) dt = __ldg(a.dt);
-  else if (t.dt_mode == 1) dt = __ldg(a.dt + w);
-  else dt = 1.f / __ldg(a.dt + sol);
+  const float dt = step_dt(t, a, w, sol);
   const int nd = t.nd;
   // axis order of the moments: 2D (y, x), 3D (z, y, x)
   const int s0 = a.shift[3 * w], s1 = a.shift[3 * w + 1], s2 = a.shift[3 * w + 2];
   const long chunk = (t.cells + a.bpw - 1) / a.bpw;
   const long c0 = (long)b * chunk, c1 = min(t.cells, c0 + chunk);
-  float m00 = 0.f, g00 = 0.f, cpot = 0.f, cmass = 0.f, cgrow = 0.f;
-  float mx0 = 0.f, mx1 = 0.f, mx2 = 0.f, gx0 = 0.f, gx1 = 0.f, gx2 = 0.f, q0 = 0.f, q1 = 0.f, q2 = 0.f;
-  float cm[kMaxChannels];
-#pragma unroll
-  for (int c = 0; c < kMaxChannels; ++c) cm[c] = 0.f;
-  bool border = false;
+  Moments mo;
   // (x, y, z) of the thread's cell, advanced by the block's stride of kNT
   // cells with one carry per axis (no divisions inside the loop)
   long cell = c0 + threadIdx.x;
@@ -586,7 +764,7 @@ __global__ void __launch_bounds__(kNT, 3) nd_epilogue_kernel(NdTab t, EpiArgs a)
       cc = centred_in(x, s2, t.W);
     }
     const bool edge = x == 0 || x == t.W - 1 || y == 0 || y == t.H - 1 || (nd == 3 && (z == 0 || z == t.D - 1));
-    for (int k = 0; k < K; ++k) cpot += __ldg(a.pot + ((long)w * K + k) * t.cells + cell) > kEps ? 1.f : 0.f;
+    for (int k = 0; k < K; ++k) mo.cpot += __ldg(a.pot + ((long)w * K + k) * t.cells + cell) > kEps ? 1.f : 0.f;
 #pragma unroll
     for (int c = 0; c < kMaxChannels; ++c) {
       if (c >= C) break;
@@ -604,23 +782,7 @@ __global__ void __launch_bounds__(kNT, 3) nd_epilogue_kernel(NdTab t, EpiArgs a)
       a.state_out[off] = state_fn(t.state_fn, sv, f, dt);
       if (a.field_out) a.field_out[off] = f;
       if (a.state_copy) a.state_copy[off] = sv;
-      const float fp = fmaxf(f, 0.f);
-      m00 += sv;
-      g00 += fp;
-      cm[c] += sv;
-      mx0 = fmaf(ca, sv, mx0);
-      mx1 = fmaf(cb, sv, mx1);
-      mx2 = fmaf(cc, sv, mx2);
-      gx0 = fmaf(ca, fp, gx0);
-      gx1 = fmaf(cb, fp, gx1);
-      gx2 = fmaf(cc, fp, gx2);
-      q0 = fmaf(ca * ca, sv, q0);
-      q1 = fmaf(cb * cb, sv, q1);
-      q2 = fmaf(cc * cc, sv, q2);
-      const bool live = sv > kEps;
-      cmass += live ? 1.f : 0.f;
-      cgrow += fp > kEps ? 1.f : 0.f;
-      border |= live && edge;
+      mo.add(c, sv, f, ca, cb, cc, edge);
     }
     x += sx;
     if (x >= t.W) {
@@ -634,77 +796,96 @@ __global__ void __launch_bounds__(kNT, 3) nd_epilogue_kernel(NdTab t, EpiArgs a)
     }
     z += sz;
   }
-  float v[14] = {m00, g00, cpot, cmass, cgrow, mx0, mx1, mx2, gx0, gx1, gx2, q0, q1, q2};
+  epi_finish(t, a, w, b, a.bpw, mo, s0, s1, s2);
+}
+
+// 3D worlds whose z-planes fit one tile: the inverse y and x transforms of
+// every kernel's product plane and the epilogue in one block per (world,
+// z-plane) -- the potentials never leave shared memory (they are stored
+// only as a requested trajectory).  Per channel the weighted field is
+// accumulated over the kernels in order, as in nd_epilogue_kernel, so the
+// results are the same.
+__global__ void __launch_bounds__(kNT, 3) nd_plane_epilogue_kernel(NdTab t, EpiArgs a, const float2* __restrict__ P,
+                                                                GPlan px, GPlan py, FastDivU wdiv) {
+  extern __shared__ __align__(16) float2 ndsm[];
+  const int H = t.H, W = t.W, D = t.D, pts = H * W;
+  const int C = t.C, K = t.K;
+  const int w = blockIdx.x / D, zp = blockIdx.x % D;
+  const int sol = w / a.n_init;
+  float2* twx = ndsm;
+  float2* twy = twx + W;
+  float2* A = twy + H;
+  float2* B = A + pts;
+  float* F = reinterpret_cast<float*>(B + pts);  // [C][pts] weighted fields
+  const float* gf = a.gf + sol * a.gf_sol_stride;
+  const float* wt = a.w + sol * a.w_sol_stride;
+  const float dt = step_dt(t, a, w, sol);
+  const int s0 = a.shift[3 * w], s1 = a.shift[3 * w + 1], s2 = a.shift[3 * w + 2];
+  const long pbase = (long)zp * pts;  // the plane's first cell
+  fill_twiddles(twx, W);
+  fill_twiddles(twy, H);
+  for (int i = threadIdx.x; i < C * pts; i += kNT) F[i] = 0.f;
+  Moments mo;
+  for (int k = 0; k < K; ++k) {
+    const float2* src = P + ((long)w * K + k) * t.cells + pbase;
+    constexpr int kLoadBatch = 8;
+    for (int b0 = threadIdx.x; b0 < pts; b0 += kLoadBatch * kNT) {
+      float2 v[kLoadBatch];
 #pragma unroll
-  for (int i = 0; i < 14; ++i) v[i] = warp_sum(v[i]);
-  const bool anyb = __any_sync(0xffffffffu, border);
+      for (int u = 0; u < kLoadBatch; ++u) {
+        const int idx = b0 + u * kNT;
+        v[u] = idx < pts ? src[idx] : make_float2(0.f, 0.f);
+      }
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u) {
+        const int idx = b0 + u * kNT;
+        if (idx < pts) A[idx] = v[u];
+      }
+    }
+    __syncthreads();
+    float2* r = fft_cols<true>(A, B, py, twy, W, W, wdiv);
+    r = fft_line<true>(r, r == A ? B : A, px, twx, H);
+    const int id = t.gf[k];
+    const float m = __ldg(gf + 2 * k), sg = __ldg(gf + 2 * k + 1);
+    for (int idx = threadIdx.x; idx < pts; idx += kNT) {
+      const float u = r[idx].x;
+      if (a.pot_out) a.pot_out[((long)w * K + k) * t.cells + pbase + idx] = u;
+      mo.cpot += u > kEps ? 1.f : 0.f;
+      const float g = growth_fn(id, u, m, sg);
+      for (int c = 0; c < C; ++c) {
+        const float wk = __ldg(wt + c * K + k);
+        if (wk != 0.f) F[c * pts + idx] = fmaf(wk, g, F[c * pts + idx]);
+      }
+    }
+    __syncthreads();  // A and B are reloaded for the next kernel
+  }
+  float wsum[kMaxChannels];
 #pragma unroll
   for (int c = 0; c < kMaxChannels; ++c) {
-    if (c >= C) break;
-    cm[c] = warp_sum(cm[c]);
+    wsum[c] = 0.f;
+    if (c < C)
+      for (int k = 0; k < K; ++k) wsum[c] += __ldg(wt + c * K + k);
   }
-  if (lane == 0) {
-    float* rd = red[wid];
-    rd[RAW_M00] = v[0];
-    rd[RAW_G00] = v[1];
-    rd[RAW_CNT_POT] = v[2];
-    rd[RAW_CNT_MASS] = v[3];
-    rd[RAW_CNT_GROW] = v[4];
-    for (int i = 0; i < 3; ++i) {
-      rd[RAW_MX + i] = v[5 + i];
-      rd[RAW_GX + i] = v[8 + i];
-      rd[RAW_MX2 + i] = v[11 + i];
+  const float ca = centred_in(zp, s0, D);
+  const bool zedge = zp == 0 || zp == D - 1;
+  for (int idx = threadIdx.x; idx < pts; idx += kNT) {
+    const int y = wdiv.div(idx), x = idx - y * W;
+    const float cb = centred_in(y, s1, H), cc = centred_in(x, s2, W);
+    const bool edge = zedge || x == 0 || x == W - 1 || y == 0 || y == H - 1;
+#pragma unroll
+    for (int c = 0; c < kMaxChannels; ++c) {
+      if (c >= C) break;
+      float f = F[c * pts + idx];
+      if (t.mean) f = f / wsum[c];
+      const long off = ((long)w * C + c) * t.cells + pbase + idx;
+      const float sv = __ldg(a.state + off);
+      a.state_out[off] = state_fn(t.state_fn, sv, f, dt);
+      if (a.field_out) a.field_out[off] = f;
+      if (a.state_copy) a.state_copy[off] = sv;
+      mo.add(c, sv, f, ca, cb, cc, edge);
     }
-    rd[RAW_BORDER] = anyb ? 1.f : 0.f;
-    for (int i = 0; i < 3; ++i) rd[RAW_SHIFT + i] = 0.f;
-    for (int c = 0; c < C; ++c) rd[RAW_CM + c] = cm[c];
   }
-  __syncthreads();
-  const int RAWS = raw_stride(C);
-  float* pw = a.partial + (long)w * a.bpw * RAWS;
-  if (threadIdx.x < RAWS) {
-    float s = 0.f;
-    for (int i = 0; i < NWARP; ++i) s += red[i][threadIdx.x];
-    if (threadIdx.x == RAW_BORDER) s = s > 0.f ? 1.f : 0.f;
-    pw[b * RAWS + threadIdx.x] = s;
-    __threadfence();
-  }
-  // The world's last block to finish (a ticket on the world's counter; no
-  // block waits) reduces all of the world's block moments in a fixed order
-  // into the step's raw record (with the shift that centred it), then
-  // advances the carried shift by the integer part of the centred-frame
-  // centroid (statistics.py:117-124).
-  __shared__ int last;
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(a.done + w, 1) == a.bpw - 1;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  for (int s = lane; s < RAWS; s += 32) {
-    float v = 0.f;
-    for (int bb = wid; bb < a.bpw; bb += NWARP) v += __ldcg(pw + bb * RAWS + s);
-    red[wid][s] = v;
-  }
-  __syncthreads();
-  __shared__ float tot[kRawMax];
-  if (threadIdx.x < RAWS) {
-    const int s = threadIdx.x;
-    float v = 0.f;
-    for (int i = 0; i < NWARP; ++i) v += red[i][s];
-    if (s == RAW_BORDER) v = v > 0.f ? 1.f : 0.f;
-    if (s == RAW_SHIFT) v = (float)s0;
-    if (s == RAW_SHIFT + 1) v = (float)s1;
-    if (s == RAW_SHIFT + 2) v = (float)s2;
-    tot[s] = v;
-    if (a.raw) a.raw[sol * a.raw_sol_stride + (w - sol * a.n_init) * a.raw_init_stride + s] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int n[3] = {nd == 2 ? t.H : t.D, nd == 2 ? t.W : t.H, t.W};
-    const int sh[3] = {s0, s1, s2};
-    for (int i = 0; i < nd; ++i) a.shift[3 * w + i] = pmod(sh[i] + (int)(tot[RAW_MX + i] / (tot[RAW_M00] + kEps)), n[i]);
-    a.done[w] = 0;
-  }
+  epi_finish(t, a, w, zp, D, mo, s0, s1, s2);
 }
 
 // ------------------------------------------------------------------ adjoint
@@ -961,6 +1142,38 @@ __global__ void nd_sum_inits_kernel(long per_sol, int n_sols, int n_init, const 
   }
 }
 
+cudaError_t allow_nd_smem() {
+  static std::mutex mu;
+  static std::vector<unsigned long long> done;  // contexts already set up
+  unsigned long long ctx = 0;
+  const bool known = current_context_id(&ctx);
+  if (known) {
+    std::lock_guard<std::mutex> lk(mu);
+    if (std::find(done.begin(), done.end(), ctx) != done.end()) return cudaSuccess;
+  }
+  const int pass_bytes = (int)((2 * kMaxPts + kGMaxN) * sizeof(float2));
+  cudaError_t e = cudaFuncSetAttribute(nd_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
+  const int plane_bytes = (int)((2 * kMaxPts + 2 * kGMaxN) * sizeof(float2));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_plane_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plane_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_plane_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, plane_bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_plane_epilogue_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kPlaneEpiSmemMax);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(nd_adj_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kConvSmemMax);
+  if (e == cudaSuccess && known) {
+    std::lock_guard<std::mutex> lk(mu);
+    done.push_back(ctx);
+  }
+  return e;
+}
+
 inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 }  // namespace
@@ -994,7 +1207,8 @@ int nd_param_blocks(const Model& m, long n_worlds) { return nd_blocks_per_world(
 size_t nd_step_workspace_bytes(const Model& m, int n_worlds) {
   const size_t nw = (size_t)n_worlds, cells = (size_t)m.cells;
   return al256(nw * m.C * cells * sizeof(float2)) + al256(nw * m.K * cells * sizeof(float2)) +
-         al256(nw * m.K * cells * sizeof(float)) + al256(nw * nd_blocks_per_world(m, (long)nw) * raw_stride(m.C) * sizeof(float));
+         al256(nw * m.K * cells * sizeof(float)) +
+         al256(nw * std::max(nd_blocks_per_world(m, (long)nw), m.D) * raw_stride(m.C) * sizeof(float));
 }
 
 size_t nd_prepared_bytes(const Model& m, int n_sols) {
@@ -1031,7 +1245,8 @@ cudaError_t launch_nd_step(const NdStep& s, cudaStream_t st) {
   ca.S = S;
   ca.P = P;
   if ((e = run_conv(false, t, (long)nw, ca, st)) != cudaSuccess) return e;
-  if ((e = inverse_real_tail(t, (long)nw * m.K, P, pot, false, 1.f, st)) != cudaSuccess) return e;
+  const bool fused = plane_epi_smem(t) > 0;
+  if (!fused && (e = inverse_real_tail(t, (long)nw * m.K, P, pot, false, 1.f, st)) != cudaSuccess) return e;
   EpiArgs a;
   a.n_worlds = s.n_worlds;
   a.n_init = s.n_init;
@@ -1052,7 +1267,15 @@ cudaError_t launch_nd_step(const NdStep& s, cudaStream_t st) {
   a.raw = s.raw;
   a.raw_sol_stride = s.raw_sol_stride;
   a.raw_init_stride = s.raw_world_stride;
-  nd_epilogue_kernel<<<(unsigned)(nw * bpw), kNT, 0, st>>>(t, a);
+  a.pot_out = s.pot_out;
+  if (fused) {
+    if ((e = allow_nd_smem()) != cudaSuccess) return e;
+    a.bpw = m.D;
+    nd_plane_epilogue_kernel<<<(unsigned)(nw * m.D), kNT, plane_epi_smem(t), st>>>(
+        t, a, P, make_plan(m.W), make_plan(m.H), make_fastdiv((unsigned)m.W));
+  } else {
+    nd_epilogue_kernel<<<(unsigned)(nw * bpw), kNT, 0, st>>>(t, a);
+  }
   return cudaGetLastError();
 }
 
