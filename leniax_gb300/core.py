@@ -44,6 +44,39 @@ def half_spectrum(K: torch.Tensor, world: Sequence[int]) -> torch.Tensor:
     return torch.view_as_real(K.contiguous())
 
 
+def direct_spectrum(K: torch.Tensor, world: Sequence[int], nb_channels: int, max_k: int) -> torch.Tensor:
+    """The real kernels of leniax's direct-convolution path, ``[...,
+    C*max_k, 1, *kernel_dims]``, as the engine's half spectra ``[..., C,
+    max_k, *world[:-1], W//2+1]`` complex64.
+
+    leniax applies them with ``core.get_potential`` (core.py:105-146): the
+    state wrap-padded by ``k//2`` before each axis (helpers.py:465-481), then
+    a VALID cross-correlation, i.e. potential[x] = sum_d state[x + d - k//2]
+    K[d].  Placing tap d of every axis at the world index (k//2 - d) mod n
+    (taps that land on the same index add up when a kernel is longer than
+    the world) gives a world-sized kernel whose FFT convolution is that same
+    sum, so the engine's FFT path computes the direct path's potential."""
+    from .grad import kernel_spectrum  # the device real-to-half FFT of world-sized kernels
+    nd = len(world)
+    world = tuple(int(w) for w in world)
+    if K.dim() < nd + 2 or K.shape[-nd - 1] != 1 or K.shape[-nd - 2] != nb_channels * max_k:
+        raise ValueError(f'direct-path kernels {tuple(K.shape)} are not [..., {nb_channels * max_k}, 1, *kernel_dims]')
+    _require_cuda('K', K)
+    lead = tuple(K.shape[:-nd - 2])
+    kd = tuple(int(k) for k in K.shape[-nd:])
+    dev = K.device
+    vals = K.reshape((-1, ) + kd)  # [planes, *kernel_dims]
+    planes = vals.shape[0]
+    kw = torch.zeros((planes, ) + world, dtype=torch.float32, device=dev)
+    axes = [(k // 2 - torch.arange(k, device=dev)) % n for k, n in zip(kd, world)]
+    grids = torch.meshgrid(*axes, indexing='ij')
+    pidx = torch.arange(planes, device=dev).view((planes, ) + (1, ) * nd).expand((planes, ) + kd)
+    kw.index_put_((pidx, ) + tuple(g.unsqueeze(0).expand((planes, ) + kd) for g in grids), vals,
+                  accumulate=True)
+    half = kernel_spectrum(kw, nd)
+    return half.reshape(lead + (nb_channels, max_k) + tuple(half.shape[1:]))
+
+
 def workspace(nbytes: int, device) -> torch.Tensor:
     return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
 
@@ -84,21 +117,75 @@ class UpdateFn:
 
     def __init__(self, kernel_shape: Sequence[int], mapping: KernelMapping, get_state_fn_slug='v1',
                  average_weight=True, fft=True):
-        if not fft:
-            raise NotImplementedError('the engine computes the potential by FFT only (core.get_potential_fft)')
         kernel_shape = tuple(int(s) for s in kernel_shape)
         self.kernel_shape = kernel_shape
-        self.model = Model(kernel_shape[3:], kernel_shape[1], mapping, get_state_fn_slug, average_weight)
+        self.fft = bool(fft)
+        self._mapping, self._slug, self._average = mapping, get_state_fn_slug, average_weight
+        self._models = {}
+        self._cached = None  # (K, K._version, world, half spectra) of the direct path
+        if self.fft:
+            self._model = Model(kernel_shape[3:], kernel_shape[1], mapping, get_state_fn_slug, average_weight)
+            self._models[self._model.world] = self._model
+        else:
+            # fft=False (helpers.py:465-487): K is [C*max_k, 1, *kernel_dims];
+            # the world is the state's, known at the first call
+            nb_channels = len(mapping.cin_kernels)
+            max_k = mapping.kernel_table()[3]
+            if len(kernel_shape) not in (4, 5) or kernel_shape[0] != nb_channels * max_k or kernel_shape[1] != 1:
+                raise ValueError(f'direct-path kernel shape {kernel_shape} is not [{nb_channels * max_k}, 1, '
+                                 '*kernel_dims]')
+            self._nb_channels = nb_channels
+            self._model = None
+
+    @property
+    def model(self) -> Model:
+        if self._model is None:
+            raise ValueError('a direct-path (fft=False) update function learns its world from the first state it '
+                             'is given: use model_for(world)')
+        return self._model
+
+    def model_for(self, world: Sequence[int]) -> Model:
+        """The engine model for worlds of shape ``world`` (the one fixed
+        model for fft=True, one per world shape for fft=False)."""
+        world = tuple(int(w) for w in world)
+        if self.fft:
+            if world != self._model.world:
+                raise ValueError(f'world {world} does not match the kernels\' world {self._model.world}')
+            return self._model
+        m = self._models.get(world)
+        if m is None:
+            m = Model(world, self._nb_channels, self._mapping, self._slug, self._average)
+            self._models[world] = m
+        self._model = m
+        return m
+
+    def spectra(self, K: torch.Tensor, world: Sequence[int]) -> torch.Tensor:
+        """The engine's half spectra (float32 view ``[..., C, max_k,
+        *world_half, 2]``) of ``K``: leniax's FFT kernels (full or half
+        spectrum) for fft=True, the direct path's real kernels for fft=False
+        (converted once per tensor and in-place version)."""
+        if self.fft:
+            return half_spectrum(K, world)
+        world = tuple(int(w) for w in world)
+        c = self._cached
+        if c is not None and c[0] is K and c[1] == K._version and c[2] == world:
+            return c[3]
+        m = self.model_for(world)
+        kh = torch.view_as_real(direct_spectrum(K.to(torch.float32), world, m.C, m.max_k).contiguous())
+        self._cached = (K, K._version, world, kh)
+        return kh
 
     def __call__(self, rng_key, state, K, gf_params, kernels_weight_per_channel, dt):
-        m = self.model
         _require_cuda('state', state)
-        if tuple(state.shape[2:]) != m.world or state.shape[1] != m.C:
+        m = self.model_for(state.shape[2:])
+        if state.shape[1] != m.C:
             raise ValueError(f'state shape {tuple(state.shape)} does not match [N, {m.C}, *{m.world}]')
         dev = state.device
         N = state.shape[0]
         state = state.contiguous()
-        kh = half_spectrum(K.to(dev), m.world)
+        kh = self.spectra(K if K.device == dev else K.to(dev), m.world)
+        if not self.fft:
+            kh = kh.unsqueeze(0)
         if kh.shape[0] != 1:
             raise ValueError('update shares one spectrum across the batch: K must be [1, C, max_k, ...]')
         gf = gf_params.to(dev, torch.float32).contiguous()

@@ -165,7 +165,7 @@ class LeniaRolloutFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, cells0, k_real, gf_params, weights, T, update_fn: UpdateFn, steps: int, checkpoint_every: int,
                 clip_grad: str, engine: str = 'auto'):
-        m = update_fn.model
+        m = update_fn.model_for(cells0.shape[3:])
         dev = cells0.device
         Ns, Ni = cells0.shape[:2]
         nd = len(m.world)
@@ -198,7 +198,7 @@ class LeniaRolloutFunction(torch.autograd.Function):
         if steps == 0:
             return grad_final, torch.zeros(ctx.k_shape, device=grad_final.device), torch.zeros_like(gf), \
                 torch.zeros_like(w), None, None, None, None, None, None
-        m = update_fn.model
+        m = update_fn.model_for(ckpts[0].shape[3:])
         dev = grad_final.device
         Ns, Ni = ckpts[0].shape[:2]
         lib = _bind(_lib.load())
@@ -260,7 +260,7 @@ class LeniaRolloutFunction(torch.autograd.Function):
 
 def _segment(update_fn, cells, k_half, gf, w, Tt, n, traj, engine='auto'):
     """n Euler steps from `cells` through lgx_run (no statistics needed)."""
-    m = update_fn.model
+    m = update_fn.model_for(cells.shape[3:])
     dev = cells.device
     Ns, Ni = cells.shape[:2]
     lib = _lib.load()

@@ -147,10 +147,23 @@ class KernelMapping:
         return cin, slot, gfs, max_k
 
 
+def crop_zero(kernels: np.ndarray) -> np.ndarray:
+    """utils.py:296-317: drop every index of each world axis at which all
+    kernels are zero (the masks are taken on the uncropped array)."""
+    nz = kernels != 0
+    keep = []
+    for ax in range(1, kernels.ndim):
+        others = tuple(a for a in range(kernels.ndim) if a != ax)
+        keep.append(np.nonzero(np.any(nz, axis=others))[0])
+    return kernels[np.ix_(np.arange(kernels.shape[0]), *keep)]
+
+
 def get_kernels_and_mapping(kernels_params: List[Dict], world_size: Sequence[int], nb_channels: int, R: float,
                             fft: bool = True, device=None) -> Tuple[torch.Tensor, KernelMapping]:
     """kernels.py:66-158.  Returns the spectrum ``[1, C, max_k, *world]``
-    complex64 (``fft=True``) on ``device`` (default: current CUDA device)."""
+    complex64 (``fft=True``), or the cropped real kernels ``[C*max_k, 1,
+    *kernel_dims]`` of the direct-convolution path (``fft=False``), on
+    ``device`` (default: current CUDA device)."""
     if device is None:
         device = torch.device('cuda', torch.cuda.current_device()) if torch.cuda.is_available() else 'cpu'
     nb_dims = len(world_size)
@@ -176,6 +189,8 @@ def get_kernels_and_mapping(kernels_params: List[Dict], world_size: Sequence[int
         mapping.cin_k_params[c_in].append(p['k_params'])
         mapping.kernels_weight_per_channel[p['c_out']][kernel_idx] = p['h']
     kernels = np.concatenate(padded, axis=0).astype(np.float32)
+    if not fft:
+        kernels = crop_zero(kernels)  # kernels.py:118-119
     kshape = kernels.shape[1:]
     max_k = max(map(len, mapping.cin_kernels))
     per_channel, true_channels = [], []

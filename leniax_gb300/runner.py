@@ -12,7 +12,7 @@ import torch
 
 from . import _lib
 from .constant import EPSILON, START_CHECK_STOP
-from .core import UpdateFn, _require_cuda, _stream_handle, half_spectrum, workspace
+from .core import UpdateFn, _require_cuda, _stream_handle, workspace
 from .statistics import ComputeStatsFn, split_stats
 from . import statistics as lstat
 
@@ -20,9 +20,10 @@ from . import statistics as lstat
 def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, gf_params, w, T, max_run_iter,
              keep_intermediary: bool, engine: str, with_box: bool, with_centroid: bool = False,
              check_status: bool = False):
-    """cells0 [Ns, Ni, C, *world], K [Ns, C, max_k, *world(-half)], gf [Ns, K, 2], w [Ns, C, K], T [Ns]."""
-    m = update_fn.model
+    """cells0 [Ns, Ni, C, *world], K [Ns, C, max_k, *world(-half)] (fft=True) or [Ns, C*max_k, 1,
+    *kernel_dims] (fft=False), gf [Ns, K, 2], w [Ns, C, K], T [Ns]."""
     _require_cuda('cells0', cells0)
+    m = update_fn.model_for(cells0.shape[3:])
     dev = cells0.device
     Ns, Ni = cells0.shape[0], cells0.shape[1]
     if tuple(cells0.shape[2:]) != (m.C, ) + m.world:
@@ -31,7 +32,7 @@ def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, g
     if steps < 0:
         raise ValueError('max_run_iter must be >= 0')
     cells0 = cells0.contiguous()
-    kh = half_spectrum(K.to(dev), m.world)
+    kh = update_fn.spectra(K if K.device == dev else K.to(dev), m.world)
     if kh.shape[0] != Ns:
         raise ValueError('K must hold one spectrum per solution')
     gf = gf_params.to(dev, torch.float32).reshape(Ns, m.K, 2).contiguous()
@@ -87,7 +88,9 @@ def run_scan(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_r
              with_box: bool = False, with_centroid: bool = False, check_status: bool = False):
     """runner.py:119-164.
 
-    cells0 ``[N_init, C, *world]``; K ``[1, C, max_k, *world]`` complex64;
+    cells0 ``[N_init, C, *world]``; K ``[1, C, max_k, *world]`` complex64
+    (or, for an fft=False update function, the direct path's real kernels
+    ``[C*max_k, 1, *kernel_dims]``);
     returns ``(cells, field, potential, stats)`` with ``cells``/``field``
     ``[T, N_init, C, *world]``, ``potential`` ``[T, N_init, K, *world]`` and
     ``stats[k]`` ``[T, N_init]`` (``channel_mass`` ``[T, N_init, C]``) plus
@@ -96,10 +99,12 @@ def run_scan(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_r
     N_init, nb_dims]``, the per-step mass centroid as an absolute torus
     position.
     """
-    m = update_fn.model
-    final, stats, ncont, nbox, traj, cen = _rollout(update_fn, compute_stats_fn, cells0.unsqueeze(0), K.reshape(
-        (1, ) + tuple(K.shape[1:])), gf_params.unsqueeze(0), kernels_weight_per_channel.unsqueeze(0), T, max_run_iter,
-                                                    True, engine, with_box, with_centroid, check_status)
+    _require_cuda('cells0', cells0)
+    m = update_fn.model_for(cells0.shape[2:])
+    Kb = K.reshape((1, ) + tuple(K.shape[1:])) if update_fn.fft else K.unsqueeze(0)
+    final, stats, ncont, nbox, traj, cen = _rollout(update_fn, compute_stats_fn, cells0.unsqueeze(0), Kb,
+                                                    gf_params.unsqueeze(0), kernels_weight_per_channel.unsqueeze(0), T,
+                                                    max_run_iter, True, engine, with_box, with_centroid, check_status)
     sd = split_stats(stats[0], m.C)
     sd['N'] = ncont[0]
     if nbox is not None:
@@ -115,7 +120,8 @@ def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_cha
                            with_box: bool = False, with_centroid: bool = False, check_status: bool = False):
     """runner.py:167-215: all solutions x inits in one engine launch.
 
-    cells0 ``[N_sols, N_init, C, *world]``; K ``[N_sols, 1, C, max_k, *world]``;
+    cells0 ``[N_sols, N_init, C, *world]``; K ``[N_sols, 1, C, max_k, *world]``
+    (fft=False: ``[N_sols, C*max_k, 1, *kernel_dims]``);
     gf_params ``[N_sols, K, 2]``; weights ``[N_sols, C, K]``; T ``[N_sols]``.
     Returns ``(stats, final_cells)``: ``stats[k]`` ``[N_sols, T, N_init]``
     (``channel_mass`` ``[N_sols, T, N_init, C]``), ``stats['N']``
@@ -123,9 +129,10 @@ def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_cha
     ``check_status=True`` synchronises after the launch and raises if the
     engine's device status word reports a staged copy that never landed.
     """
-    m = update_fn.model
+    _require_cuda('cells0', cells0)
+    m = update_fn.model_for(cells0.shape[3:])
     Ns = cells0.shape[0]
-    Kr = K.reshape((Ns, ) + tuple(K.shape[2:])) if K.dim() == 3 + len(m.world) + 1 else K
+    Kr = K.reshape((Ns, ) + tuple(K.shape[2:])) if update_fn.fft and K.dim() == 3 + len(m.world) + 1 else K
     final, stats, ncont, nbox, _, cen = _rollout(update_fn, compute_stats_fn, cells0, Kr, gf_params,
                                                  kernels_weight_per_channel, T, max_run_iter, False, engine, with_box,
                                                  with_centroid, check_status)

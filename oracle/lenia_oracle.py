@@ -251,10 +251,16 @@ def _pad_kernel(k, world_size):
 
 
 def crop_zero(kernels):
-    """utils.crop_zero: drop all-zero border rows/columns (3-D array)."""
-    nz = np.nonzero(np.abs(kernels).sum(axis=0))
-    sl = tuple(slice(int(a.min()), int(a.max()) + 1) for a in nz)
-    return kernels[(slice(None), ) + sl]
+    """utils.py:296-317: remove, along each world axis, every index where
+    all kernels are zero (interior ones included); the zero masks are those
+    of the uncropped array."""
+    where_zero = kernels == 0
+    out = kernels
+    for ax in range(1, kernels.ndim):
+        others = tuple(a for a in range(kernels.ndim) if a != ax)
+        keep = ~np.all(where_zero, axis=others)
+        out = np.compress(keep, out, axis=ax)
+    return out
 
 
 def get_kernels_and_mapping(kernels_params: List[Dict], world_size: Sequence[int], nb_channels: int, R: float,
@@ -344,23 +350,33 @@ def get_potential_fft(state, K, tc_indices=None, workers=None):
 
 def get_potential_conv(state, K, padding, tc_indices=None):
     """core.py:105-146: wrap-pad then depthwise VALID cross-correlation
-    (``lax.conv_general_dilated`` with ``feature_group_count=C``)."""
+    (``lax.conv_general_dilated`` with ``feature_group_count=C``), over the
+    2 or 3 world axes."""
     C = state.shape[1]
     padded = np.pad(state, padding, mode='wrap')
     O = K.shape[0]
     per_group = O // C
-    kh, kw = K.shape[-2:]
-    H = padded.shape[2] - kh + 1
-    W = padded.shape[3] - kw + 1
-    out = np.zeros((state.shape[0], O, H, W), dtype=state.dtype)
+    kd = K.shape[2:]
+    out_dims = tuple(padded.shape[2 + i] - kd[i] + 1 for i in range(len(kd)))
+    out = np.zeros((state.shape[0], O) + out_dims, dtype=state.dtype)
     for o in range(O):
         c = o // per_group
-        for i in range(kh):
-            for j in range(kw):
-                out[:, o] += K[o, 0, i, j] * padded[:, c, i:i + H, j:j + W]
+        for tap in np.ndindex(*kd):
+            window = tuple(slice(t, t + n) for t, n in zip(tap, out_dims))
+            out[:, o] += K[(o, 0) + tap] * padded[(slice(None), c) + window]
     if tc_indices is not None:
         out = np.take(out, np.array(tc_indices), axis=1)
     return out
+
+
+def update_conv(state, K, gf_params, weights, dt, model):
+    """core.py:13-49 with the direct-convolution potential (fft=False):
+    ``K`` ``[C*max_k, 1, *kernel_dims]`` with the padding of
+    helpers.py:465-481."""
+    potential = get_potential_conv(state, K, conv_padding(K.shape), model.tc_indices)
+    field = get_field(potential, gf_params, weights, model.gf_slugs, model.average)
+    new_state = STATE_REGISTER[model.state_slug](state, field, dt)
+    return new_state, field, potential
 
 
 def conv_padding(kernel_shape):

@@ -1,0 +1,46 @@
+"""The direct-convolution path's kernels (leniax ``fft=False``,
+kernels.py:66-158 with utils.crop_zero): the product's cropped real kernels
+``[C*max_k, 1, *kernel_dims]`` equal the oracle's, value for value, for the
+golden models and a 3D world.  Host-only."""
+import numpy as np
+import pytest
+
+from leniax_gb300 import kernels
+from oracle import lenia_oracle as O
+from tests.cases import bump_kernel_params, golden_case
+
+
+def _both(kp, world, C, R):
+    Kp, mp = kernels.get_kernels_and_mapping([dict(p) for p in kp], list(world), C, R, False, 'cpu')
+    Ko, mpo = O.get_kernels_and_mapping([dict(p) for p in kp], list(world), C, R, False, np.float32)
+    return Kp.numpy(), mp, Ko, mpo
+
+
+@pytest.mark.parametrize('name', ['orbium', 'orbium_scutium', 'aquarium'])
+def test_direct_kernels_match_the_oracle(name):
+    cfg, _, _ = golden_case(name)
+    Kp, mp, Ko, mpo = _both(cfg['kernels_params'], cfg['world_size'], cfg['nb_channels'], cfg['R'])
+    assert Kp.shape == Ko.shape and Kp.shape[1] == 1
+    assert Kp.shape[0] == cfg['nb_channels'] * max(map(len, mp.cin_kernels))
+    assert (mp.true_channels is None) == (mpo['true_channels'] is None)
+    np.testing.assert_allclose(Kp, Ko, rtol=1e-6, atol=1e-9)
+
+
+def test_direct_kernels_3d_and_crop():
+    Kp, mp, Ko, _ = _both(bump_kernel_params(), [24, 20, 16], 1, 5.0)
+    # a ring of radius 5 cropped to its support (the bump is zero on the rim)
+    assert Kp.shape == Ko.shape and Kp.shape[:2] == (1, 1) and len(set(Kp.shape[2:])) == 1
+    assert Kp.shape[2] % 2 == 1 and Kp.shape[2] < 11
+    np.testing.assert_allclose(Kp, Ko, rtol=1e-6, atol=1e-9)
+
+
+def test_crop_zero_removes_every_all_zero_index():
+    # utils.py:296-317 drops interior all-zero rows too, not only the border
+    k = np.zeros((2, 5, 6), np.float32)
+    k[0, 0, 1] = 1
+    k[1, 4, 4] = 2
+    k[0, 2, 5] = 3
+    got = kernels.crop_zero(k)
+    want = O.crop_zero(k)
+    assert got.shape == want.shape == (2, 3, 3)  # rows 0, 2, 4; columns 1, 4, 5
+    np.testing.assert_array_equal(got, want)
