@@ -264,6 +264,28 @@ LGX_API size_t lgx_kernel_spectrum_nd_workspace_bytes(int nb_dims, const int* wo
 LGX_API int lgx_kernel_spectrum_nd(int nb_dims, const int* world, int planes, const float* k_real, float* k_half,
                                    void* workspace, size_t workspace_bytes, void* stream);
 
+/* The step's pointwise stages on their own, for callers of leniax's building
+ * blocks (every pointer a device pointer, stream-ordered, no workspace):
+ *   lgx_growth   replaces the growth_functions.* calls of core.get_field
+ *                (growth_functions.py:6-253): out[n, K, cells] = growth_k(potential)
+ *                with gf_ids[k] (host array of K LGX_GF_* ids) and gf_params [K, 2];
+ *   lgx_weighted replaces core.weighted_sum / weighted_mean (core.py:202-242):
+ *                out[n, C, cells] = sum_k weights[c, k] fields[n, k] (divided by
+ *                sum_k weights[c, k] when mean != 0);
+ *   lgx_field    replaces core.get_field (core.py:163-199): growth and merge fused;
+ *   lgx_state    replaces core.get_state / get_state_v2 / get_state_simple
+ *                (core.py:245-319): out = f(state, field, dt) for LGX_STATE_* id,
+ *                dt a scalar (dt_per_world 0) or [n].
+ * Shapes: n worlds, K kernels <= 64, C channels <= 16, `cells` per plane. */
+LGX_API int lgx_growth(int n, int K, long cells, const int* gf_ids, const float* potential, const float* gf_params,
+                       float* out, void* stream);
+LGX_API int lgx_weighted(int n, int K, int C, long cells, const float* fields, const float* weights, int mean,
+                         float* out, void* stream);
+LGX_API int lgx_field(int n, int K, int C, long cells, const int* gf_ids, const float* potential,
+                      const float* gf_params, const float* weights, int mean, float* field, void* stream);
+LGX_API int lgx_state(int n, int C, long cells, int state_fn, const float* state, const float* field,
+                      const float* dt, int dt_per_world, float* out, void* stream);
+
 /* Measurement helper (no counterpart in the reference): launch a pure-FMA
  * kernel of `blocks` x 256 threads and return the number of FP32 flops it
  * performs (or -1).  Timing it with events gives the FP32-pipe peak used as

@@ -37,7 +37,8 @@ EXPORTED = (
     'lgx_run_workspace_bytes', 'lgx_run', 'lgx_update_workspace_bytes', 'lgx_update', 'lgx_fp32_probe',
     'lgx_batch_workspace_bytes', 'lgx_batch_run', 'lgx_workspace_status', 'lgx_ring_kernels_workspace_bytes',
     'lgx_ring_kernels', 'lgx_selftest_wait_timeout', 'lgx_adjoint_kernel_grad_acc_bytes', 'lgx_kernel_spectrum_nd',
-    'lgx_kernel_spectrum_nd_workspace_bytes', 'lgx_plan_set_adjoint_engine'
+    'lgx_kernel_spectrum_nd_workspace_bytes', 'lgx_plan_set_adjoint_engine', 'lgx_growth', 'lgx_weighted',
+    'lgx_field', 'lgx_state'
 )
 
 
@@ -130,6 +131,13 @@ def load():
         lib.lgx_fp32_probe.restype = ctypes.c_longlong
         lib.lgx_selftest_wait_timeout.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
         lib.lgx_selftest_wait_timeout.restype = ctypes.c_int
+        vp, ci, cl = ctypes.c_void_p, ctypes.c_int, ctypes.c_long
+        lib.lgx_growth.argtypes = [ci, ci, cl, ctypes.POINTER(ci), vp, vp, vp, vp]
+        lib.lgx_weighted.argtypes = [ci, ci, ci, cl, vp, vp, ci, vp, vp]
+        lib.lgx_field.argtypes = [ci, ci, ci, cl, ctypes.POINTER(ci), vp, vp, vp, ci, vp, vp]
+        lib.lgx_state.argtypes = [ci, ci, cl, ci, vp, vp, vp, ci, vp, vp]
+        for f in (lib.lgx_growth, lib.lgx_weighted, lib.lgx_field, lib.lgx_state):
+            f.restype = ci
         if lib.lgx_version() != 1:
             raise RuntimeError('leniax_gb300 engine ABI version mismatch')
         _lib = lib

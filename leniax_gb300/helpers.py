@@ -1,12 +1,17 @@
 """Pipeline builders (leniax ``helpers.py``): ``build_update_fn``
-(helpers.py:401-427), ``init`` (35-88), ``create_init_cells`` (91-128) and
-``init_and_run`` (131-189) for v2 configurations whose cells are arrays."""
+(helpers.py:401-427), ``build_get_potential_fn`` (430-487),
+``build_get_field_fn`` (490-516), ``init`` (35-88), ``create_init_cells``
+(91-128) and ``init_and_run`` (131-189) for v2 configurations whose cells
+are arrays."""
 import copy
-from typing import Dict, List, Sequence
+import functools
+from typing import Dict, List, Optional, Sequence
 
 import numpy as np
 import torch
 
+from . import core as lcore
+from . import growth_functions as lgf
 from . import kernels as lkernels
 from . import runner as lrunner
 from . import statistics as lstat
@@ -17,6 +22,31 @@ def build_update_fn(kernel_shape: Sequence[int], mapping: lkernels.KernelMapping
                     average_weight: bool = True, fft: bool = True) -> UpdateFn:
     """helpers.py:401-427"""
     return UpdateFn(kernel_shape, mapping, get_state_fn_slug, average_weight, fft)
+
+
+def build_get_potential_fn(kernel_shape: Sequence[int], true_channels: Optional[List[bool]] = None, fft: bool = True,
+                           channel_first: bool = True):
+    """helpers.py:430-487: ``core.get_potential_fft`` (fft) or
+    ``core.get_potential`` with the wrap padding of the kernel shape, keeping
+    the true channels."""
+    tc_indices = None if true_channels is None else tuple(i for i, t in enumerate(true_channels) if t is True)
+    if fft:
+        return functools.partial(lcore.get_potential_fft, tc_indices=tc_indices, channel_first=channel_first)
+    if not channel_first:
+        raise NotImplementedError('the engine takes channel-first states')
+    pad = [(0, 0), (0, 0)]
+    for d in tuple(kernel_shape)[2:]:
+        pad.append((d // 2, d // 2 - 1) if d % 2 == 0 else (d // 2, d // 2))
+    return functools.partial(lcore.get_potential, tc_indices=tc_indices, padding=tuple(pad),
+                             channel_first=channel_first)
+
+
+def build_get_field_fn(cin_gfs: List[List[str]], average: bool = True):
+    """helpers.py:490-516: ``core.get_field`` with the flattened growth
+    functions and the weighted mean (or sum)."""
+    growth_fn_t = tuple(lgf.register[slug] for per_channel in cin_gfs for slug in per_channel)
+    weighted_fn = lcore.weighted_mean if average else lcore.weighted_sum
+    return functools.partial(lcore.get_field, growth_fn_t=growth_fn_t, weighted_fn=weighted_fn)
 
 
 def merge_cells(cells: np.ndarray, other: np.ndarray, offset=None) -> np.ndarray:
