@@ -116,3 +116,130 @@ def init_and_run(rng_key, config: Dict, use_init_cells: bool = True, with_jit: b
         n = int(stats['N'])
         all_cells, all_fields, all_pots = all_cells[:n], all_fields[:n], all_pots[:n]
     return all_cells, all_fields, all_pots, stats
+
+
+def _model_setup(config: Dict, use_init_cells: bool, fft: bool, device):
+    wp = config['world_params']
+    cells, K, mapping = init(config, use_init_cells, fft, device)
+    update_fn = build_update_fn(K.shape, mapping, wp.get('get_state_fn_slug', 'v1'), wp.get('weighted_average', True),
+                                fft)
+    return cells, K, mapping, update_fn, lstat.build_compute_stats_fn(wp, config['render_params'])
+
+
+def multi_init_and_run(rng_key, main_config: Dict, configs: List[Dict], use_init_cells: bool = True, fft: bool = True,
+                       device=None, engine: str = 'auto'):
+    """helpers.py:192-237: ``run_scan`` of every configuration in ``configs``
+    with the model of ``main_config`` (same shapes; leniax vmaps run_scan
+    over them), here one engine launch for all of them.  Returns ``(cells,
+    fields, potentials, stats)`` with a leading configuration axis:
+    ``[n_cfg, T, N_init, C|K, *world]`` and ``stats[k]`` ``[n_cfg, T,
+    N_init]``, squeezed as in the reference."""
+    main = copy.deepcopy(main_config)
+    wp = main['world_params']
+    _, _, _, update_fn, compute_stats_fn = _model_setup(main, use_init_cells, fft, device)
+    cells_l, K_l, gf_l, w_l, T_l = [], [], [], [], []
+    for cfg in configs:
+        cells, K, mapping = init(copy.deepcopy(cfg), use_init_cells, fft, device)
+        cells_l.append(cells)
+        K_l.append(K[0] if fft else K)
+        gf_l.append(mapping.get_gf_params(K.device))
+        w_l.append(mapping.get_kernels_weight_per_channel(K.device))
+        T_l.append(float(cfg['world_params']['T']))
+    dev = cells_l[0].device
+    cells0 = torch.stack(cells_l)  # [n_cfg, N_init, C, *world]
+    final, stats, ncont, _, traj, _ = lrunner._rollout(update_fn, compute_stats_fn, cells0, torch.stack(K_l),
+                                                       torch.stack(gf_l), torch.stack(w_l),
+                                                       torch.tensor(T_l, device=dev), main['run_params']['max_run_iter'],
+                                                       True, engine, False)
+    n_cfg, n_init = cells0.shape[:2]
+    out = []
+    for t in traj:  # [T, n_cfg * N_init, ...] -> [n_cfg, T, N_init, ...]
+        out.append(t.reshape((t.shape[0], n_cfg, n_init) + tuple(t.shape[2:])).transpose(0, 1))
+    sd = lstat.split_stats(stats, update_fn.model_for(cells0.shape[3:]).C)
+    sd['N'] = ncont
+    sd = {k: v.squeeze() for k, v in sd.items()}
+    return out[0], out[1], out[2], sd
+
+
+def search_for_init(rng_key: int, config: Dict, fft: bool = True, device=None, engine: str = 'auto'):
+    """helpers.py:319-393: draw ``run_params.nb_init_search`` initial states
+    with ``algo.init_slug`` and return the first that lasts
+    ``run_params.max_run_iter`` steps (else the longest before it), as
+    ``({'N', 'all_cells', 'all_stats'}, index)``.  All candidates run in one
+    engine launch; the chosen one is run again with its trajectory (the
+    engine computes each world on its own, so it is the same run).  The
+    states come from the engine's seeded stream (an integer ``rng_key``), not
+    JAX's."""
+    from . import initializations as linit
+    wp, rp, run = config['world_params'], config['render_params'], config['run_params']
+    C, R = wp['nb_channels'], wp['R']
+    world_size = list(rp['world_size'])
+    nb_init_search, max_run_iter = run['nb_init_search'], run['max_run_iter']
+    kp = [dict(p) for p in config['kernels_params']]
+    K, mapping = lkernels.get_kernels_and_mapping(kp, world_size, C, R, fft, device)
+    dev = K.device
+    gf, w = mapping.get_gf_params(dev), mapping.get_kernels_weight_per_channel(dev)
+    update_fn = build_update_fn(K.shape, mapping, wp.get('get_state_fn_slug', 'v1'), wp.get('weighted_average', True),
+                                fft)
+    compute_stats_fn = lstat.build_compute_stats_fn(wp, rp)
+    T = torch.tensor(float(wp['T']), dtype=torch.float32, device=dev)
+    rng_key, noises = linit.register[config['algo']['init_slug']](rng_key, C * nb_init_search, world_size, R,
+                                                                  kp[0]['gf_params'])
+    noises = noises.reshape([nb_init_search, C] + world_size).cpu().numpy()
+    cells0 = np.concatenate([create_init_cells(world_size, C, [noises[i]]) for i in range(nb_init_search)])
+    cells0 = torch.from_numpy(cells0).to(dev)  # [nb_init_search, C, *world]
+    sd, _ = lrunner.run_scan_mem_optimized(None, cells0[None], K[None], gf[None], w[None],
+                                           T.reshape(1), max_run_iter, R, update_fn, compute_stats_fn, engine)
+    n_done = [int(v) for v in sd['N'][0].tolist()]
+    best_i, current_max, i = None, 0, 0
+    for i, n in enumerate(n_done):  # the reference's sequential selection
+        if current_max < n:
+            current_max, best_i = n, i
+        if n >= max_run_iter:
+            break
+    if best_i is None:
+        return {}, i
+    all_cells, _, _, all_stats = lrunner.run_scan(None, cells0[best_i:best_i + 1], K, gf, w, T, max_run_iter, R,
+                                                  update_fn, compute_stats_fn, engine)
+    return {'N': all_stats['N'], 'all_cells': all_cells, 'all_stats': all_stats}, i
+
+
+def search_for_mutation(rng_key: int, config: Dict, nb_scale_for_stability: int = 1, use_init_cells: bool = True,
+                        fft: bool = True, mutation_rate: float = 1e-5, device=None):
+    """helpers.py:240-316: up to ``run_params.nb_mut_search`` mutations of the
+    ``genotype`` genes (a normal step of ``mutation_rate`` each), each run at
+    ``nb_scale_for_stability`` world scales; returns the mutation that lasts
+    longest over the scales (stopping at one that lasts every step) and its
+    index.  The normal draws come from numpy's PCG64 seeded with the integer
+    ``rng_key``, not JAX's stream."""
+    from .qd import get_param, set_param
+    world_size = config['render_params']['world_size']
+    run = config['run_params']
+    nb_mut_search, max_run_iter = run['nb_mut_search'], run['max_run_iter']
+    genes = config['genotype']
+    noise = np.random.Generator(np.random.PCG64(int(rng_key))).standard_normal(nb_mut_search * len(genes),
+                                                                                dtype=np.float32)
+    best_run, current_max, i = {}, 0, 0
+    for i in range(nb_mut_search):
+        copied = copy.deepcopy(config)
+        for g_i, gene in enumerate(genes):
+            val = np.float32(get_param(copied, gene['key'])) + noise[i * len(genes) + g_i] * np.float32(mutation_rate)
+            set_param(copied, gene['key'], float(val))
+        total_iter_done, nb_iter_done = 0, 0
+        all_cells = stats_dict = None
+        for scale_power in range(nb_scale_for_stability):
+            scaled = copy.deepcopy(copied)
+            scaled['render_params']['world_size'] = [ws * 2**scale_power for ws in world_size]
+            scaled['world_params']['scale'] = 2**scale_power
+            all_cells, _, _, stats_dict = init_and_run(rng_key, scaled, use_init_cells=use_init_cells, with_jit=True,
+                                                       fft=fft, device=device)
+            all_cells = all_cells[:, 0]
+            n = int(stats_dict['N'])
+            nb_iter_done = max(nb_iter_done, n)
+            total_iter_done += n
+        if current_max < total_iter_done:
+            current_max = total_iter_done
+            best_run = {'N': nb_iter_done, 'all_cells': all_cells, 'all_stats': stats_dict, 'config': copied}
+        if total_iter_done >= max_run_iter * nb_scale_for_stability:
+            break
+    return best_run, i

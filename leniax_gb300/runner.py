@@ -145,6 +145,30 @@ def run_scan_mem_optimized(rng_key, cells0, K, gf_params, kernels_weight_per_cha
     return sd, final
 
 
+def run_scan_mem_optimized_pmap(rng_key, cells0, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int,
+                                R: float, update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, engine: str = 'auto'):
+    """runner.py:218-268: ``run_scan_mem_optimized`` over a leading device
+    axis (``cells0`` ``[N_device, N_sols, N_init, C, *world]``, the other
+    arguments ``[N_device, N_sols, ...]``).  Slice d runs on CUDA device
+    ``d mod device_count`` (launches are asynchronous, so the devices work
+    together); results come back stacked on the first slice's device.  The
+    one-process-per-GPU form of the same sharding is ``leniax_gb300.sharding``.
+    """
+    n_dev = int(cells0.shape[0])
+    count = max(1, torch.cuda.device_count())
+    home = cells0.device
+    parts = []
+    for d in range(n_dev):
+        dev = torch.device('cuda', d % count) if count > 1 else home
+        with torch.cuda.device(dev):
+            Td = torch.as_tensor(T)[d] if torch.as_tensor(T).dim() else torch.as_tensor(T)
+            parts.append(run_scan_mem_optimized(rng_key, cells0[d].to(dev), K[d].to(dev), gf_params[d].to(dev),
+                                                kernels_weight_per_channel[d].to(dev), Td, max_run_iter, R,
+                                                update_fn, compute_stats_fn, engine))
+    stats = {k: torch.stack([p[0][k].to(home) for p in parts]) for k in parts[0][0]}
+    return stats, torch.stack([p[1].to(home) for p in parts])
+
+
 def run(rng_key, cells, K, gf_params, kernels_weight_per_channel, T, max_run_iter: int, R: float,
         update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, stat_trunc: bool = False, engine: str = 'auto'):
     """runner.py:16-116: single configuration with the eager total-mass
