@@ -6,8 +6,6 @@ run the whole rollout -- Euler steps, per-step statistics, the stop
 heuristics -- on the device in one engine call (``lgx_run``).  ``run``
 (runner.py:16-116) is the eager driver with leniax's total-mass heuristics.
 """
-from typing import Dict, Optional, Tuple
-
 import torch
 
 from . import _lib

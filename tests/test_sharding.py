@@ -4,7 +4,6 @@ function of the shard)."""
 import os
 import socket
 
-import pytest
 import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
