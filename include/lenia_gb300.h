@@ -77,7 +77,7 @@ extern "C" {
 #define LGX_ENGINE_PLAIN_STREAMED 5 /* one world and one step per launch through the streamed
                                  engine's kernel sequence (row, column, row-inverse and
                                  reduce kernels), for any model the streamed engine runs */
-#define LGX_ENGINE_ND 6       /* general N-D engine: any 2D / 3D world whose sides (2..512)
+#define LGX_ENGINE_ND 6       /* general N-D engine: any 2D / 3D world whose sides (2..4096)
                                  factor into 2, 3, 5 and 7 -- odd, non-square and 3D sides
                                  such as 48^3 included -- with any C and K; mixed-radix line
                                  FFT passes over full complex spectra in HBM              */

@@ -255,7 +255,7 @@ int lgx_plan_create(const lgx_model_desc* d, lgx_plan** out) {
     if (!nd_side_ok(d->world[i]))
       return fail(LGX_ERR_UNSUPPORTED,
                   "world axis %d has size %d: sides from 2 to %d whose prime factors are 2, 3, 5 and 7", i,
-                  d->world[i], 512);
+                  d->world[i], nd_max_side());
     m.world[i] = d->world[i];
   }
   m.C = d->nb_channels;

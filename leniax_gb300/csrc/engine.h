@@ -183,6 +183,7 @@ cudaError_t launch_prepare_streamed_spectrum(const Model& m, int n_sols, const f
 // Any 2D / 3D torus whose sides factor into 2, 3, 5, 7 (2..512), any C and K:
 // mixed-radix line passes over full complex spectra in HBM (nd.cu).
 bool nd_side_ok(int n);
+int nd_max_side();  // longest world axis of the N-D engine
 bool nd_supported(const Model& m);
 int nd_blocks_per_world(const Model& m, long n_worlds);
 // Prepared spectra [Ns, C, max_k, cells] complex: the Hermitian half

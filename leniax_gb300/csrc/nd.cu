@@ -39,6 +39,7 @@ namespace lgx {
 namespace {
 
 constexpr int kNT = 256;          // threads per block
+constexpr int kNdMaxN = 4096;     // longest world axis (one 4096-point line per pass tile)
 constexpr int kMaxPts = 4096;     // complex points of one pass tile (two buffers in shared memory)
 // Launches smaller than this many blocks (two on each of GB300's 152 SMs)
 // get smaller tiles / chunks so that one small world still spreads over the
@@ -395,6 +396,59 @@ __global__ void nd_half_kernel(long planes, int D, int H, int W, const float2* _
 
 inline int grid_for(long total) { return (int)std::max(1L, std::min<long>((total + kNT - 1) / kNT, 1L << 16)); }
 
+// ------------------------------------------------------------------ separate last-axis passes
+// For worlds whose fused-pass tile set does not fit (long last axes with many
+// channels): the last forward axis, these products, then the first inverse
+// axis run as three launches.
+// P[w, k] = S[w, c_in(k)] * prepared[sol(w), c_in(k), slot(k)]
+__global__ void nd_multiply_kernel(NdTab t, int n_worlds, int n_init, const float2* __restrict__ S,
+                                   const float2* __restrict__ kf, long kf_sol_stride, float2* __restrict__ P) {
+  const long total = (long)n_worlds * t.K * t.cells;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const long cell = i % t.cells;
+    const long wk = i / t.cells;
+    const int k = (int)(wk % t.K), w = (int)(wk / t.K);
+    const int sol = w / n_init, c = t.cin[k];
+    const float2 s = S[((long)w * t.C + c) * t.cells + cell];
+    const float2 kk = __ldg(kf + sol * kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + cell);
+    P[i] = cmul(s, kk);
+  }
+}
+
+// gk[w, k] += A_k conj(S_cin(k)) (kernel gradient), Q[w, c] = sum_{k: c_in(k)
+// = c} A_k conj(prepared K_k)
+__global__ void nd_adj_spectral_kernel(NdTab t, int n_worlds, int n_init, const float2* __restrict__ A,
+                                       const float2* __restrict__ S, const float2* __restrict__ kf,
+                                       long kf_sol_stride, float2* __restrict__ gk, float2* __restrict__ Q) {
+  const long total = (long)n_worlds * t.cells;
+  const int C = t.C, K = t.K;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+    const int w = (int)(i / t.cells);
+    const long cell = i - (long)w * t.cells;
+    const int sol = w / n_init;
+    float2 q[kMaxChannels];
+#pragma unroll
+    for (int c = 0; c < kMaxChannels; ++c) q[c] = make_float2(0.f, 0.f);
+    for (int k = 0; k < K; ++k) {
+      const int c = t.cin[k];
+      const float2 ak = A[((long)w * K + k) * t.cells + cell];
+      const float2 sc = S[((long)w * C + c) * t.cells + cell];
+      float2* g = gk + ((long)w * K + k) * t.cells + cell;
+      *g = cadd(*g, cmulc(ak, sc));
+      const float2 kk = __ldg(kf + sol * kf_sol_stride + ((long)c * t.max_k + t.slot[k]) * t.cells + cell);
+      const float2 pr = cmulc(ak, kk);
+#pragma unroll
+      for (int cc = 0; cc < kMaxChannels; ++cc)
+        if (cc == c) q[cc] = cadd(q[cc], pr);
+    }
+#pragma unroll
+    for (int c = 0; c < kMaxChannels; ++c) {
+      if (c >= C) break;
+      Q[((long)w * C + c) * t.cells + cell] = q[c];
+    }
+  }
+}
+
 // ------------------------------------------------------------------ fused convolution pass
 // Along the last world axis (z in 3D, y in 2D) line i of a plane holds the
 // points i + j I, j < L, with I = cells / L lines per plane.  One block takes
@@ -539,25 +593,36 @@ __global__ void __launch_bounds__(kNT) nd_adj_conv_kernel(NdTab t, ConvArgs a, G
 // Tile and shared memory of a fused convolution pass; `bufs` complex tiles
 // besides the twiddles (C + 2 forward, 2C + 2 adjoint).
 constexpr long kConvSmemPts = 96 * 1024 / 8;  // 96 KB of tiles: two blocks per SM
-// the largest tile set: one 512-point line, 2 x 16 + 2 buffers, twiddles
-constexpr int kConvSmemMax = (kGMaxN + (2 * kMaxChannels + 2) * kGMaxN) * (int)sizeof(float2);
+// the largest tile set a fused pass may take; worlds whose one-line tile set
+// is larger (long last axes with many channels) take the separate passes
+constexpr int kConvSmemMax = 200 * 1024;
+
+// Lines per tile and shared memory of the fused pass along the last axis, or
+// 0 when even one line per tile does not fit.
+size_t conv_smem(const NdTab& t, bool adjoint, long nw, int* nl_out) {
+  const long L = t.nd == 3 ? t.D : t.H;
+  const long I = t.cells / L;
+  const long bufs = adjoint ? 2L * t.C + 2 : (long)t.C + 2;
+  const long cap_pts = std::min<long>(kMaxPts, (kConvSmemPts - L) / bufs);
+  const long cap = std::max<long>(1, cap_pts / L);
+  const long fill = (nw * I + kFillBlocks - 1) / kFillBlocks;
+  const long nl = std::min<long>(std::min<long>(cap, std::max<long>(4, fill)), I);
+  const size_t smem = (size_t)(L + bufs * nl * L) * sizeof(float2);
+  if (nl_out) *nl_out = (int)nl;
+  return smem <= (size_t)kConvSmemMax ? smem : 0;
+}
 
 cudaError_t run_conv(bool adjoint, const NdTab& t, long nw, ConvArgs a, cudaStream_t st) {
   a.L = t.nd == 3 ? t.D : t.H;
   a.I = t.cells / a.L;
   const GPlan p = make_plan(a.L);
   if (p.stages == 0) return cudaErrorInvalidValue;
-  const long bufs = adjoint ? 2L * t.C + 2 : (long)t.C + 2;
-  const long cap_pts = std::min<long>(kMaxPts, (kConvSmemPts - a.L) / bufs);
-  const long cap = std::max<long>(1, cap_pts / a.L);
-  const long fill = (nw * a.I + kFillBlocks - 1) / kFillBlocks;
-  a.nl = (int)std::min<long>(std::min<long>(cap, std::max<long>(4, fill)), a.I);
+  const size_t smem = conv_smem(t, adjoint, nw, &a.nl);
+  if (smem == 0) return cudaErrorInvalidConfiguration;
   a.tiles = (int)((a.I + a.nl - 1) / a.nl);
   a.fnl = make_fastdiv((unsigned)a.nl);
-  const size_t smem = (size_t)(a.L + bufs * a.nl * a.L) * sizeof(float2);
   const long blocks = nw * a.tiles;
   if (blocks >= (1L << 31)) return cudaErrorInvalidConfiguration;
-  if (smem > (size_t)kConvSmemMax) return cudaErrorInvalidConfiguration;
   cudaError_t e = allow_nd_smem();
   if (e != cudaSuccess) return e;
   if (adjoint) nd_adj_conv_kernel<<<(unsigned)blocks, kNT, smem, st>>>(t, a, p);
@@ -1151,11 +1216,11 @@ cudaError_t allow_nd_smem() {
     std::lock_guard<std::mutex> lk(mu);
     if (std::find(done.begin(), done.end(), ctx) != done.end()) return cudaSuccess;
   }
-  const int pass_bytes = (int)((2 * kMaxPts + kGMaxN) * sizeof(float2));
+  const int pass_bytes = (int)((2 * kMaxPts + kNdMaxN) * sizeof(float2));
   cudaError_t e = cudaFuncSetAttribute(nd_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(nd_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
-  const int plane_bytes = (int)((2 * kMaxPts + 2 * kGMaxN) * sizeof(float2));
+  const int plane_bytes = (int)((2 * kMaxPts + 2 * kNdMaxN) * sizeof(float2));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(nd_plane_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plane_bytes);
   if (e == cudaSuccess)
@@ -1179,7 +1244,9 @@ inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 }  // namespace
 
 // ---------------------------------------------------------------------- API
-bool nd_side_ok(int n) { return n >= 2 && n <= kGMaxN && make_plan(n).stages > 0; }
+bool nd_side_ok(int n) { return n >= 2 && n <= kNdMaxN && make_plan(n).stages > 0; }
+
+int nd_max_side() { return kNdMaxN; }
 
 bool nd_supported(const Model& m) {
   if (m.nb_dims != 2 && m.nb_dims != 3) return false;
@@ -1238,13 +1305,22 @@ cudaError_t launch_nd_step(const NdStep& s, cudaStream_t st) {
   float* pot = s.pot_out ? s.pot_out : U;
   cudaError_t e = forward_real_head(t, (long)nw * m.C, s.state, S, st);
   if (e != cudaSuccess) return e;
-  ConvArgs ca{};
-  ca.n_init = s.n_init;
-  ca.kf = s.kf;
-  ca.kf_sol_stride = s.kf_sol_stride;
-  ca.S = S;
-  ca.P = P;
-  if ((e = run_conv(false, t, (long)nw, ca, st)) != cudaSuccess) return e;
+  const int last = t.nd == 3 ? 2 : 1;  // the last world axis
+  if (conv_smem(t, false, (long)nw, nullptr) > 0) {
+    ConvArgs ca{};
+    ca.n_init = s.n_init;
+    ca.kf = s.kf;
+    ca.kf_sol_stride = s.kf_sol_stride;
+    ca.S = S;
+    ca.P = P;
+    if ((e = run_conv(false, t, (long)nw, ca, st)) != cudaSuccess) return e;
+  } else {
+    if ((e = run_pass(false, last, t, (long)nw * m.C, S, nullptr, nullptr, false, 1.f, st)) != cudaSuccess) return e;
+    nd_multiply_kernel<<<grid_for((long)nw * m.K * cells), kNT, 0, st>>>(t, s.n_worlds, s.n_init, S, s.kf,
+                                                                          s.kf_sol_stride, P);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = run_pass(true, last, t, (long)nw * m.K, P, nullptr, nullptr, false, 1.f, st)) != cudaSuccess) return e;
+  }
   const bool fused = plane_epi_smem(t) > 0;
   if (!fused && (e = inverse_real_tail(t, (long)nw * m.K, P, pot, false, 1.f, st)) != cudaSuccess) return e;
   EpiArgs a;
@@ -1351,15 +1427,23 @@ cudaError_t launch_nd_adjoint(const Model& m, const NdAdjoint& j, void* ws, cuda
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     if ((e = forward_real_head(t, (long)nw * KC, ar, A, st)) != cudaSuccess) return e;
-    ConvArgs ca{};
-    ca.n_init = j.n_init;
-    ca.kf = kf;
-    ca.kf_sol_stride = kf_sol;
-    ca.S = S;
-    ca.A = A;
-    ca.gk = j.gk;
-    ca.Q = Q;
-    if ((e = run_conv(true, t, (long)nw, ca, st)) != cudaSuccess) return e;
+    if (conv_smem(t, true, (long)nw, nullptr) > 0) {
+      ConvArgs ca{};
+      ca.n_init = j.n_init;
+      ca.kf = kf;
+      ca.kf_sol_stride = kf_sol;
+      ca.S = S;
+      ca.A = A;
+      ca.gk = j.gk;
+      ca.Q = Q;
+      if ((e = run_conv(true, t, (long)nw, ca, st)) != cudaSuccess) return e;
+    } else {
+      const int last = t.nd == 3 ? 2 : 1;
+      if ((e = run_pass(false, last, t, (long)nw * KC, A, nullptr, nullptr, false, 1.f, st)) != cudaSuccess) return e;
+      nd_adj_spectral_kernel<<<grid_for((long)nw * cells), kNT, 0, st>>>(t, nw, j.n_init, A, S, kf, kf_sol, j.gk, Q);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      if ((e = run_pass(true, last, t, (long)nw * m.C, Q, nullptr, nullptr, false, 1.f, st)) != cudaSuccess) return e;
+    }
     if ((e = inverse_real_tail(t, (long)nw * m.C, Q, lam_out, true, 1.f, st)) != cudaSuccess) return e;
     lam_in = lam_out;
   }

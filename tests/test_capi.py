@@ -98,7 +98,7 @@ def test_other_worlds_select_the_nd_engine_and_its_adjoint(nb_dims, world):
 @pytest.mark.parametrize('kw,code', [
     (dict(world=(66, 66)), _lib.LGX_ERR_UNSUPPORTED),    # 66 = 2 * 3 * 11: no radix-11 pass
     (dict(world=(26, 32)), _lib.LGX_ERR_UNSUPPORTED),    # 26 = 2 * 13
-    (dict(world=(1024, 1024)), _lib.LGX_ERR_UNSUPPORTED),  # sides up to 512
+    (dict(world=(8192, 8192)), _lib.LGX_ERR_UNSUPPORTED),  # sides up to 4096
     (dict(nb_dims=3, world=(32, 22, 32)), _lib.LGX_ERR_UNSUPPORTED),
     (dict(nb_dims=4), _lib.LGX_ERR_INVALID),
     (dict(kernel_cin=[1]), _lib.LGX_ERR_INVALID),
