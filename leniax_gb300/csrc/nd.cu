@@ -40,6 +40,7 @@ namespace {
 
 constexpr int kNT = 256;          // threads per block
 constexpr int kNdMaxN = 4096;     // longest world axis (one 4096-point line per pass tile)
+constexpr int kBluesteinMaxN = 2048;  // longest axis with a prime factor above 7 (M <= 4096)
 constexpr int kMaxPts = 4096;     // complex points of one pass tile (two buffers in shared memory)
 // Launches smaller than this many blocks (two on each of GB300's 152 SMs)
 // get smaller tiles / chunks so that one small world still spreads over the
@@ -84,24 +85,89 @@ NdTab make_tab(const Model& m, int dt_mode) {
 // Lines of a pass: line (g, i) starts at g * gstride + i and has L points
 // `stride` apart; g < G, i < I.  I == 1: a tile is nl consecutive groups
 // (rows of the x pass, contiguous); I > 1: nl consecutive i of one group.
+// The smallest M >= 2L - 1 whose prime factors are 2, 3, 5, 7 (the
+// Bluestein transform length of an L-point line), or 0 past the tile size.
+inline int bluestein_size(int L) {
+  if (L < 2 || L > kBluesteinMaxN) return 0;
+  for (int m = 2 * L - 1; m <= kMaxPts; ++m)
+    if (make_plan(m).stages > 0) return m;
+  return 0;
+}
+
 struct Pass {
   float2* data;          // complex planes (in and out, in place)
   const float* src_real;  // IN_REAL: real input of the same geometry
   float* dst_real;        // OUT_REAL: Re(result) * scale (stored, or added when accumulate)
   long G, I, gstride, stride;
   int L, nl;
+  int M;                  // Bluestein lines: the transform length M >= 2L - 1 (0: an L-point transform)
   FastDivU fnl;            // division by nl
   int in_real, out_real, accumulate;
   float scale;
 };
 
+// Bluestein's chirp-z transform (L. Bluestein, "A linear filtering approach
+// to the computation of discrete Fourier transform", 1970) for lines whose
+// length has a prime factor above 7: with c_n = exp(-i pi n^2 / L),
+// X_k = c_k sum_n (x_n c_n) conj(c_{k-n}), a cyclic convolution of length
+// M >= 2L - 1 done with M-point transforms (the inverse transform uses
+// conj(c)).  The tile holds nl lines of M points (x_n c_n, then zeros);
+// `chirp` c_n (n < L) and `bhat` = FFT_M(b), b_m = conj(c_|m|) for |m| < L
+// (indices mod M), are in shared memory.  b is even, so FFT_M(conj(b)) =
+// conj(bhat).  Unnormalised like fft_line; returns the buffer holding X.
 template <bool INV>
+__device__ float2* bluestein_lines(float2* A, float2* B, const GPlan& p, const float2* tw, const float2* chirp,
+                                   const float2* bhat, int nl, int L) {
+  const int M = p.n;
+  for (int l = 0; l < nl; ++l)
+    for (int j = threadIdx.x; j < L; j += blockDim.x) {
+      const float2 c = chirp[j];
+      A[l * M + j] = INV ? cmulc(A[l * M + j], c) : cmul(A[l * M + j], c);
+    }
+  __syncthreads();
+  float2* r = fft_line<false>(A, B, p, tw, nl);
+  for (int l = 0; l < nl; ++l)
+    for (int k = threadIdx.x; k < M; k += blockDim.x)
+      r[l * M + k] = INV ? cmulc(r[l * M + k], bhat[k]) : cmul(r[l * M + k], bhat[k]);
+  __syncthreads();
+  float2* q = fft_line<true>(r, r == A ? B : A, p, tw, nl);
+  const float inv_m = 1.f / (float)M;
+  for (int l = 0; l < nl; ++l)
+    for (int k = threadIdx.x; k < L; k += blockDim.x) {
+      const float2 v = INV ? cmulc(q[l * M + k], chirp[k]) : cmul(q[l * M + k], chirp[k]);
+      q[l * M + k] = make_float2(v.x * inv_m, v.y * inv_m);
+    }
+  __syncthreads();
+  return q;
+}
+
+// chirp c_n = exp(-2 pi i (n^2 mod 2L) / 2L) and bhat = FFT_M(b), computed by
+// the block in shared memory with A and B as the transform's scratch
+__device__ void bluestein_tables(float2* chirp, float2* bhat, float2* A, float2* B, const GPlan& p,
+                                 const float2* tw, int L) {
+  const int M = p.n;
+  for (int n = threadIdx.x; n < L; n += blockDim.x) chirp[n] = tw_entry((int)(((long)n * n) % (2L * L)), 2 * L);
+  __syncthreads();
+  for (int m = threadIdx.x; m < M; m += blockDim.x) {
+    const int d = m < L ? m : (M - m < L ? M - m : -1);
+    A[m] = d >= 0 ? conjf2(chirp[d]) : make_float2(0.f, 0.f);
+  }
+  __syncthreads();
+  const float2* r = fft_line<false>(A, B, p, tw, 1);
+  for (int m = threadIdx.x; m < M; m += blockDim.x) bhat[m] = r[m];
+  __syncthreads();
+}
+
+template <bool INV, bool BL>
 __global__ void __launch_bounds__(kNT, 3) nd_pass_kernel(Pass a, GPlan p) {
   extern __shared__ __align__(16) float2 ndsm[];
   const int L = a.L, nl = a.nl;
+  const int S = BL ? a.M : L;  // points per line in the tile
   float2* tw = ndsm;
-  float2* A = tw + L;
-  float2* B = A + (size_t)nl * L;
+  float2* A = tw + S;
+  float2* B = A + (size_t)nl * S;
+  float2* chirp = B + (size_t)nl * S;  // Bluestein tables (BL only)
+  float2* bhat = chirp + L;
   long g0, i0;
   int lines;
   if (a.I == 1) {
@@ -114,7 +180,11 @@ __global__ void __launch_bounds__(kNT, 3) nd_pass_kernel(Pass a, GPlan p) {
     i0 = (blockIdx.x % tiles) * nl;
     lines = (int)min((long)nl, a.I - i0);
   }
-  fill_twiddles(tw, L);
+  fill_twiddles(tw, S);
+  if (BL) {
+    __syncthreads();
+    bluestein_tables(chirp, bhat, A, B, p, tw, L);
+  }
   const int pts = nl * L;
   // A tile of the x pass is nl whole rows, contiguous in memory and in the
   // tile (point idx at row-block offset idx); a strided pass's tile holds
@@ -134,13 +204,18 @@ __global__ void __launch_bounds__(kNT, 3) nd_pass_kernel(Pass a, GPlan p) {
       const int idx = base + u * blockDim.x;
       long off;
       bool in;
-      if (rows) {
+      if (rows && !BL) {
         dst[u] = idx < pts ? idx : -1;
+        in = idx < valid;
+        off = gbase + idx;
+      } else if (rows) {  // Bluestein rows: tile lines of M points
+        const int l = idx / L, j = idx - l * L;
+        dst[u] = idx < pts ? l * S + j : -1;
         in = idx < valid;
         off = gbase + idx;
       } else {
         const int j = a.fnl.div(idx), l = idx - j * nl;
-        dst[u] = idx < pts ? l * L + j : -1;
+        dst[u] = idx < pts ? l * S + j : -1;
         in = idx < pts && l < lines;
         off = gbase + l + (long)j * a.stride;
       }
@@ -151,19 +226,26 @@ __global__ void __launch_bounds__(kNT, 3) nd_pass_kernel(Pass a, GPlan p) {
     for (int u = 0; u < kLoadBatch; ++u)
       if (dst[u] >= 0) A[dst[u]] = v[u];
   }
+  if (BL)  // the zero padding of every tile line
+    for (int l = 0; l < nl; ++l)
+      for (int j = L + threadIdx.x; j < S; j += blockDim.x) A[l * S + j] = make_float2(0.f, 0.f);
   __syncthreads();
-  const float2* res = fft_line<INV>(A, B, p, tw, nl);
+  const float2* res = BL ? bluestein_lines<INV>(A, B, p, tw, chirp, bhat, nl, L) : fft_line<INV>(A, B, p, tw, nl);
   for (int idx = threadIdx.x; idx < valid; idx += blockDim.x) {
     long off;
     int src;
-    if (rows) {
+    if (rows && !BL) {
       off = gbase + idx;
       src = idx;
+    } else if (rows) {
+      const int l = idx / L;
+      off = gbase + idx;
+      src = l * S + (idx - l * L);
     } else {
       const int j = a.fnl.div(idx), l = idx - j * nl;
       if (l >= lines) continue;
       off = gbase + l + (long)j * a.stride;
-      src = l * L + j;
+      src = l * S + j;
     }
     const float2 v = res[src];
     if (a.out_real) {
@@ -212,9 +294,16 @@ cudaError_t run_pass(bool inv, int axis, const NdTab& t, long planes, float2* da
     a.gstride = HW * t.D;
     a.stride = HW;
   }
-  const GPlan p = make_plan(a.L);
-  if (p.stages == 0) return cudaErrorInvalidValue;
-  const int cap = std::max(1, kMaxPts / a.L);
+  GPlan p = make_plan(a.L);
+  a.M = 0;
+  if (p.stages == 0) {  // Bluestein lines
+    a.M = bluestein_size(a.L);
+    if (a.M == 0) return cudaErrorInvalidValue;
+    p = make_plan(a.M);
+  }
+  const bool bl = a.M > 0;
+  const int S = bl ? a.M : a.L;
+  const int cap = std::max(1, kMaxPts / S);
   // lines per tile: the full tile, or fewer when the pass has too few lines
   // to fill the GPU (at least 4 adjacent lines of a strided pass, so each
   // load still covers a 32-byte sector)
@@ -223,12 +312,17 @@ cudaError_t run_pass(bool inv, int axis, const NdTab& t, long planes, float2* da
   a.nl = (int)std::min<long>(std::min<long>(cap, want), a.I == 1 ? a.G : a.I);
   a.fnl = make_fastdiv((unsigned)a.nl);
   const long tiles = a.I == 1 ? (a.G + a.nl - 1) / a.nl : a.G * ((a.I + a.nl - 1) / a.nl);
-  const size_t smem = (size_t)(a.L + 2 * a.nl * a.L) * sizeof(float2);
+  const size_t smem = (size_t)(S + 2L * a.nl * S + (bl ? a.L + S : 0)) * sizeof(float2);
   cudaError_t e = allow_nd_smem();
   if (e != cudaSuccess) return e;
   if (tiles >= (1L << 31)) return cudaErrorInvalidConfiguration;
-  if (inv) nd_pass_kernel<true><<<(unsigned)tiles, kNT, smem, st>>>(a, p);
-  else nd_pass_kernel<false><<<(unsigned)tiles, kNT, smem, st>>>(a, p);
+  if (bl) {
+    if (inv) nd_pass_kernel<true, true><<<(unsigned)tiles, kNT, smem, st>>>(a, p);
+    else nd_pass_kernel<false, true><<<(unsigned)tiles, kNT, smem, st>>>(a, p);
+  } else {
+    if (inv) nd_pass_kernel<true, false><<<(unsigned)tiles, kNT, smem, st>>>(a, p);
+    else nd_pass_kernel<false, false><<<(unsigned)tiles, kNT, smem, st>>>(a, p);
+  }
   return cudaGetLastError();
 }
 
@@ -294,7 +388,9 @@ __global__ void __launch_bounds__(kNT, 3) nd_plane_kernel(PlaneArgs a, GPlan px,
   }
 }
 
-bool plane_ok(const NdTab& t) { return t.D > 1 && (long)t.H * t.W <= kMaxPts; }
+bool plane_ok(const NdTab& t) {
+  return t.D > 1 && (long)t.H * t.W <= kMaxPts && make_plan(t.H).stages > 0 && make_plan(t.W).stages > 0;
+}
 
 // Shared memory of the fused plane epilogue (twiddles, two tiles, the
 // channels' fields), or 0 when the world does not take it.
@@ -601,6 +697,7 @@ constexpr int kConvSmemMax = 200 * 1024;
 // 0 when even one line per tile does not fit.
 size_t conv_smem(const NdTab& t, bool adjoint, long nw, int* nl_out) {
   const long L = t.nd == 3 ? t.D : t.H;
+  if (make_plan((int)L).stages == 0) return 0;  // Bluestein lines take the separate passes
   const long I = t.cells / L;
   const long bufs = adjoint ? 2L * t.C + 2 : (long)t.C + 2;
   const long cap_pts = std::min<long>(kMaxPts, (kConvSmemPts - L) / bufs);
@@ -1216,10 +1313,12 @@ cudaError_t allow_nd_smem() {
     std::lock_guard<std::mutex> lk(mu);
     if (std::find(done.begin(), done.end(), ctx) != done.end()) return cudaSuccess;
   }
-  const int pass_bytes = (int)((2 * kMaxPts + kNdMaxN) * sizeof(float2));
-  cudaError_t e = cudaFuncSetAttribute(nd_pass_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(nd_pass_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
+  // twiddles, two tiles and, for Bluestein lines, the chirp and its spectrum
+  const int pass_bytes = (int)((kNdMaxN + 2 * kMaxPts + kBluesteinMaxN + kMaxPts) * sizeof(float2));
+  cudaError_t e = cudaSuccess;
+  for (auto f : {nd_pass_kernel<false, false>, nd_pass_kernel<true, false>, nd_pass_kernel<false, true>,
+                 nd_pass_kernel<true, true>})
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, pass_bytes);
   const int plane_bytes = (int)((2 * kMaxPts + 2 * kNdMaxN) * sizeof(float2));
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(nd_plane_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, plane_bytes);
@@ -1244,7 +1343,9 @@ inline size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
 }  // namespace
 
 // ---------------------------------------------------------------------- API
-bool nd_side_ok(int n) { return n >= 2 && n <= kNdMaxN && make_plan(n).stages > 0; }
+bool nd_side_ok(int n) {
+  return n >= 2 && ((n <= kNdMaxN && make_plan(n).stages > 0) || bluestein_size(n) > 0);
+}
 
 int nd_max_side() { return kNdMaxN; }
 

@@ -95,11 +95,23 @@ def test_other_worlds_select_the_nd_engine_and_its_adjoint(nb_dims, world):
     assert lib.lgx_adjoint_kernel_grad_acc_bytes(p.handle, 2, 3) == 2 * 3 * 3 * cells * 8
 
 
+@pytest.mark.parametrize('world', [(66, 66), (127, 127), (26, 100), (1031, 64), (2048, 2048), (4096, 16)])
+def test_any_side_up_to_2048_and_smooth_sides_up_to_4096_take_the_nd_engine(world):
+    # sides with a prime factor above 7 run Bluestein lines (up to 2048);
+    # sides of factors 2, 3, 5, 7 up to 4096
+    lib = _lib.load()
+    p = _plan(world=world)
+    assert lib.lgx_select_engine(p.handle, 1, 2, 0) == _lib.ENGINES['nd']
+    assert lib.lgx_run_workspace_bytes(p.handle, 1, 2, 4, 0) > 0
+    assert lib.lgx_update_workspace_bytes(p.handle, 3) > 0
+
+
 @pytest.mark.parametrize('kw,code', [
-    (dict(world=(66, 66)), _lib.LGX_ERR_UNSUPPORTED),    # 66 = 2 * 3 * 11: no radix-11 pass
-    (dict(world=(26, 32)), _lib.LGX_ERR_UNSUPPORTED),    # 26 = 2 * 13
+    (dict(world=(2053, 64)), _lib.LGX_ERR_UNSUPPORTED),  # a prime above 2048 (Bluestein lines up to 2048)
+    (dict(world=(64, 4094)), _lib.LGX_ERR_UNSUPPORTED),  # 4094 = 2 * 23 * 89, above 2048
     (dict(world=(8192, 8192)), _lib.LGX_ERR_UNSUPPORTED),  # sides up to 4096
-    (dict(nb_dims=3, world=(32, 22, 32)), _lib.LGX_ERR_UNSUPPORTED),
+    (dict(nb_dims=3, world=(32, 4099, 32)), _lib.LGX_ERR_UNSUPPORTED),
+    (dict(world=(1, 32)), _lib.LGX_ERR_UNSUPPORTED),  # sides from 2
     (dict(nb_dims=4), _lib.LGX_ERR_INVALID),
     (dict(kernel_cin=[1]), _lib.LGX_ERR_INVALID),
     (dict(growth_ids=[42]), _lib.LGX_ERR_UNSUPPORTED),
