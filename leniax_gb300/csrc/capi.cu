@@ -504,6 +504,7 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
     a.traj_cells = j->traj_cells;
     a.traj_field = j->traj_field;
     a.traj_pot = j->traj_potential;
+    a.no_stats = (j->stats || j->n_continue || j->n_box || j->centroid) ? 0 : 1;
     const int wpc = 512 / ((m.H / 2) * (m.H == 128 ? 8 : 4));
     const int items = (nw + wpc - 1) / wpc;
     const int grid = std::max(1, std::min(items, resident_max_grid(m.H)));

@@ -59,6 +59,9 @@ struct ResidentArgs {
   // one-world-per-launch engine chains single-step launches through it.
   const int* shift_in;
   int* shift_out;
+  // 1: no statistics are read from this rollout (no raw moments, no carried
+  // shift): the 128 x 128 kernel then skips their per-cell work
+  int no_stats;
 };
 cudaError_t launch_resident(int N, const ResidentArgs& a, int grid, cudaStream_t st);
 int resident_max_grid(int N);

@@ -25,7 +25,7 @@ namespace lgx {
 
 namespace {
 
-template <int N, int G, int GF>
+template <int N, int G, int GF, bool STATS>
 __global__ void __launch_bounds__(512, 1) resident_kernel(ResidentArgs a) {
   using CF = RCfg<N, G>;
   extern __shared__ __align__(16) float2 sm[];
@@ -33,7 +33,8 @@ __global__ void __launch_bounds__(512, 1) resident_kernel(ResidentArgs a) {
   __syncthreads();
   int loaded_sol = -1;
   const int n_items = (a.n_worlds + CF::WPC - 1) / CF::WPC;
-  for (int item = blockIdx.x; item < n_items; item += gridDim.x) resident_item<N, G, GF>(a, item, sm, sm + 3 * N, loaded_sol);
+  for (int item = blockIdx.x; item < n_items; item += gridDim.x)
+    resident_item<N, G, GF, STATS>(a, item, sm, sm + 3 * N, loaded_sol);
 }
 
 template <int N>
@@ -60,21 +61,24 @@ __global__ void prepare_resident_kernel(int n_sols, const float2* __restrict__ k
   }
 }
 
-template <int N, int G, int GF>
+template <int N, int G, int GF, bool STATS>
 cudaError_t launch_one(const ResidentArgs& a, int grid, cudaStream_t st) {
   using CF = RCfg<N, G>;
-  cudaError_t e = cudaFuncSetAttribute(resident_kernel<N, G, GF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaError_t e = cudaFuncSetAttribute(resident_kernel<N, G, GF, STATS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)CF::SMEM);
   if (e != cudaSuccess) return e;
-  resident_kernel<N, G, GF><<<grid, 512, CF::SMEM, st>>>(a);
+  resident_kernel<N, G, GF, STATS><<<grid, 512, CF::SMEM, st>>>(a);
   return cudaGetLastError();
 }
 
-template <int N, int G>
+// The statistics-free variant exists for 128 x 128 (the differentiation
+// workload's checkpointed forward and trajectory recompute); smaller worlds
+// compute the moments and ignore them.
+template <int N, int G, bool STATS>
 cudaError_t launch_gf(const ResidentArgs& a, int grid, cudaStream_t st) {
-  if (a.gf_id == LGX_GF_GAUSSIAN) return launch_one<N, G, GF_FAST_GAUSSIAN>(a, grid, st);
-  if (a.gf_id == LGX_GF_POLY_QUAD4) return launch_one<N, G, GF_FAST_POLY4>(a, grid, st);
-  return launch_one<N, G, GF_GENERIC>(a, grid, st);
+  if (a.gf_id == LGX_GF_GAUSSIAN) return launch_one<N, G, GF_FAST_GAUSSIAN, STATS>(a, grid, st);
+  if (a.gf_id == LGX_GF_POLY_QUAD4) return launch_one<N, G, GF_FAST_POLY4, STATS>(a, grid, st);
+  return launch_one<N, G, GF_GENERIC, STATS>(a, grid, st);
 }
 
 }  // namespace
@@ -102,9 +106,9 @@ int resident_max_grid(int N) {
 
 cudaError_t launch_resident(int N, const ResidentArgs& a, int grid, cudaStream_t st) {
   switch (N) {
-    case 32: return launch_gf<32, 4>(a, grid, st);
-    case 64: return launch_gf<64, 4>(a, grid, st);
-    case 128: return launch_gf<128, 8>(a, grid, st);
+    case 32: return launch_gf<32, 4, true>(a, grid, st);
+    case 64: return launch_gf<64, 4, true>(a, grid, st);
+    case 128: return a.no_stats ? launch_gf<128, 8, false>(a, grid, st) : launch_gf<128, 8, true>(a, grid, st);
   }
   return cudaErrorInvalidValue;
 }

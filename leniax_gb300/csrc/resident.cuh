@@ -40,7 +40,7 @@ __device__ __forceinline__ int swz(int r) {
 // (N/2)*G-thread slice of the 512-thread CTA.  `tw` holds the three N-entry
 // twiddle tables, `work` the slices' shared buffers (RCfg::SMEM - 3N float2).
 // `loaded_sol` caches which solution's prepared spectrum each slice holds.
-template <int N, int G, int GF>
+template <int N, int G, int GF, bool STATS = true>
 __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, const float2* tw, float2* work,
                                               int& loaded_sol) {
   using CF = RCfg<N, G>;
@@ -157,7 +157,7 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
         }
       }
       named_bar(bar_id, NT);
-      if (step > 0 && wid == NW - 1) finalize(step - 1);
+      if (STATS && step > 0 && wid == NW - 1) finalize(step - 1);
       // ------------------------------------------------------- column pass
       {
         const int c = grp;  // column pair (c, N-c); c == 0 carries (0, N/2)
@@ -311,22 +311,24 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
           } else {
             z[k1] = make_float2(state_fn(sfid, sa, fa, dt), state_fn(sfid, sb, fb, dt));
           }
-          // statistics moments of the pre-update cells (statistics.py:64-100)
-          const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
-          const float cx = (float)(((xb + G * k1) & (N - 1)) - N / 2);
-          S2 = __fadd2_rn(S2, s2);
-          G2 = __fadd2_rn(G2, make_float2(fpa, fpb));
-          const float ss = sa + sb, gg = fpa + fpb;
-          mxx = fmaf(ss, cx, mxx);
-          mx2x = fmaf(ss * cx, cx, mx2x);
-          gxx = fmaf(gg, cx, gxx);
-          cpot += (pa > kEps ? 1.f : 0.f) + (pb > kEps ? 1.f : 0.f);
-          const bool la = sa > kEps, lb = sb > kEps;
-          cmass += (la ? 1.f : 0.f) + (lb ? 1.f : 0.f);
-          cgrow += (fpa > kEps ? 1.f : 0.f) + (fpb > kEps ? 1.f : 0.f);
-          liveA |= la;
-          liveB |= lb;
-          if (k1 == 0 || k1 == P - 1) liveX |= (x == 0 || x == N - 1) && (la || lb);
+          if constexpr (STATS) {
+            // statistics moments of the pre-update cells (statistics.py:64-100)
+            const float fpa = fmaxf(fa, 0.f), fpb = fmaxf(fb, 0.f);
+            const float cx = (float)(((xb + G * k1) & (N - 1)) - N / 2);
+            S2 = __fadd2_rn(S2, s2);
+            G2 = __fadd2_rn(G2, make_float2(fpa, fpb));
+            const float ss = sa + sb, gg = fpa + fpb;
+            mxx = fmaf(ss, cx, mxx);
+            mx2x = fmaf(ss * cx, cx, mx2x);
+            gxx = fmaf(gg, cx, gxx);
+            cpot += (pa > kEps ? 1.f : 0.f) + (pb > kEps ? 1.f : 0.f);
+            const bool la = sa > kEps, lb = sb > kEps;
+            cmass += (la ? 1.f : 0.f) + (lb ? 1.f : 0.f);
+            cgrow += (fpa > kEps ? 1.f : 0.f) + (fpb > kEps ? 1.f : 0.f);
+            liveA |= la;
+            liveB |= lb;
+            if (k1 == 0 || k1 == P - 1) liveX |= (x == 0 || x == N - 1) && (la || lb);
+          }
           if (a.traj_cells) {
             float* tc = a.traj_cells + tbase;
             tc[(2 * r) * N + x] = sa;
@@ -343,6 +345,7 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
             tp[(2 * r + 1) * N + x] = pb;
           }
         }
+        if constexpr (STATS) {
         // live cell on the outer layer of the un-centred torus (box stop set)
         const bool border = liveX || (r == 0 && liveA) || (r == N / 2 - 1 && liveB);
         const float Sa = S2.x, Sb = S2.y, Ga = G2.x, Gb = G2.y;
@@ -363,12 +366,13 @@ __device__ __forceinline__ void resident_item(const ResidentArgs& a, int item, c
         for (int i = 12; i < 16; ++i) acc[i] = 0.f;
         const float tot = warp_sum16(acc);  // lane L: total of value L >> 1
         if ((lane & 1) == 0 && lane < 24) part[wid * 16 + (lane >> 1)] = tot;
+        }
       }
       // no barrier here: the next row pass of this group touches only its own
       // packed row, and the next step's first barrier orders these partials
     }
     named_bar(bar_id, NT);
-    if (a.steps > 0 && wid == NW - 1) {
+    if (STATS && a.steps > 0 && wid == NW - 1) {
       finalize(a.steps - 1);
       if (a.shift_out && lane == 0) {  // the lane that advanced the shift
         a.shift_out[2 * world] = shv[0];
