@@ -44,3 +44,27 @@ def test_crop_zero_removes_every_all_zero_index():
     want = O.crop_zero(k)
     assert got.shape == want.shape == (2, 3, 3)  # rows 0, 2, 4; columns 1, 4, 5
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize('shape', [(4, 1, 3, 3), (2, 1, 8, 6), (1, 1, 5, 4, 7)])
+def test_potential_builder_pads_like_the_reference(shape):
+    # helpers.py:465-481: (d // 2, d // 2 - 1) for even kernel sides,
+    # (d // 2, d // 2) for odd ones, after the batch and channel axes
+    from leniax_gb300 import helpers
+    fn = helpers.build_get_potential_fn(shape, [True] * shape[0], fft=False)
+    want = [(0, 0), (0, 0)] + [(d // 2, d // 2 - 1) if d % 2 == 0 else (d // 2, d // 2) for d in shape[2:]]
+    assert list(fn.keywords['padding']) == want
+    assert fn.keywords['tc_indices'] == tuple(range(shape[0]))
+    assert list(fn.keywords['padding']) == list(O.conv_padding(shape))
+
+
+def test_field_builder_flattens_growth_functions_in_channel_order():
+    # helpers.py:490-516: the growth functions of every channel, in order,
+    # and the weighted mean (or sum)
+    from leniax_gb300 import core, growth_functions, helpers
+    fn = helpers.build_get_field_fn([['gaussian', 'poly_quad4'], [], ['step']], average=False)
+    assert fn.keywords['growth_fn_t'] == (growth_functions.gaussian, growth_functions.poly_quad4,
+                                          growth_functions.step)
+    assert fn.keywords['weighted_fn'] is core.weighted_sum
+    assert helpers.build_get_field_fn([['identity']]).keywords['weighted_fn'] is core.weighted_mean
+    assert growth_functions.engine_id('triangle') == growth_functions.triangle.id
