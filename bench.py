@@ -302,6 +302,7 @@ def run_ours(args, rank, world_size):
     adjoint = measure_adjoint(dev, fp32_peak=fp32_peak)
     adjoint['variant_3d'] = measure_adjoint_3d(dev)
     multichannel = measure_multichannel(dev, fp32_peak=fp32_peak)
+    nd = measure_nd(dev, fp32_peak=fp32_peak)
     uneven = measure_uneven(dev, fp32_peak=fp32_peak)
 
     gpu_launches = args.steps * 4  # prepare spectrum, resident kernel, stats, heuristics per rollout
@@ -344,6 +345,7 @@ def run_ours(args, rank, world_size):
         },
         'adjoint': adjoint,
         'multichannel': multichannel,
+        'nd': nd,
         'uneven': uneven,
         'clocks': clocks,
         'gpu_launches': gpu_launches,
@@ -523,6 +525,47 @@ def measure_multichannel(dev, worlds=256, size=256, C=3, per_channel=5, steps=51
         'roofline_fp32': {'bound': 'fp32', 'achieved': tflops, 'peak': fp32_peak, 'unit': 'TFLOP/s',
                           'frac': tflops / fp32_peak if fp32_peak else None,
                           'flops_per_world_step': flops_per_world_step(C, nk, P)},
+        'l2': 'flushed between timed rollouts (256 MB write)',
+    }
+
+
+def measure_nd(dev, worlds=64, size=48, steps=64, reps=2, fp32_peak=None):
+    """The general N-D engine on 3D worlds no specialised engine serves: 64
+    worlds of 48x48x48 (bump kernel R=8, gaussian growth m=0.15 s=0.03,
+    dt=0.1, uniform[0,1) central 16^3 patches), 64 steps with leniax
+    statistics and both stop sets; FP32 roofline of the algorithmic flops."""
+    import torch
+    from leniax_gb300 import helpers, kernels, runner, statistics
+    R_nd = 8.0
+    kp = [dict(KPARAMS[0], gf_params=[0.15, 0.03])]
+    K, mp = kernels.get_kernels_and_mapping([dict(p) for p in kp], [size] * 3, 1, R_nd, True, dev)
+    upd = helpers.build_update_fn(K.shape, mp)
+    stats_fn = statistics.ComputeStatsFn([size] * 3, R_nd, T_RATE)
+    rng = np.random.Generator(np.random.PCG64(5))
+    c = np.zeros((1, worlds, 1, size, size, size), np.float32)
+    lo, p = (size - size // 3) // 2, size // 3
+    c[..., lo:lo + p, lo:lo + p, lo:lo + p] = rng.random((worlds, 1, p, p, p), dtype=np.float32)
+    cells = torch.from_numpy(c).to(dev)
+    gf, w, T = mp.get_gf_params(dev)[None], mp.get_kernels_weight_per_channel(dev)[None], torch.tensor([T_RATE])
+
+    def run(n_steps):
+        return runner.run_scan_mem_optimized(None, cells, K[None], gf, w, T, n_steps, R_nd, upd, stats_fn,
+                                             with_box=True)
+
+    run(4)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ms = _timed(lambda: run(steps), torch.cuda.current_stream(dev), flush, reps)
+    P = size**3
+    flops = flops_per_world_step(1, 1, P) * worlds * steps
+    tflops = flops / (ms / 1e3) / 1e12
+    return {
+        'workload': f'nd-{worlds}x{size}x{size}x{size}-c1k1-{steps}steps', 'engine': 'nd', 'metric': METRIC,
+        'value': worlds * P * steps / (ms / 1e3), 'unit': METRIC, 'ms_per_rollout': ms,
+        'ms_per_euler_step': ms / steps,
+        'roofline_fp32': {'bound': 'fp32', 'achieved': tflops, 'peak': fp32_peak, 'unit': 'TFLOP/s',
+                          'frac': tflops / fp32_peak if fp32_peak else None,
+                          'flops_per_world_step': flops_per_world_step(1, 1, P)},
         'l2': 'flushed between timed rollouts (256 MB write)',
     }
 
