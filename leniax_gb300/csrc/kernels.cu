@@ -85,7 +85,7 @@ __device__ __forceinline__ float ring_value(const RingArgs& a, int k, long cell,
   for (int ax = a.nd - 1; ax >= 0; --ax) {
     const int o = (int)(rest % N);
     rest /= N;
-    const int p = (o + N / 2) & (N - 1);  // unshifted padded index
+    const int p = (o - N / 2 + N) % N;  // unshifted padded index (fftshift rolls by N // 2)
     const int i = p - pad;
     inside = inside && i >= 0 && i < 2 * krp;
     cc[ax] = ((float)i - (float)krp) / rR;
@@ -181,10 +181,8 @@ __global__ void __launch_bounds__(128) zline_fft_kernel(long lines, float2* __re
 int validate(const lgx_ring_batch* j) {
   if (!j) return kfail(LGX_ERR_INVALID, "lgx_ring_kernels: null job");
   if (j->nb_dims != 2 && j->nb_dims != 3) return kfail(LGX_ERR_INVALID, "lgx_ring_kernels: nb_dims must be 2 or 3");
-  const bool ok2 = j->nb_dims == 2 && (j->size == 32 || j->size == 64 || j->size == 128 || j->size == 256);
-  const bool ok3 = j->nb_dims == 3 && (j->size == 32 || j->size == 64);
-  if (!ok2 && !ok3)
-    return kfail(LGX_ERR_UNSUPPORTED, "lgx_ring_kernels: %dD worlds of side %d (2D 32..256, 3D 32/64)", j->nb_dims,
+  if (!nd_side_ok(j->size))
+    return kfail(LGX_ERR_UNSUPPORTED, "lgx_ring_kernels: %dD worlds of side %d (the N-D engine's sides)", j->nb_dims,
                  j->size);
   if (j->n < 1) return kfail(LGX_ERR_INVALID, "lgx_ring_kernels: n must be >= 1");
   if (j->kf_id < LGX_KF_POLY_QUAD || j->kf_id > LGX_KF_TRIANGLE)
@@ -201,6 +199,19 @@ long cells_of(const lgx_ring_batch* j) {
   return c;
 }
 
+// the register-resident spectrum of the resident / streamed sizes, else the
+// N-D engine's line passes
+bool fast_spectrum(const lgx_ring_batch* j) {
+  return (j->nb_dims == 2 && (j->size == 32 || j->size == 64 || j->size == 128 || j->size == 256)) ||
+         (j->nb_dims == 3 && (j->size == 32 || j->size == 64));
+}
+
+size_t spectrum_ws_bytes(const lgx_ring_batch* j) {
+  if (fast_spectrum(j)) return al256((size_t)j->n * cells_of(j) * sizeof(float));
+  const int world[3] = {j->size, j->size, j->size};
+  return nd_spectrum_workspace_bytes(j->nb_dims, world, j->n);
+}
+
 }  // namespace
 
 extern "C" {
@@ -210,7 +221,7 @@ int lgx_ring_kernels_workspace_bytes(const lgx_ring_batch* j, size_t* bytes) {
   *bytes = 0;
   const int v = validate(j);
   if (v != LGX_OK) return v;
-  *bytes = al256((size_t)j->n * sizeof(float)) + al256((size_t)j->n * cells_of(j) * sizeof(float));
+  *bytes = al256((size_t)j->n * sizeof(float)) + spectrum_ws_bytes(j);
   return LGX_OK;
 }
 
@@ -245,7 +256,11 @@ int lgx_ring_kernels(const lgx_ring_batch* j, void* ws, size_t ws_bytes, void* s
   ring_normalise_kernel<<<(unsigned)std::min<long>((total + 255) / 256, 8192), 256, 0, st>>>(cells, j->n,
                                                                                            j->kernel_out, sums);
   if ((e = cudaGetLastError()) != cudaSuccess) return kfail(LGX_ERR_CUDA, "lgx_ring_kernels: %s", cudaGetErrorString(e));
-  if (j->k_half) {
+  if (j->k_half && !fast_spectrum(j)) {
+    const int world[3] = {j->size, j->size, j->size};
+    e = launch_nd_spectrum(j->nb_dims, world, j->n, j->kernel_out, reinterpret_cast<float2*>(j->k_half), spec_ws, st);
+    if (e != cudaSuccess) return kfail(LGX_ERR_CUDA, "lgx_ring_kernels spectrum: %s", cudaGetErrorString(e));
+  } else if (j->k_half) {
     const int N = j->size;
     float2* kh = reinterpret_cast<float2*>(j->k_half);
     const int planes = j->nb_dims == 2 ? j->n : j->n * N;  // 3D: every z plane first

@@ -241,8 +241,9 @@ def ring_kernels(world: Sequence[int], R, r, b, kf_slug: str, kf_params, spectru
     ``r[i]``, ring weights ``b[i]`` (list) and kernel-function parameters
     ``kf_params[i]``; placed and fftshifted on the world grid as
     ``get_kernels_and_mapping`` does.  Returns ``(kernels [n, *world] float32,
-    K_half [n, *world[:-1], W//2+1] complex64 or None)``.  2D worlds of side
-    32..256, 3D worlds of side 32 or 64."""
+    K_half [n, *world[:-1], W//2+1] complex64 or None)``.  Square 2D and
+    cubic 3D worlds of any side the N-D engine takes (odd and prime sides
+    included: fftshift rolls by side // 2)."""
     import ctypes
     from . import _lib
     world = [int(w) for w in world]

@@ -23,7 +23,8 @@ CASES = [
 ]
 
 
-@pytest.mark.parametrize('world', [[32, 32], [64, 64], [128, 128], [256, 256], [32, 32, 32], [64, 64, 64]])
+@pytest.mark.parametrize('world', [[32, 32], [64, 64], [128, 128], [256, 256], [32, 32, 32], [64, 64, 64],
+                                   [48, 48], [45, 45], [100, 100], [66, 66], [24, 24, 24], [27, 27, 27]])
 @pytest.mark.parametrize('kf_slug,kf_params,b', CASES)
 def test_ring_kernels_match_host_construction(cuda, world, kf_slug, kf_params, b):
     size = world[0]
