@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define LGX_ABI_VERSION 1
+#define LGX_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define LGX_API __attribute__((visibility("default")))
@@ -137,6 +137,10 @@ typedef struct lgx_rollout {
                             stream right before and after its dominant kernel(s)
                             (the resident kernel, or the streamed step loop), so
                             callers can time them without a host sync; NULL to skip */
+  const float* stats_R_sol; /* [Ns] per-solution static R of compute_stats, or NULL:
+                               stats_R for every solution (uneven batches give every
+                               world its own R)                                    */
+  const float* stats_T_sol; /* [Ns] per-solution static T, or NULL: stats_T        */
 } lgx_rollout;
 
 /* ABI version (LGX_ABI_VERSION). */

@@ -90,6 +90,8 @@ class Rollout(ctypes.Structure):
         ('engine', ctypes.c_int),
         ('centroid', _fp),
         ('main_events', _fp * 2),
+        ('stats_R_sol', _fp),
+        ('stats_T_sol', _fp),
     ]
 
 
@@ -138,7 +140,7 @@ def load():
         lib.lgx_state.argtypes = [ci, ci, cl, ci, vp, vp, vp, ci, vp, vp]
         for f in (lib.lgx_growth, lib.lgx_weighted, lib.lgx_field, lib.lgx_state):
             f.restype = ci
-        if lib.lgx_version() != 1:
+        if lib.lgx_version() != 2:
             raise RuntimeError('leniax_gb300 engine ABI version mismatch')
         _lib = lib
         return lib

@@ -6,7 +6,10 @@ leniax batches a search with ``jax.vmap`` over identically shaped worlds
 world size and one R at a time).  Here every world carries its own kernel
 spectrum (its own R), ``(m, s)``, kernel weight and ``T``; worlds of one shape
 form a :class:`WorldClass`, and :class:`UnevenBatch` runs up to eight classes
-(2D 32^2/64^2/128^2/256^2, 3D 32^3/64^3) through ``lgx_batch_run``:
+(2D 32^2/64^2/128^2/256^2, 3D 32^3/64^3) through ``lgx_batch_run``, and any
+number of classes of other shapes (every world the N-D engine takes: odd,
+prime, non-square, large, other 3D sides) through one ``lgx_run`` each on the
+same stream (every world its own solution, with its own statistics R and T):
 
 * a device work queue (one item = 8, 4 or 1 small 2D worlds, or one large
   world) consumed by one 512-thread CTA per SM with an atomic counter,
@@ -144,11 +147,15 @@ class UnevenBatch:
         self.device = classes[0].cells0.device
         self.inputs = []
         self.outputs = []
-        arr = (BatchClassC * len(classes))()
+        # classes of the persistent launch; the others run through lgx_run
+        self._persistent = [i for i, c in enumerate(classes)
+                            if (len(c.world), c.world[0]) in SHAPES and all(w == c.world[0] for w in c.world)]
+        if len(self._persistent) > MAX_CLASSES:
+            raise ValueError(f'at most {MAX_CLASSES} classes of the persistent shapes, got {len(self._persistent)}')
+        self._generic = []  # (class index, plan, Rollout, workspace)
+        arr = (BatchClassC * max(1, len(self._persistent)))()
         for i, c in enumerate(classes):
             nd, size = len(c.world), c.world[0]
-            if (nd, size) not in SHAPES or any(w != size for w in c.world):
-                raise ValueError(f'class {i}: world {c.world} not supported (2D 32/64/128/256, 3D 32/64, square)')
             for name in ('cells0', 'gf_params', 'weights', 'T', 'R'):
                 _require_cuda(f'class {i} {name}', getattr(c, name))
             if c.gf_slug not in _lib.GF_IDS or c.state_slug not in _lib.STATE_IDS:
@@ -170,7 +177,10 @@ class UnevenBatch:
                 out['centroid'] = torch.empty((n, max(self.steps, 1), nd), device=self.device)
             self.inputs.append(dict(zip(('cells0', 'k_half', 'gf_params', 'weights', 'T', 'R', 'T_static'), ins)))
             self.outputs.append(out)
-            a = arr[i]
+            if i not in self._persistent:
+                self._generic.append(self._generic_run(i, c, ins, out))
+                continue
+            a = arr[self._persistent.index(i)]
             a.nb_dims, a.size, a.n_worlds = nd, size, n
             a.gf_id, a.state_fn, a.mean = _lib.GF_IDS[c.gf_slug], _lib.STATE_IDS[c.state_slug], int(c.average)
             a.cells0, a.k_half, a.gf_params, a.weights, a.T, a.stats_R, a.stats_T = [t.data_ptr() for t in ins]
@@ -180,19 +190,43 @@ class UnevenBatch:
                 a.n_box, a.centroid = out['N_box'].data_ptr(), out['centroid'].data_ptr()
         self._arr = arr
         job = BatchJobC()
-        job.n_classes, job.steps, job.classes = len(classes), self.steps, arr
+        job.n_classes, job.steps, job.classes = len(self._persistent), self.steps, arr
         job.order, job.grid, job.line_group = ORDERS[order], self.grid, self.line_group
         self.class_order = list(class_order) if class_order is not None else None
         if order == 'explicit':
             if self.class_order is None:
                 raise ValueError("order='explicit' needs class_order")
-            self._order_arr = (ctypes.c_int * len(self.class_order))(*self.class_order)
+            # the queue order of the persistent classes, in their own indices
+            persistent_order = [self._persistent.index(i) for i in self.class_order if i in self._persistent]
+            self._order_arr = (ctypes.c_int * max(1, len(persistent_order)))(*persistent_order)
             job.class_order = self._order_arr
         self._job = job
-        nbytes = ctypes.c_size_t(0)
-        _lib.check(self.lib.lgx_batch_workspace_bytes(ctypes.byref(job), ctypes.byref(nbytes)))
-        self.ws = workspace(nbytes.value, self.device)
+        self.ws = None
+        if self._persistent:
+            nbytes = ctypes.c_size_t(0)
+            _lib.check(self.lib.lgx_batch_workspace_bytes(ctypes.byref(job), ctypes.byref(nbytes)))
+            self.ws = workspace(nbytes.value, self.device)
         self.graph = None
+
+    def _generic_run(self, i, c, ins, out):
+        """The lgx_run job of a class the persistent launch does not take:
+        its n worlds as n solutions of one init each."""
+        nd = len(c.world)
+        plan = _lib.Plan(nd, tuple(c.world), 1, [0], [0], [_lib.GF_IDS[c.gf_slug]], 1, _lib.STATE_IDS[c.state_slug],
+                         bool(c.average))
+        job = _lib.Rollout()
+        job.n_sols, job.n_init, job.steps = c.n, 1, self.steps
+        job.cells0, job.k_half, job.gf_params, job.weights, job.T = [t.data_ptr() for t in ins[:5]]
+        job.stats_R, job.stats_T = 1.0, 1.0  # overridden per world below
+        job.stats_R_sol, job.stats_T_sol = ins[5].data_ptr(), ins[6].data_ptr()
+        job.final_cells = out['final'].data_ptr()
+        if self.with_stats:
+            # [n, steps, 12] / [n] / [n, steps, nd] are lgx_run's [Ns, steps, Ni = 1, ...] layouts
+            job.stats, job.n_continue = out['stats'].data_ptr(), out['N'].data_ptr()
+            job.n_box, job.centroid = out['N_box'].data_ptr(), out['centroid'].data_ptr()
+        job.engine = 0
+        ws = workspace(self.lib.lgx_run_workspace_bytes(plan.handle, c.n, 1, self.steps, 0), self.device)
+        return i, plan, job, ws
 
     @property
     def cells_per_run(self) -> int:
@@ -201,7 +235,10 @@ class UnevenBatch:
     def launch(self, stream=None):
         """Enqueue one rollout on ``stream`` (default: the current stream)."""
         h = stream.cuda_stream if stream is not None else _stream_handle(self.device)
-        _lib.check(self.lib.lgx_batch_run(ctypes.byref(self._job), self.ws.data_ptr(), self.ws.numel(), h))
+        if self._persistent:
+            _lib.check(self.lib.lgx_batch_run(ctypes.byref(self._job), self.ws.data_ptr(), self.ws.numel(), h))
+        for _, plan, job, ws in self._generic:
+            _lib.check(self.lib.lgx_run(plan.handle, ctypes.byref(job), ws.data_ptr(), ws.numel(), h))
 
     def capture(self):
         """Capture :meth:`launch` in a CUDA graph; :meth:`run` then replays it."""
@@ -227,7 +264,11 @@ class UnevenBatch:
     def status(self) -> int:
         """Device status word of the last run (0: ok; 1: a staged copy did not
         land within its bounded wait).  Synchronises the current stream."""
-        return _lib.workspace_status(self.ws.data_ptr(), torch.cuda.current_stream(self.device).cuda_stream)
+        h = torch.cuda.current_stream(self.device).cuda_stream
+        code = _lib.workspace_status(self.ws.data_ptr(), h) if self.ws is not None else 0
+        for _, _, _, ws in self._generic:
+            code = code or _lib.workspace_status(ws.data_ptr(), h)
+        return code
 
     def results(self) -> List[Dict[str, torch.Tensor]]:
         """Per class: ``final`` cells and, with statistics, leniax's stats dict

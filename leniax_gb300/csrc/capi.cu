@@ -606,6 +606,8 @@ int lgx_run(const lgx_plan* plan, const lgx_rollout* j, void* ws, size_t ws_byte
   for (int i = 0; i < 3; ++i) sa.world[i] = m.world[i];
   sa.R = j->stats_R;
   sa.T = j->stats_T;
+  sa.R_arr = j->stats_R_sol;
+  sa.T_arr = j->stats_T_sol;
   sa.raw = raw;
   sa.stats = j->stats;
   sa.n_continue = j->n_continue;

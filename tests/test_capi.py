@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol():
     lib = _lib.load()
     for s in declared_symbols():
         assert hasattr(lib, s), s
-    assert lib.lgx_version() == 1
+    assert lib.lgx_version() == 2
 
 
 def _plan(**kw):

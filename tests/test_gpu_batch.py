@@ -185,3 +185,43 @@ def test_autotuner_picks_a_candidate_and_caches_it(cuda, tmp_path, monkeypatch):
     s1 = autotune.tuned_settings(classes, 16)
     s2 = autotune.tuned_settings(classes, 16)
     assert s1 == s2 and (tmp_path / 'tune.json').exists()
+
+
+def test_classes_of_any_shape_run_beside_the_persistent_launch(cuda):
+    # shapes the persistent launch does not take (100^2, odd 45^2, prime-
+    # factored 66^2, 3D 24^3) run through lgx_run with every world its own
+    # solution and its own statistics R and T; every world matches the
+    # oracle run alone, and a graph replay reproduces a launch
+    dev = torch.device('cuda')
+    spec = [(2, 64, 3, (8, 12)), (2, 100, 2, (10, 16)), (2, 45, 2, (6, 9)), (2, 66, 2, (8, 12)),
+            (3, 24, 2, (4, 6))]
+    params = _world_params(spec, 11)
+    classes, cells = _classes(dev, spec, params)
+    steps = 16
+    b = lbatch.UnevenBatch(classes, steps)
+    b.run()
+    res = b.results()
+    assert b.status() == 0
+    for ci, ((nd, size, n, _), (R, m, s, T)) in enumerate(zip(spec, params)):
+        fin = res[ci]['final'].cpu().numpy()
+        st = {k: v.cpu().numpy() for k, v in res[ci]['stats'].items()}
+        for w in range(n):
+            o64, f64 = _oracle_world(nd, size, cells[ci][w], R[w], m[w], s[w], T[w], steps, np.float64)
+            o32, f32 = _oracle_world(nd, size, cells[ci][w], R[w], m[w], s[w], T[w], steps, np.float32)
+            tag = f'{nd}D {size} world {w}'
+            spread = np.abs(f32 - f64).max()
+            assert np.abs(fin[w] - f64[0, 0]).max() <= max(2e-4, 8 * spread), (tag, spread)
+            assert int(st['N'][w, 0]) == int(o64['N'][0]), tag
+            assert int(st['N_box'][w, 0]) == int(o64['N_box'][0]), tag
+            mass, m64, m32 = st['mass'][w, :, 0], o64['mass'][:, 0], o32['mass'][:, 0]
+            tol = np.maximum(1e-4 * np.abs(m64), 8 * np.abs(m32 - m64)) + 1e-7
+            assert (np.abs(mass - m64) <= tol).all(), tag
+            # per-world R and T reach the statistics (mass_volume counts / R^2)
+            mv, mv64 = st['mass_volume'][w, :, 0], o64['mass_volume'][:, 0]
+            assert np.allclose(mv, mv64, rtol=1e-4, atol=8 / float(R[w])**2), tag
+    want = [r['final'].clone() for r in res]
+    g = lbatch.UnevenBatch(classes, steps).capture()
+    g.run()
+    torch.cuda.synchronize()
+    for a, r in zip(want, g.results()):
+        assert torch.equal(a, r['final'])
