@@ -11,6 +11,9 @@ device it will run on:
   radix-16 in-register pass for 64^3) when a 3D class is present;
 * the persistent grid: one CTA per SM, or fewer when the queue is shorter.
 
+Only the classes of the persistent launch are tuned; classes of other shapes
+run through one ``lgx_run`` each whatever the settings.
+
 Results are cached per device and class signature in a JSON file
 (``$LGX_AUTOTUNE_CACHE`` or ``~/.cache/leniax_gb300/autotune.json``).
 """
@@ -22,7 +25,7 @@ from typing import Dict, List
 
 import torch
 
-from .batch import UnevenBatch, WorldClass
+from .batch import UnevenBatch, WorldClass, persistent_shape
 
 _lock = threading.Lock()
 
@@ -37,7 +40,7 @@ def cache_path() -> str:
 def signature(classes: List[WorldClass]) -> str:
     dev = classes[0].cells0.device
     name = torch.cuda.get_device_name(dev)
-    parts = [f'{len(c.world)}d{c.world[0]}x{c.n}:{c.gf_slug}:{c.state_slug}' for c in classes]
+    parts = [f'{len(c.world)}d{"x".join(map(str, c.world))}:n{c.n}:{c.gf_slug}:{c.state_slug}' for c in classes]
     return name + '|' + ','.join(parts)
 
 
@@ -86,33 +89,41 @@ def _items(c: WorldClass) -> int:
 
 
 def tune(classes: List[WorldClass], steps: int, probe_steps: int = 8, reps: int = 3) -> Dict:
-    """Time the candidates on ``probe_steps``-step rollouts; return the best
-    settings (keyword arguments of :class:`UnevenBatch`) and the timings."""
+    """Time the candidates on ``probe_steps``-step rollouts of the persistent
+    classes; return the best settings (keyword arguments of
+    :class:`UnevenBatch`, class indices into ``classes``) and the timings."""
     probe_steps = max(1, min(int(steps), int(probe_steps)))
-    sms = torch.cuda.get_device_properties(classes[0].cells0.device).multi_processor_count
-    has3d = any(len(c.world) == 3 for c in classes)
+    pers = [i for i, c in enumerate(classes) if persistent_shape(c.world)]
+    if not pers:
+        return {'settings': dict(order='largest_first', line_group=4, grid=0), 'item_ms': [None] * len(classes),
+                'probe_steps': probe_steps, 'candidates': []}
+    sub = [classes[i] for i in pers]
+    sms = torch.cuda.get_device_properties(sub[0].cells0.device).multi_processor_count
+    has3d = any(len(c.world) == 3 for c in sub)
     lgs = [4, 2] if has3d else [4]
     # measured cost of one item of each class, with the best line width per class
-    item_ms = []
-    for c in classes:
-        best = math.inf
+    item_ms = [None] * len(classes)
+    for i in pers:
+        c, best = classes[i], math.inf
         for lg in (lgs if len(c.world) == 3 else [4]):
             b = UnevenBatch([c], probe_steps, line_group=lg, with_stats=False)
             t = _time(b, reps)
             waves = math.ceil(_items(c) / min(sms, _items(c)))
             best = min(best, t / waves)
-        item_ms.append(best)
-    measured = sorted(range(len(classes)), key=lambda i: -item_ms[i])
+        item_ms[i] = best
+    measured = sorted(range(len(sub)), key=lambda j: -item_ms[pers[j]])
     cands = []
     for lg in lgs:
         cands.append(dict(order='explicit', class_order=measured, line_group=lg, grid=0))
         cands.append(dict(order='largest_first', line_group=lg, grid=0))
     timings = []
     for kw in cands:
-        b = UnevenBatch(classes, probe_steps, with_stats=False, **kw)
+        b = UnevenBatch(sub, probe_steps, with_stats=False, **kw)
         timings.append((_time(b, reps), kw))
     timings.sort(key=lambda x: x[0])
     best = dict(timings[0][1])
+    if 'class_order' in best:  # indices into the persistent classes -> into ``classes``
+        best['class_order'] = [pers[j] for j in best['class_order']]
     return {'settings': best, 'item_ms': item_ms, 'probe_steps': probe_steps,
             'candidates': [{'ms': t, **kw} for t, kw in timings]}
 

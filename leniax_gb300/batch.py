@@ -66,6 +66,12 @@ def _bind(lib):
     return lib
 
 
+def persistent_shape(world: Sequence[int]) -> bool:
+    """Whether worlds of this shape run in the persistent launch (square or
+    cubic sides of ``SHAPES``); every other shape runs through ``lgx_run``."""
+    return (len(world), world[0]) in SHAPES and all(w == world[0] for w in world)
+
+
 @dataclass
 class WorldClass:
     """Worlds of one shape.  ``cells0`` ``[n, *world]`` float32; ``K`` each
@@ -135,8 +141,8 @@ class UnevenBatch:
 
     def __init__(self, classes: List[WorldClass], steps: int, order='largest_first', grid=0, line_group=4,
                  with_stats=True, class_order: Optional[Sequence[int]] = None):
-        if not 1 <= len(classes) <= MAX_CLASSES:
-            raise ValueError(f'1..{MAX_CLASSES} world classes, got {len(classes)}')
+        if not classes:
+            raise ValueError('an uneven batch needs at least one world class')
         if order not in ORDERS:
             raise ValueError(f'order must be one of {sorted(ORDERS)}')
         self.lib = _bind(_lib.load())
@@ -148,8 +154,7 @@ class UnevenBatch:
         self.inputs = []
         self.outputs = []
         # classes of the persistent launch; the others run through lgx_run
-        self._persistent = [i for i, c in enumerate(classes)
-                            if (len(c.world), c.world[0]) in SHAPES and all(w == c.world[0] for w in c.world)]
+        self._persistent = [i for i, c in enumerate(classes) if persistent_shape(c.world)]
         if len(self._persistent) > MAX_CLASSES:
             raise ValueError(f'at most {MAX_CLASSES} classes of the persistent shapes, got {len(self._persistent)}')
         self._generic = []  # (class index, plan, Rollout, workspace)
