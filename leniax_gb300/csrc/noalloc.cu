@@ -162,6 +162,8 @@ extern "C" LGX_API int lgx_run_noalloc(const lgx_plan* plan, const lgx_rollout* 
   for (int i = 0; i < 3; ++i) sa.world[i] = m.world[i];
   sa.R = j->stats_R;
   sa.T = j->stats_T;
+  sa.R_arr = j->stats_R_sol;
+  sa.T_arr = j->stats_T_sol;
   sa.raw = raw;
   sa.stats = j->stats;
   sa.n_continue = j->n_continue;

@@ -27,8 +27,10 @@ def _bind(lib):
     lib.lgx_noalloc_last_error.restype = ctypes.c_char_p
 
 
-def _job(cells, kh, gf, w, T, steps, outs, R):
+def _job(cells, kh, gf, w, T, steps, outs, R, per_sol=None):
     job = _lib.Rollout()
+    if per_sol is not None:  # per-solution statistics R and T
+        job.stats_R_sol, job.stats_T_sol = per_sol[0].data_ptr(), per_sol[1].data_ptr()
     job.n_sols, job.n_init, job.steps = cells.shape[0], cells.shape[1], steps
     job.cells0, job.k_half, job.gf_params, job.weights, job.T = (cells.data_ptr(), kh.data_ptr(), gf.data_ptr(),
                                                                   w.data_ptr(), T.data_ptr())
@@ -75,13 +77,15 @@ def _model(size, dev):
     return upd, kh, gf, w, torch.tensor([10.0, 5.0], device=dev), R
 
 
-@pytest.mark.parametrize('size,traj', [(32, False), (64, False), (128, False), (64, True)])
-def test_noalloc_rollout_matches_workspace_rollout_twice(cuda, size, traj):
+@pytest.mark.parametrize('size,traj,per_sol', [(32, False, False), (64, False, False), (128, False, False),
+                                               (64, True, False), (64, False, True)])
+def test_noalloc_rollout_matches_workspace_rollout_twice(cuda, size, traj, per_sol):
     dev = cuda
     lib = _lib.load()
     _bind(lib)
     steps, n_sols, n_init = (24 if traj else 48), 2, 5
     upd, kh, gf, w, T, R = _model(size, dev)
+    sol = (torch.tensor([R, 2.0 * R], device=dev), torch.tensor([10.0, 7.0], device=dev)) if per_sol else None
     plan = upd.model.plan.handle
     stream = torch.cuda.current_stream(dev).cuda_stream
     for call, seed in enumerate((3, 4)):
@@ -91,9 +95,10 @@ def test_noalloc_rollout_matches_workspace_rollout_twice(cuda, size, traj):
         ref = _outs(cells, steps, dev, traj)
         ws = torch.empty(lib.lgx_run_workspace_bytes(plan, n_sols, n_init, steps, _lib.ENGINES['resident']),
                          dtype=torch.uint8, device=dev)
-        _lib.check(lib.lgx_run(plan, _job(cells, kh, gf, w, T, steps, ref, R), ws.data_ptr(), ws.numel(), stream))
+        _lib.check(lib.lgx_run(plan, _job(cells, kh, gf, w, T, steps, ref, R, sol), ws.data_ptr(), ws.numel(),
+                               stream))
         got = _outs(cells, steps, dev, traj)
-        rc = lib.lgx_run_noalloc(plan, _job(cells, kh, gf, w, T, steps, got, R), stream)
+        rc = lib.lgx_run_noalloc(plan, _job(cells, kh, gf, w, T, steps, got, R, sol), stream)
         assert rc == _lib.LGX_OK, lib.lgx_noalloc_last_error()
         torch.cuda.synchronize()
         # same kernels on the same inputs: the state tolerance of the parity tests (1e-5) holds with margin
@@ -104,6 +109,15 @@ def test_noalloc_rollout_matches_workspace_rollout_twice(cuda, size, traj):
         if traj:
             for a, b in zip(got['traj'], ref['traj']):
                 assert (a - b).abs().max().item() <= 1e-5, call
+        if per_sol:
+            # the second solution's statistics R differs from the scalar one: its mass (/ R^2) does too
+            scalar = _outs(cells, steps, dev)
+            _lib.check(lib.lgx_run(plan, _job(cells, kh, gf, w, T, steps, scalar, R), ws.data_ptr(), ws.numel(),
+                                   stream))
+            torch.cuda.synchronize()
+            assert torch.allclose(scalar['stats'][0], got['stats'][0], rtol=1e-6, atol=1e-7), call
+            mass = 1  # stats columns: channel_mass, mass, ...
+            assert torch.allclose(got['stats'][1, ..., mass] * 4, scalar['stats'][1, ..., mass], rtol=1e-5), call
 
 
 def test_noalloc_zero_steps_returns_the_initial_cells(cuda):
