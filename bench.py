@@ -79,25 +79,40 @@ def host_cores():
         return os.cpu_count() or 1
 
 
+class _OracleSample:
+    """The FP32 numpy/scipy restatement of the path (the oracle) on the host
+    cores: ``run(steps)`` advances CPU_SAMPLE_WORLDS worlds of the workload
+    ``steps`` Euler steps from their initial states (statistics and both stop
+    sets included) and returns the seconds it took."""
+
+    def __init__(self):
+        from oracle import lenia_oracle as O
+        self.O = O
+        self.cores = host_cores()
+        self.K, mp = O.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, np.float32)
+        self.mp, self.model = mp, O.Model(mp)
+        self.cells = make_inputs(CPU_SAMPLE_WORLDS, seed=1)[0]
+
+    def run(self, steps):
+        t0 = time.perf_counter()
+        self.O.run_scan(self.cells, self.K, self.mp['gf_params'], self.mp['weights'], T_RATE, steps, R, self.model,
+                        keep_intermediary=False, workers=self.cores, with_box=True)
+        return time.perf_counter() - t0
+
+    def describe(self, steps, seconds):
+        return (f'{CPU_SAMPLE_WORLDS} worlds x {steps} steps of the workload (numpy/scipy.fft FP32 restatement, '
+                f'scipy workers={self.cores}), {seconds:.1f} s')
+
+
 def cpu_baseline():
-    """FP32 numpy/scipy restatement of the path (the oracle) on the host cores,
-    timed on a bounded sample of the workload."""
-    from oracle import lenia_oracle as O
-    cores = host_cores()
-    K, mp = O.get_kernels_and_mapping([dict(p) for p in KPARAMS], [SIZE, SIZE], 1, R, True, np.float32)
-    model = O.Model(mp)
-    cells = make_inputs(CPU_SAMPLE_WORLDS, seed=1)[0]
-    O.run_scan(cells, K, mp['gf_params'], mp['weights'], T_RATE, 4, R, model, keep_intermediary=False, workers=cores)
-    t0 = time.perf_counter()
-    O.run_scan(cells, K, mp['gf_params'], mp['weights'], T_RATE, CPU_SAMPLE_STEPS, R, model, keep_intermediary=False,
-               workers=cores, with_box=True)
-    dt = time.perf_counter() - t0
+    """The oracle on the host cores, timed on one bounded sample of the
+    workload (CPU_SAMPLE_WORLDS worlds x CPU_SAMPLE_STEPS steps)."""
+    smp = _OracleSample()
+    smp.run(4)
+    dt = smp.run(CPU_SAMPLE_STEPS)
     value = CPU_SAMPLE_WORLDS * P_CELLS * CPU_SAMPLE_STEPS / dt
-    return {
-        'value': value, 'unit': METRIC, 'cores': cores, 'kind': 'port',
-        'sample': f'{CPU_SAMPLE_WORLDS} worlds x {CPU_SAMPLE_STEPS} steps of the workload '
-                  f'(numpy/scipy.fft FP32 restatement, scipy workers={cores}), {dt:.1f} s'
-    }
+    return {'value': value, 'unit': METRIC, 'cores': smp.cores, 'kind': 'port',
+            'sample': smp.describe(CPU_SAMPLE_STEPS, dt)}
 
 
 class ClockSampler:
@@ -693,17 +708,35 @@ def profile_case(args):
     print(json.dumps({'profile_case': name, 'worlds': nw, 'steps': ns, **info}))
 
 
-def run_reference(args):
+def run_reference(args, budget_s=90.0):
     """Reference arm: the reference's CPU algorithm for this path (leniax's JAX
-    is not installable here, so its numpy restatement), all host threads."""
-    cb = cpu_baseline()
+    is not installable here, so its numpy restatement), all host threads.
+    One step is one bounded sample of the workload (CPU_SAMPLE_WORLDS worlds
+    from their initial states, the same number of Euler steps each time),
+    sized from a short calibration so that the ``warmup + steps`` samples take
+    about ``budget_s`` seconds; ``steps`` samples are timed."""
+    smp = _OracleSample()
+    cal_steps = 8
+    smp.run(2)
+    per_step = smp.run(cal_steps) / cal_steps
+    n_samples = max(1, args.warmup + args.steps)
+    euler = int(min(CPU_SAMPLE_STEPS, max(16, budget_s / n_samples / per_step)))
+    for _ in range(args.warmup):
+        smp.run(euler)
+    times = [smp.run(euler) for _ in range(max(1, args.steps))]
+    total = sum(times)
+    value = CPU_SAMPLE_WORLDS * P_CELLS * euler * len(times) / total
+    cb = {'value': value, 'unit': METRIC, 'cores': smp.cores, 'kind': 'port',
+          'sample': smp.describe(euler, total / len(times)) + ' per step'}
     return {
-        'impl': 'reference', 'metric': METRIC, 'value': cb['value'], 'unit': METRIC, 'n_gpus': args.gpus,
-        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': None, 'higher_is_better': True, 'scaling': 'weak',
-        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (PCG64 seeded uniform patches)',
-        'config': {'workload': WORKLOAD, 'parallelism': 'host cores'},
+        'impl': 'reference', 'metric': METRIC, 'value': value, 'unit': METRIC, 'n_gpus': args.gpus,
+        'steps': len(times), 'warmup': args.warmup, 'ms_per_step': 1e3 * total / len(times),
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+        'data': 'synthetic (PCG64 seeded uniform patches)',
+        'config': {'workload': WORKLOAD, 'parallelism': 'host cores',
+                   'step': f'{CPU_SAMPLE_WORLDS} worlds x {euler} Euler steps of the workload'},
         'cpu_baseline': cb,
-        'e2e': {'value': cb['value'], 'unit': METRIC, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'e2e': {'value': value, 'unit': METRIC, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
     }
 
 
