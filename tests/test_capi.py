@@ -106,6 +106,30 @@ def test_any_side_up_to_2048_and_smooth_sides_up_to_4096_take_the_nd_engine(worl
     assert lib.lgx_update_workspace_bytes(p.handle, 3) > 0
 
 
+def _smooth(n):
+    for p in (2, 3, 5, 7):
+        while n % p == 0:
+            n //= p
+    return n == 1
+
+
+def test_side_rule_over_every_side():
+    # a plan takes side n iff 2 <= n <= 4096 with prime factors 2, 3, 5, 7
+    # (mixed-radix lines) or 2 <= n <= 2048 (Bluestein lines); every
+    # accepted side runs on some engine with a sized workspace
+    lib = _lib.load()
+    for n in range(1, 4101):
+        want = 2 <= n and ((n <= 4096 and _smooth(n)) or n <= 2048)
+        try:
+            p = _plan(world=(n, 16))
+        except _lib.LgxError as e:
+            assert not want and e.code == _lib.LGX_ERR_UNSUPPORTED, n
+            continue
+        assert want, n
+        assert lib.lgx_select_engine(p.handle, 1, 1, 0) >= 0, n
+        assert lib.lgx_run_workspace_bytes(p.handle, 1, 1, 2, 0) > 0, n
+
+
 @pytest.mark.parametrize('kw,code', [
     (dict(world=(2053, 64)), _lib.LGX_ERR_UNSUPPORTED),  # a prime above 2048 (Bluestein lines up to 2048)
     (dict(world=(64, 4094)), _lib.LGX_ERR_UNSUPPORTED),  # 4094 = 2 * 23 * 89, above 2048
