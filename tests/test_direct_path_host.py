@@ -46,6 +46,16 @@ def test_crop_zero_removes_every_all_zero_index():
     np.testing.assert_array_equal(got, want)
 
 
+def test_crop_zero_kat():
+    # tests/test_utils.py:20-43: two 4 x 4 kernels cropped to their common 2 x 3 support
+    k = np.zeros((2, 4, 4), np.float32)
+    k[0, 1, 1] = k[0, 2, 1] = k[0, 2, 2] = 1
+    k[1, 1, 2] = k[1, 1, 3] = k[1, 2, 1] = 1
+    want = np.array([[[1, 0, 0], [1, 1, 0]], [[0, 1, 1], [1, 0, 0]]], np.float32)
+    np.testing.assert_array_equal(O.crop_zero(k), want)
+    np.testing.assert_array_equal(kernels.crop_zero(k), want)
+
+
 @pytest.mark.parametrize('shape', [(4, 1, 3, 3), (2, 1, 8, 6), (1, 1, 5, 4, 7)])
 def test_potential_builder_pads_like_the_reference(shape):
     # helpers.py:465-481: (d // 2, d // 2 - 1) for even kernel sides,
