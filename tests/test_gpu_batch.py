@@ -187,6 +187,28 @@ def test_autotuner_picks_a_candidate_and_caches_it(cuda, tmp_path, monkeypatch):
     assert s1 == s2 and (tmp_path / 'tune.json').exists()
 
 
+def test_tuned_settings_with_other_shapes_keep_the_results(cuda, tmp_path, monkeypatch):
+    # classes outside the persistent shapes are not timed; the tuned class
+    # order indexes the full class list; tuned and untuned batches agree
+    # (the untuned one uses the tuned 3D line width: widths differ in
+    # rounding, within the line-width test's 1e-5)
+    from leniax_gb300 import autotune
+    monkeypatch.setenv('LGX_AUTOTUNE_CACHE', str(tmp_path / 'tune.json'))
+    dev = torch.device('cuda')
+    spec = [(2, 45, 2, (6, 9)), (2, 64, 8, (8, 12)), (3, 24, 2, (4, 6)), (3, 32, 2, (5, 8))]
+    classes, _ = _classes(dev, spec, _world_params(spec, 23))
+    res = autotune.tune(classes, 8, probe_steps=2, reps=1)
+    assert res['item_ms'][0] is None and res['item_ms'][2] is None
+    assert res['item_ms'][1] > 0 and res['item_ms'][3] > 0
+    if 'class_order' in res['settings']:
+        assert sorted(res['settings']['class_order']) == [1, 3]
+    tuned = lbatch.UnevenBatch(classes, 8, **res['settings']).run().results()
+    plain = lbatch.UnevenBatch(classes, 8, line_group=res['settings']['line_group']).run().results()
+    for a, b in zip(tuned, plain):
+        assert (a['final'] - b['final']).abs().max().item() <= 1e-5
+        assert torch.equal(a['stats']['N'], b['stats']['N'])
+
+
 def test_classes_of_any_shape_run_beside_the_persistent_launch(cuda):
     # shapes the persistent launch does not take (100^2, odd 45^2, prime-
     # factored 66^2, 3D 24^3) run through lgx_run with every world its own
