@@ -116,15 +116,16 @@ def world_spectra(world: Sequence[int], R: Sequence[float], kernel_params: Dict,
     return K
 
 
-def _half(K: torch.Tensor, world) -> torch.Tensor:
+def _half(K: torch.Tensor, world, n: int) -> torch.Tensor:
     W = world[-1]
     if K.dtype != torch.complex64:
         raise TypeError(f'K must be complex64, got {K.dtype}')
     _require_cuda('K', K, torch.complex64)
     if K.shape[-1] == W:
         K = K[..., :W // 2 + 1]
-    if tuple(K.shape[1:]) != tuple(world[:-1]) + (W // 2 + 1, ):
-        raise ValueError(f'K has shape {tuple(K.shape)}; expected [n, {", ".join(map(str, world[:-1]))}, {W // 2 + 1}]')
+    if tuple(K.shape) != (n, ) + tuple(world[:-1]) + (W // 2 + 1, ):
+        raise ValueError(f'K has shape {tuple(K.shape)}; expected [{n}, {", ".join(map(str, world[:-1]))}, '
+                         f'{W // 2 + 1}]')
     return torch.view_as_real(K.contiguous())
 
 
@@ -170,7 +171,11 @@ class UnevenBatch:
                 t = getattr(c, name)
                 if tuple(t.shape) != shape:
                     raise ValueError(f'class {i}: {name} has shape {tuple(t.shape)}, expected {shape}')
-            kh = _half(c.K, c.world)
+            kh = _half(c.K, c.world, n)
+            if c.T_static is not None:
+                _require_cuda(f'class {i} T_static', c.T_static)
+                if tuple(c.T_static.shape) != (n, ):
+                    raise ValueError(f'class {i}: T_static has shape {tuple(c.T_static.shape)}, expected ({n},)')
             tst = (c.T_static if c.T_static is not None else c.T).float().contiguous()
             ins = [c.cells0.contiguous(), kh, c.gf_params.contiguous(), c.weights.contiguous(), c.T.contiguous(),
                    c.R.float().contiguous(), tst]

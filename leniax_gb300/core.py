@@ -45,6 +45,18 @@ def half_spectrum(K: torch.Tensor, world: Sequence[int]) -> torch.Tensor:
     return torch.view_as_real(K.contiguous())
 
 
+def check_spectra(kh: torch.Tensor, lead: Sequence[int], nb_channels: int, max_k: int, world: Sequence[int]):
+    """Raise unless ``kh`` (the float32 view of half spectra) is ``[*lead,
+    C, max_k, *world[:-1], W//2+1, 2]``: the engine reads exactly that many
+    values through a bare pointer."""
+    world = tuple(int(w) for w in world)
+    want = tuple(int(v) for v in lead) + (nb_channels, max_k) + world[:-1] + (world[-1] // 2 + 1, 2)
+    if tuple(kh.shape) != want:
+        got = ', '.join(map(str, tuple(kh.shape)[:-1]))
+        raise ValueError(f'K spectra [{got}] (half spectrum) do not match [{", ".join(map(str, want[:-1]))}]: '
+                         f'{nb_channels} channels, max_k = {max_k}, world {world}')
+
+
 def direct_spectrum(K: torch.Tensor, world: Sequence[int], nb_channels: int, max_k: int,
                     pads: Optional[Sequence[int]] = None) -> torch.Tensor:
     """The real kernels of leniax's direct-convolution path, ``[...,
@@ -191,8 +203,9 @@ class UpdateFn:
         kh = self.spectra(K if K.device == dev else K.to(dev), m.world)
         if not self.fft:
             kh = kh.unsqueeze(0)
-        if kh.shape[0] != 1:
+        if kh.dim() < 1 or kh.shape[0] != 1:
             raise ValueError('update shares one spectrum across the batch: K must be [1, C, max_k, ...]')
+        check_spectra(kh, (1, ), m.C, m.max_k, m.world)
         gf = gf_params.to(dev, torch.float32).contiguous()
         w = kernels_weight_per_channel.to(dev, torch.float32).contiguous()
         if gf.shape != (m.K, 2) or w.shape != (m.C, m.K):
@@ -273,6 +286,7 @@ def get_potential_fft(state: torch.Tensor, K: torch.Tensor, tc_indices=None, cha
     if K.dim() != 3 + len(world) or K.shape[0] != 1 or K.shape[1] != state.shape[1]:
         raise ValueError(f'K {tuple(K.shape)} is not [1, {state.shape[1]}, max_k, *{world}]')
     kh = half_spectrum(K if K.device == state.device else K.to(state.device), world)
+    check_spectra(kh, (1, ), int(K.shape[1]), int(K.shape[2]), world)
     return _potentials(state, kh, int(K.shape[1]), int(K.shape[2]), tc_indices)
 
 

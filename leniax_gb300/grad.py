@@ -165,7 +165,10 @@ class LeniaRolloutFunction(torch.autograd.Function):
     @staticmethod
     def forward(ctx, cells0, k_real, gf_params, weights, T, update_fn: UpdateFn, steps: int, checkpoint_every: int,
                 clip_grad: str, engine: str = 'auto'):
+        _require_cuda('cells0', cells0)
         m = update_fn.model_for(cells0.shape[3:])
+        if cells0.dim() != 3 + len(m.world) or tuple(cells0.shape[2:]) != (m.C, ) + m.world:
+            raise ValueError(f'cells0 {tuple(cells0.shape)} does not match [Ns, Ni, {m.C}, *{m.world}]')
         dev = cells0.device
         Ns, Ni = cells0.shape[:2]
         nd = len(m.world)
@@ -173,6 +176,10 @@ class LeniaRolloutFunction(torch.autograd.Function):
         k_half = _engine_spectra(m, kernel_spectrum(kr, nd))
         gf = gf_params.detach().float().reshape(Ns, m.K, 2).contiguous()
         w = weights.detach().float().reshape(Ns, m.C, m.K).contiguous()
+        for name, t in (('k_real', kr), ('gf_params', gf), ('weights', w)):
+            _require_cuda(name, t)
+            if t.device != dev:
+                raise ValueError(f'{name} is on {t.device}, cells0 on {dev}')
         Tt = torch.as_tensor(T, dtype=torch.float32, device=dev).reshape(-1).expand(Ns).contiguous()
         k = max(1, int(checkpoint_every))
         ckpts = [cells0.detach().contiguous()]

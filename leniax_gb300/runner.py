@@ -10,7 +10,7 @@ import torch
 
 from . import _lib
 from .constant import EPSILON, START_CHECK_STOP
-from .core import UpdateFn, _require_cuda, _stream_handle, workspace
+from .core import UpdateFn, _require_cuda, _stream_handle, check_spectra, workspace
 from .statistics import ComputeStatsFn, split_stats
 from . import statistics as lstat
 
@@ -31,13 +31,16 @@ def _rollout(update_fn: UpdateFn, compute_stats_fn: ComputeStatsFn, cells0, K, g
         raise ValueError('max_run_iter must be >= 0')
     cells0 = cells0.contiguous()
     kh = update_fn.spectra(K if K.device == dev else K.to(dev), m.world)
-    if kh.shape[0] != Ns:
+    if kh.dim() < 1 or kh.shape[0] != Ns:
         raise ValueError('K must hold one spectrum per solution')
+    check_spectra(kh, (Ns, ), m.C, m.max_k, m.world)
     gf = gf_params.to(dev, torch.float32).reshape(Ns, m.K, 2).contiguous()
     ww = w.to(dev, torch.float32).reshape(Ns, m.C, m.K).contiguous()
     Tt = torch.as_tensor(T, dtype=torch.float32, device=dev).reshape(-1)
     if Tt.numel() == 1 and Ns > 1:
         Tt = Tt.expand(Ns)
+    if Tt.numel() != Ns:
+        raise ValueError(f'T has {Tt.numel()} values for {Ns} solutions')
     Tt = Tt.contiguous()
     nw = Ns * Ni
     S = m.C + _lib.NSTAT_SCALAR

@@ -78,3 +78,15 @@ def test_field_builder_flattens_growth_functions_in_channel_order():
     assert fn.keywords['weighted_fn'] is core.weighted_sum
     assert helpers.build_get_field_fn([['identity']]).keywords['weighted_fn'] is core.weighted_mean
     assert growth_functions.engine_id('triangle') == growth_functions.triangle.id
+
+
+def test_check_spectra_names_the_expected_layout():
+    # the engine reads [*lead, C, max_k, *world[:-1], W//2+1] complex values through a bare pointer
+    from leniax_gb300.core import check_spectra
+    import torch
+    check_spectra(torch.zeros((2, 3, 4, 24, 17, 2)), (2, ), 3, 4, (24, 32))
+    check_spectra(torch.zeros((1, 1, 1, 8, 6, 5, 2)), (1, ), 1, 1, (8, 6, 8))
+    for bad in ((2, 3, 4, 12, 17, 2), (2, 2, 4, 24, 17, 2), (2, 3, 3, 24, 17, 2), (2, 3, 4, 24, 32, 2),
+                (3, 3, 4, 24, 17, 2), (3, 4, 24, 17, 2)):
+        with pytest.raises(ValueError, match='do not match'):
+            check_spectra(torch.zeros(bad), (2, ), 3, 4, (24, 32))

@@ -131,3 +131,40 @@ def test_uneven_batch_with_an_empty_class(cuda):
     for k in rb['stats']:
         assert torch.equal(ra['stats'][k], rb['stats'][k]), k
     assert tuple(a.results()[1]['final'].shape) == (0, 32, 32)
+
+
+def test_inputs_that_do_not_fit_the_model_are_refused_before_any_launch(cuda):
+    # the engine reads spectra, parameters and T through bare pointers: a
+    # tensor of another shape must be refused on the host
+    from leniax_gb300 import core
+    from leniax_gb300 import grad as lgrad
+    from leniax_gb300 import workloads
+    dev = cuda
+    K, mp = kernels.get_kernels_and_mapping(bump_kernel_params(), [64, 64], 1, 10.0, True, dev)
+    upd = helpers.build_update_fn(K.shape, mp)
+    gf, w = mp.get_gf_params(dev), mp.get_kernels_weight_per_channel(dev)
+    state = torch.zeros((2, 1, 64, 64), device=dev)
+    short = K[..., :32, :]  # the spectrum of a 32 x 64 world
+    with pytest.raises(ValueError):
+        upd(None, state, short, gf, w, torch.tensor(0.1, device=dev))
+    with pytest.raises(ValueError):
+        core.get_potential_fft(state, short)
+    stats_fn = statistics.ComputeStatsFn([64, 64], 10.0, 10.0)
+    cells = torch.zeros((1, 2, 1, 64, 64), device=dev)
+    two_channels = torch.cat([K, K], dim=1)[None]  # [Ns = 1, 1, C = 2, max_k, 64, 64] for a one-channel model
+    with pytest.raises(ValueError):
+        runner.run_scan_mem_optimized(None, cells, two_channels, gf[None], w[None], torch.tensor([10.]), 4, 10.0, upd,
+                                      stats_fn)
+    cells2 = torch.zeros((2, 2, 1, 64, 64), device=dev)
+    with pytest.raises(ValueError):  # three T for two solutions
+        runner.run_scan_mem_optimized(None, cells2, torch.stack([K, K]), torch.stack([gf, gf]), torch.stack([w, w]),
+                                      torch.tensor([10., 10., 10.]), 4, 10.0, upd, stats_fn)
+    with pytest.raises(ValueError):  # growth parameters left on the host
+        lgrad.rollout(cells, torch.zeros((1, 1, 64, 64), device=dev), gf[None].cpu(), w[None], torch.tensor([10.]),
+                      upd, 2)
+    with pytest.raises(ValueError):  # one spectrum for two worlds
+        lbatch.UnevenBatch([lbatch.WorldClass(cells0=torch.zeros((2, 32, 32), device=dev),
+                                              K=lbatch.world_spectra((32, 32), [6.0], workloads.RING, dev),
+                                              gf_params=torch.tensor([[0.15, 0.015]] * 2, device=dev),
+                                              weights=torch.ones(2, device=dev), T=torch.full((2, ), 10., device=dev),
+                                              R=torch.full((2, ), 6., device=dev))], 4)
