@@ -77,10 +77,12 @@ extern "C" {
 #define LGX_ENGINE_PLAIN_STREAMED 5 /* one world and one step per launch through the streamed
                                  engine's kernel sequence (row, column, row-inverse and
                                  reduce kernels), for any model the streamed engine runs */
-#define LGX_ENGINE_ND 6       /* general N-D engine: any 2D / 3D world whose sides (2..4096)
-                                 factor into 2, 3, 5 and 7 -- odd, non-square and 3D sides
-                                 such as 48^3 included -- with any C and K; mixed-radix line
-                                 FFT passes over full complex spectra in HBM              */
+#define LGX_ENGINE_ND 6       /* general N-D engine: any 2D / 3D world whose sides are
+                                 2..4096 with prime factors 2, 3, 5, 7 (mixed-radix lines)
+                                 or any side 2..2048 (Bluestein chirp-z lines) -- odd,
+                                 prime, non-square and 3D sides such as 48^3 included --
+                                 with any C and K; line FFT passes over full complex
+                                 spectra in HBM                                          */
 
 /* number of scalar statistics besides the C channel masses */
 #define LGX_NSTAT_SCALAR 11
