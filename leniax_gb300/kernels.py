@@ -1,7 +1,8 @@
 """Kernel construction and mapping: the inputs of the Lenia hot path.
 
 Mirror of leniax ``kernels.py`` (``KernelMapping`` 10-63,
-``get_kernels_and_mapping`` 66-158, ``circle_2d`` 176-212) and
+``get_kernels_and_mapping`` 66-158, ``circle_2d`` 176-212, ``ellipse_2d`` /
+``oriented_ellipse_2d`` 214-311, ``register`` 312-317) and
 ``kernel_functions.py`` (7-261).  This is the once-per-configuration boundary
 preparation (host side, like the reference); the per-step hot path runs in the
 CUDA engine.  The spectrum is returned as a CUDA complex64 tensor
@@ -103,12 +104,58 @@ def circle_2d(R, k_params, kf_slug, kf_params):
     return circle_nd(R, k_params, kf_slug, kf_params, 2)
 
 
+def _ellipse_rings(R, k_params, kf_slug, kf_params):
+    """The part leniax's ``ellipse_2d`` and ``oriented_ellipse_2d`` share
+    (kernels.py:214-311), float32: ``k_params`` = [r, b, a, b_axis,
+    theta / pi]; the grid of ``circle_2d`` rotated by theta, distances on an
+    ellipse of semi-axes a and b_axis (in units of r R), rings as in
+    ``circle_2d``.  Returns the rotated first coordinate and the
+    unnormalised kernel."""
+    f32 = np.float32
+    r = k_params[0]
+    bs = np.asarray(k_params[1], dtype=f32)
+    a, b = f32(k_params[2]), f32(k_params[3])
+    theta = f32(k_params[4] * math.pi)
+    k_radius_px = math.ceil(r * R)
+    coords = np.indices([k_radius_px * 2] * 2).astype(f32)
+    centered = (coords - f32(k_radius_px)) / f32(r * R)
+    cos, sin = np.cos(theta), np.sin(theta)
+    rot0 = centered[0] * cos + centered[1] * sin
+    rot1 = -centered[0] * sin + centered[1] * cos
+    distances = np.sqrt((rot0 / a)**2 + (rot1 / b)**2)
+    nb_b = bs.shape[0]
+    B_dist = f32(nb_b) * distances
+    bs_mat = bs[np.minimum(np.floor(B_dist).astype(np.int64), nb_b - 1)]
+    raw_kernel = kf_register[kf_slug](np.asarray(kf_params, dtype=f32), np.mod(B_dist, f32(1)))
+    return rot0, (distances < 1) * raw_kernel * bs_mat
+
+
+def ellipse_2d(R, k_params, kf_slug, kf_params):
+    """kernels.py:214-259: the elliptic rings normalised to sum 1, then
+    signed by the rotated first coordinate (-1 below -0.01, +1 above 0.01,
+    the coordinate itself in between)."""
+    rot0, kernel = _ellipse_rings(R, k_params, kf_slug, kf_params)
+    kernel = kernel / kernel.sum()
+    sign = rot0.copy()
+    sign[rot0 < -0.01] = -1
+    sign[sign > 0.01] = 1
+    return (kernel * sign).astype(np.float32)[np.newaxis]
+
+
+def oriented_ellipse_2d(R, k_params, kf_slug, kf_params):
+    """kernels.py:262-307: the elliptic rings times the rotated first
+    coordinate, normalised to an absolute sum of 1."""
+    rot0, kernel = _ellipse_rings(R, k_params, kf_slug, kf_params)
+    kernel = kernel * rot0
+    return (kernel / np.abs(kernel).sum()).astype(np.float32)[np.newaxis]
+
+
 def raw(R, k_params, kf_slug, kf_params):
     """kernels.py:161-173"""
     return np.asarray(k_params, dtype=np.float32)
 
 
-register = {'raw': raw, 'circle_2d': circle_2d}
+register = {'raw': raw, 'circle_2d': circle_2d, 'ellipse_2d': ellipse_2d, 'oriented_ellipse_2d': oriented_ellipse_2d}
 
 
 class KernelMapping:
