@@ -300,3 +300,92 @@ def rollout(cells0, k_real, gf_params, weights, T, update_fn: UpdateFn, steps: i
         raise ValueError(f'engine must be one of {ENGINES}')
     return LeniaRolloutFunction.apply(cells0, k_real, gf_params, weights, T, update_fn, steps, checkpoint_every,
                                       clip_grad, engine)
+
+
+def direct_world_kernels(K: torch.Tensor, world: Sequence[int], nb_channels: int, max_k: int, cin: Sequence[int],
+                         slot: Sequence[int]) -> torch.Tensor:
+    """leniax's direct-path kernels ``[*lead, C*max_k, 1, *kernel_dims]``
+    (``kernels.get_kernels_and_mapping(..., fft=False)``) as the world-sized
+    real kernels ``[*lead, K, *world]`` of the true kernels (``cin``,
+    ``slot``), the layout :func:`rollout` takes; differentiable in ``K``.
+
+    ``core.get_potential`` (core.py:105-146) wrap-pads the state by ``k//2``
+    before each axis and cross-correlates: potential[x] = sum_d state[x + d -
+    k//2] K[d].  A world kernel with tap d at index (k//2 - d) mod n gives the
+    same sum as a circular convolution (taps landing on one index add up when
+    a kernel is longer than the world), the placement of
+    ``core.direct_spectrum``."""
+    world = tuple(int(w) for w in world)
+    nd = len(world)
+    if K.dim() < nd + 2 or K.shape[-nd - 1] != 1 or K.shape[-nd - 2] != nb_channels * max_k:
+        raise ValueError(f'direct-path kernels {tuple(K.shape)} are not [..., {nb_channels * max_k}, 1, *kernel_dims]')
+    kd = tuple(int(k) for k in K.shape[-nd:])
+    lead = tuple(K.shape[:-nd - 2])
+    flat = torch.zeros(kd, dtype=torch.long)
+    stride = 1
+    for ax in reversed(range(nd)):
+        pos = (kd[ax] // 2 - torch.arange(kd[ax])) % world[ax]
+        shape = [1] * nd
+        shape[ax] = kd[ax]
+        flat = flat + pos.reshape(shape) * stride
+        stride *= world[ax]
+    taps = K.reshape(lead + (nb_channels * max_k, -1))
+    sel = torch.tensor([c * max_k + s for c, s in zip(cin, slot)], dtype=torch.long, device=K.device)
+    taps = taps.index_select(-2, sel)  # [*lead, K, taps]
+    out = torch.zeros(lead + (len(sel), stride), dtype=K.dtype, device=K.device)
+    out = out.index_add(out.dim() - 1, flat.reshape(-1).to(K.device), taps)
+    return out.reshape(lead + (len(sel), ) + world)
+
+
+class LeniaApply:
+    """The per-step ``apply_fn`` of leniax's differentiable pipelines
+    (``runner.make_pipeline_fn``, runner.py:363-423; the flax ``Step`` of the
+    reference's kernel-learning example) on the engine:
+    ``apply_fn(variables, rng_key, state, dt=dt) -> (state, field,
+    potential)``, differentiable through :func:`rollout`.
+
+    ``variables['params']`` (then ``variables``) holds ``'K'`` -- leniax's
+    direct-path kernels ``[C*max_k, 1, *kernel_dims]`` or world-sized real
+    kernels ``[K, *world]`` (fftshifted: the kernel's centre at index 0) --
+    ``'gf_params'`` ``[K, 2]`` and ``'kernels_weight_per_channel'`` ``[C,
+    K]``; ``state`` is ``[N, C, *world]``.  The adjoint differentiates cell
+    states only, so ``field`` and ``potential`` come back as ``None``.
+    :meth:`rollout` advances several steps in one engine call (what
+    ``make_pipeline_fn`` uses when it keeps only the last state)."""
+
+    def __init__(self, update_fn: UpdateFn, checkpoint_every: int = 16, clip_grad: str = 'ste', engine: str = 'auto'):
+        if clip_grad not in CLIP_GRAD:
+            raise ValueError("clip_grad must be 'ste' or 'mask'")
+        if engine not in ENGINES:
+            raise ValueError(f'engine must be one of {ENGINES}')
+        self.update_fn = update_fn
+        self.checkpoint_every = int(checkpoint_every)
+        self.clip_grad = clip_grad
+        self.engine = engine
+
+    def kernels(self, variables, world):
+        """(world-sized real kernels ``[K, *world]``, gf_params, weights) of ``variables``."""
+        p = {k: v for k, v in variables.items() if k != 'params'}
+        p.update(variables.get('params', {}))
+        missing = [k for k in ('K', 'gf_params', 'kernels_weight_per_channel') if k not in p]
+        if missing:
+            raise KeyError(f'variables hold no {missing}')
+        m = self.update_fn.model_for(world)
+        K = p['K']
+        if K.dim() == 2 + len(m.world):
+            K = direct_world_kernels(K, m.world, m.C, m.max_k, m.cin, m.slot)
+        elif tuple(K.shape) != (m.K, ) + m.world:
+            raise ValueError(f'K {tuple(K.shape)} is neither [{m.C * m.max_k}, 1, *kernel_dims] nor '
+                             f'[{m.K}, *{m.world}]')
+        return K, p['gf_params'], p['kernels_weight_per_channel']
+
+    def rollout(self, variables, state: torch.Tensor, steps: int, dt) -> torch.Tensor:
+        """The state after ``steps`` Euler steps of ``dt`` from ``state``."""
+        k_real, gf, w = self.kernels(variables, tuple(state.shape[2:]))
+        T = torch.full((1, ), 1.0 / float(dt), dtype=torch.float32)
+        fin = rollout(state[None], k_real[None], gf[None], w[None], T, self.update_fn, int(steps),
+                      self.checkpoint_every, self.clip_grad, self.engine)
+        return fin[0]
+
+    def __call__(self, variables, rng_key, state: torch.Tensor, dt):
+        return self.rollout(variables, state, 1, dt), None, None

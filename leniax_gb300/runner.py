@@ -204,3 +204,98 @@ def run(rng_key, cells, K, gf_params, kernels_weight_per_channel, T, max_run_ite
     out_stats = {k: v[:n] for k, v in stats.items() if k not in ('N', 'N_box')}
     out_stats['N'] = torch.tensor(last, device=dev)
     return all_cells[:n], all_fields[:n], all_pots[:n], out_stats
+
+
+# ---------------------------------------------------------------- differentiable pipelines
+def normalize_fn(g: torch.Tensor) -> torch.Tensor:
+    """runner.py:447-448: ``g`` divided by its 2-norm (over all entries) + 1e-8."""
+    return g / (torch.linalg.vector_norm(g) + 1e-8)
+
+
+def _flatten(tree):
+    """Leaves (tensors) of nested dicts / lists / tuples, and a rebuild function."""
+    if isinstance(tree, dict):
+        keys = sorted(tree)
+        parts = [_flatten(tree[k]) for k in keys]
+        leaves = [leaf for p in parts for leaf in p[0]]
+        sizes = [len(p[0]) for p in parts]
+
+        def rebuild(vals):
+            out, i = {}, 0
+            for k, (_, rb), n in zip(keys, parts, sizes):
+                out[k] = rb(vals[i:i + n])
+                i += n
+            return out
+
+        return leaves, rebuild
+    if isinstance(tree, (list, tuple)):
+        parts = [_flatten(v) for v in tree]
+        leaves = [leaf for p in parts for leaf in p[0]]
+        sizes = [len(p[0]) for p in parts]
+
+        def rebuild_seq(vals):
+            out, i = [], 0
+            for (_, rb), n in zip(parts, sizes):
+                out.append(rb(vals[i:i + n]))
+                i += n
+            return type(tree)(out)
+
+        return leaves, rebuild_seq
+    return [tree], lambda vals: vals[0]
+
+
+def make_pipeline_fn(max_run_iter: int, dt: float, apply_fn, loss_fn, keep_intermediary_data: bool = False,
+                     keep_all_timesteps: bool = True):
+    """runner.py:363-423: ``fn(rng_key, params, variables, state0, targets)
+    -> (loss, rest)`` runs ``max_run_iter`` steps of ``apply_fn({'params':
+    params, **variables}, rng_key, state, dt=dt)`` from ``state0`` and
+    returns ``loss_fn(rng_key, preds, targets)`` split as ``(loss, rest)``.
+    ``preds['cells']`` is every pre-update state ``[max_run_iter, *state0]``
+    (``keep_all_timesteps``) or the last state; with
+    :class:`leniax_gb300.grad.LeniaApply` the last-state form runs as one
+    engine rollout.  The engine's adjoint differentiates cell states, so
+    ``keep_intermediary_data`` (fields and potentials in ``preds``) is
+    refused."""
+    if keep_intermediary_data:
+        raise NotImplementedError('the engine adjoint differentiates cell states only: use '
+                                  'keep_intermediary_data=False')
+    steps = int(max_run_iter)
+
+    def fn(rng_key, params, variables, state0, targets):
+        vs = {'params': params, **variables}
+        if keep_all_timesteps:
+            states, cur = [], state0
+            for _ in range(steps):
+                states.append(cur)
+                cur = apply_fn(vs, rng_key, cur, dt=dt)[0]
+            cells = torch.stack(states) if states else state0.new_empty((0, ) + tuple(state0.shape))
+        elif hasattr(apply_fn, 'rollout'):
+            cells = apply_fn.rollout(vs, state0, steps, dt)
+        else:
+            cells = state0
+            for _ in range(steps):
+                cells = apply_fn(vs, rng_key, cells, dt=dt)[0]
+        loss, *rest = loss_fn(rng_key, {'cells': cells}, targets)
+        return loss, rest
+
+    return fn
+
+
+def make_gradient_fn(pipeline_fn, normalize: bool = True):
+    """runner.py:426-444: ``fn(rng_key, params, variables, state0, targets)
+    -> ((loss, aux), grads)``, ``grads`` shaped like ``params`` (nested
+    dicts / sequences of tensors), each divided by its norm
+    (:func:`normalize_fn`) when ``normalize``."""
+
+    def fn(rng_key, params, variables, state0, targets):
+        leaves, rebuild = _flatten(params)
+        leaves = [t.detach().requires_grad_(True) for t in leaves]
+        with torch.enable_grad():
+            loss, aux = pipeline_fn(rng_key, rebuild(leaves), variables, state0, targets)
+            grads = torch.autograd.grad(loss, leaves, allow_unused=True)
+        grads = [torch.zeros_like(p) if g is None else g for p, g in zip(leaves, grads)]
+        if normalize:
+            grads = [normalize_fn(g) for g in grads]
+        return (loss.detach(), aux), rebuild(grads)
+
+    return fn
