@@ -13,6 +13,7 @@ import torch
 from . import core as lcore
 from . import growth_functions as lgf
 from . import kernels as lkernels
+from . import loader as lloader
 from . import runner as lrunner
 from . import statistics as lstat
 from .core import UpdateFn
@@ -72,17 +73,12 @@ def create_init_cells(world_size: List[int], nb_channels: int, other_cells=(), o
 
 
 def init(config: Dict, use_init_cells: bool = True, fft: bool = True, device=None):
-    """helpers.py:35-88 for cells given as arrays / nested lists."""
+    """helpers.py:35-88: the configuration's cells (encoded strings, nested
+    lists or arrays, ``loader.load_raw_cells``) placed in the world."""
     wp, rp = config['world_params'], config['render_params']
     nb_dims, C = wp['nb_dims'], wp['nb_channels']
     world_size = rp['world_size']
-    rpp = config['run_params']
-    cells = rpp.get('init_cells', rpp.get('cells')) if use_init_cells else rpp.get('cells')
-    if isinstance(cells, str):
-        raise NotImplementedError('string-encoded cells: decode them to an array before calling init')
-    raw_cells = np.asarray(cells, dtype=np.float32)
-    if raw_cells.ndim == nb_dims and C == 1:
-        raw_cells = raw_cells[np.newaxis]
+    raw_cells = lloader.load_raw_cells(config, use_init_cells).numpy()
     if raw_cells.ndim > 1 + nb_dims:
         init_cells = raw_cells
     else:

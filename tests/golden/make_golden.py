@@ -10,8 +10,10 @@ It reads ``tests/fixtures/{orbium-test,orbium-scutium-test,aquarium-test}.yaml``
 last frames ``*_last_frame*.p`` (numpy pickles, loaded with an unpickler that
 admits numpy's array-reconstruction classes only).  For each case it writes:
 
-* ``<case>.json``      -- world/run params and v2 kernel params
+* ``<case>.json``      -- world/run params, v2 kernel params
                           (v1 -> v2 migration as in leniax ``utils.py:91-124``)
+                          and the fixture's encoded initial cells (``cells_code``,
+                          when the fixture gives them as a string)
 * ``<case>_init.npy``  -- decoded initial cells ``[C, h, w]`` (float32)
 * ``<case>_last.npy``  -- leniax's golden state after ``max_run_iter - 1`` steps
 
@@ -157,6 +159,8 @@ def main():
             'decimal': decimal,
             'kernels_params': kernels,
         }
+        if isinstance(cells, str):
+            out['cells_code'] = cells
         with open(os.path.join(HERE, f'{case}.json'), 'w') as f:
             json.dump(out, f, indent=1)
         np.save(os.path.join(HERE, f'{case}_init.npy'), raw.astype(np.float32))
