@@ -361,7 +361,7 @@ LGX_API const char* lgx_noalloc_last_error(void);
 
 typedef struct lgx_ring_batch {
   int nb_dims;  /* 2 or 3 */
-  int size;     /* world side: 2D 32..256, 3D 32/64 */
+  int size;     /* world side: any square / cubic side the N-D engine takes (2..4096) */
   int n;        /* kernels */
   int kf_id;    /* LGX_KF_* */
   int nb_max;   /* row length of b */

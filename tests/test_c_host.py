@@ -2,7 +2,9 @@
 C99, links the engine library and creates, queries and destroys plans
 through the C ABI; model validation answers with the header's status codes
 (no device work: runs without a GPU)."""
+import ctypes
 import os
+import re
 import shutil
 import subprocess
 
@@ -81,3 +83,47 @@ def test_c_host_compiles_links_and_validates_plans(tmp_path):
     assert int(lines['3d'].split('=')[1]) == _lib.ENGINES['nd']
     assert lines['big'].startswith(f'rc={_lib.LGX_ERR_UNSUPPORTED} plan=0 msg=world axis 0')
     assert lines['bad'].startswith(f'rc={_lib.LGX_ERR_INVALID} plan=0 msg=kernel 1 reads channel 1 of 1')
+
+
+def _mirrors():
+    from leniax_gb300 import batch, grad, initializations, kernels
+    return {'lgx_model_desc': _lib.ModelDesc, 'lgx_rollout': _lib.Rollout, 'lgx_adjoint_job': grad.AdjointJob,
+            'lgx_ring_batch': kernels.RingBatchC.get(), 'lgx_init_job': initializations.InitJobC,
+            'lgx_batch_class': batch.BatchClassC, 'lgx_batch_job': batch.BatchJobC}
+
+
+def test_ctypes_mirrors_match_the_header_layout(tmp_path):
+    # every struct of include/lenia_gb300.h against its ctypes mirror: the
+    # same field names, offsets and size (the engine reads them through a bare pointer)
+    gcc = shutil.which('gcc')
+    if gcc is None:
+        pytest.skip('gcc not available')
+    mirrors = _mirrors()
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "lenia_gb300.h"', 'int main(void) {']
+    for cname, cls in mirrors.items():
+        lines.append(f'  printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ['  return 0;', '}']
+    src = tmp_path / 'layout.c'
+    src.write_text('\n'.join(lines) + '\n')
+    exe = tmp_path / 'layout'
+    subprocess.run([gcc, '-std=c99', '-Wall', '-Werror', '-I', os.path.join(ROOT, 'include'), str(src), '-o',
+                    str(exe)], check=True, capture_output=True, text=True)
+    got = {}
+    for line in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        cname, fname, val = line.split()
+        got[(cname, fname)] = int(val)
+    header = open(os.path.join(ROOT, 'include', 'lenia_gb300.h')).read()
+    for cname, cls in mirrors.items():
+        assert got[(cname, 'sizeof')] == ctypes.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, (cname, fname)
+        # and the mirror lists every field the header declares
+        body = header[header.index(f'typedef struct {cname} {{'):]
+        body = body[:body.index(f'}} {cname};')]
+        declared = set()
+        for stmt in re.sub(r'/\*.*?\*/', '', body[body.index('{') + 1:], flags=re.S).split(';'):
+            for part in filter(None, (p.strip() for p in stmt.split(','))):
+                declared.add(re.search(r'(\w+)\s*(?:\[\d+\])?$', part).group(1))
+        assert declared == {f for f, _ in cls._fields_}, (cname, declared ^ {f for f, _ in cls._fields_})
