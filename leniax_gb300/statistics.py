@@ -114,4 +114,4 @@ def stats_list_to_dict(all_stats: List[Dict]) -> Dict[str, torch.Tensor]:
     """statistics.py:339-360"""
     if not all_stats:
         return {}
-    return {k: torch.stack([s[k] for s in all_stats]) for k in all_stats[0]}
+    return {k: torch.stack([torch.as_tensor(s[k]) for s in all_stats]) for k in all_stats[0]}

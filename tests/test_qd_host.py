@@ -56,3 +56,22 @@ def test_update_individuals_behaviours_window():
     # individual 1: ns = 250, first best init 1 -> window [122, 250) + 1000
     assert abs(inds[1].features[0] - (1000. + 185.5)) < 1e-9
     assert inds[1].qd_config['algo']['best_init_idxs'] == [1, 2]
+
+
+def test_stats_list_to_dict_and_flat_kernel_params():
+    # statistics.py:339-360: per-step dicts (floats or arrays) -> per-key arrays over the steps
+    import torch
+    from leniax_gb300 import kernels, statistics
+    steps = [{'mass': 1.0, 'channel_mass': torch.tensor([0.5, 0.5])}, {'mass': 2.0, 'channel_mass': torch.tensor([1., 1.])}]
+    d = statistics.stats_list_to_dict(steps)
+    assert d['mass'].tolist() == [1.0, 2.0] and tuple(d['channel_mass'].shape) == (2, 2)
+    assert statistics.stats_list_to_dict([]) == {}
+    # kernels.py:38-45: the kernel params in the mapping's channel-sorted order
+    kp = [{'k_slug': 'circle_2d', 'k_params': [1.0, [1.0]], 'kf_slug': 'gauss_bump', 'kf_params': [4.0],
+           'gf_slug': 'gaussian', 'gf_params': [0.15, 0.015], 'h': 1.0, 'c_in': 1, 'c_out': 0},
+          {'k_slug': 'circle_2d', 'k_params': [0.5, [1.0, 0.5]], 'kf_slug': 'gauss_bump', 'kf_params': [4.0],
+           'gf_slug': 'gaussian', 'gf_params': [0.2, 0.02], 'h': 1.0, 'c_in': 0, 'c_out': 1}]
+    _, mp = kernels.get_kernels_and_mapping(kp, [32, 32], 2, 8.0, True, torch.device('cpu'))
+    assert mp.get_k_params() == [[0.5, [1.0, 0.5]], [1.0, [1.0]]]
+    assert mp.get_gf_params().tolist() == [[0.20000000298023224, 0.019999999552965164], [0.15000000596046448,
+                                                                                       0.014999999664723873]]
