@@ -53,3 +53,17 @@ def test_cropped_perlin_keeps_one_centred_square():
     np.testing.assert_array_equal(crop[:, :, lo:lo + size, lo:lo + size], full[:, :, 24:24 + size, 24:24 + size])
     crop[:, :, lo:lo + size, lo:lo + size] = 0
     assert not crop.any()
+
+
+def test_product_noise_function_matches_the_oracle():
+    # leniax_gb300.perlin.generate_perlin_noise_2d (the torch form of perlin.py:16-71)
+    import torch
+    from leniax_gb300 import perlin
+    for res, shape, n in (((4, 8), (64, 128), 3), ((3, 2), (48, 40), 2), ((1, 1), (16, 16), 1)):
+        a = _angles(n, res, seed=sum(shape))
+        want = O.perlin_noise_2d(a, shape, res)
+        got = perlin.generate_perlin_noise_2d(torch.from_numpy(a), shape, res, n).numpy()
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
+        got32 = perlin.generate_perlin_noise_2d(torch.from_numpy(a.astype(np.float32)), shape, res, n).numpy()
+        np.testing.assert_allclose(got32, want, atol=2e-6)
+    assert abs(float(perlin.interpolant(torch.tensor(0.5))) - 0.5) < 1e-12
