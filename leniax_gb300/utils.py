@@ -1,10 +1,13 @@
-"""State utilities of leniax ``utils.py`` used around the path: rolling a
-world onto its mass centroid and cropping it (``center_world`` 270-293,
+"""Utilities of leniax ``utils.py`` used around the path: rolling a world
+onto its mass centroid and cropping it (``center_world`` 270-293,
 ``auto_center`` 320-349, ``center_and_crop`` 352-385), what the reference
-applies to a found creature before encoding it (``qd.py:422``).  Torch ops
-on the state's own device; ``crop_zero`` is the kernel builder's
-(``utils.py:296-317``)."""
-from typing import Sequence, Tuple
+applies to a found creature before encoding it (``qd.py:422``), as torch ops
+on the state's own device (``crop_zero`` is the kernel builder's,
+``utils.py:296-317``); and the migration of version-1 configurations, whose
+kernels are described by numeric ids (``update_config_v1_v2`` 91-150,
+``st2fracs2float`` 214-225)."""
+from fractions import Fraction
+from typing import Dict, List, Sequence, Tuple
 
 import torch
 
@@ -73,4 +76,57 @@ def center_and_crop(cells: torch.Tensor) -> torch.Tensor:
     return cells
 
 
-__all__ = ['center_world', 'crop_zero', 'auto_center', 'center_and_crop']
+# version-1 numeric ids of the growth and kernel functions (utils.py:104-105)
+V1_GROWTH_SLUGS = {0: 'poly_quad4', 1: 'gaussian', 2: 'gaussian_target', 3: 'step'}
+V1_KERNEL_FUNCTION_SLUGS = {0: 'poly_quad', 1: 'gauss_bump', 2: 'step', 3: 'staircase', 4: 'gauss'}
+
+
+def st2fracs2float(st: str) -> List[float]:
+    """utils.py:214-225: ``'1,2/3,6.7'`` -> ``[1.0, 0.666..., 6.7]``."""
+    return [float(Fraction(part)) for part in st.split(',')]
+
+
+def _v2_key(key: str) -> str:
+    # a version-1 parameter path (kernels_params.k.<i>.m / .s) in version-2 terms
+    return key.replace('kernels_params.k', 'kernels_params').replace('.m', '.gf_params.0').replace('.s', '.gf_params.1')
+
+
+def update_config_v1_v2(config: Dict) -> Dict:
+    """utils.py:91-150, in place: each version-1 kernel entry (``r``, ring
+    weights ``b`` -- a list or a string of fractions --, ``k_id`` / ``q``,
+    ``gf_id`` / ``m`` / ``s``, ``h``, ``c_in``, ``c_out``) becomes a
+    ``circle_2d`` kernel with its kernel and growth functions named by slug;
+    genotype keys and phenotype entries are renamed alike; the initial-state
+    slug follows the state function (``perlin`` for v1, ``perlin_local``
+    for v2)."""
+    config['version'] = 2
+    kernels = []
+    for k in config['kernels_params']['k']:
+        kernels.append({
+            'k_slug': 'circle_2d',
+            'k_params': [k.get('r', 1.), st2fracs2float(k['b']) if isinstance(k['b'], str) else k['b']],
+            'kf_slug': V1_KERNEL_FUNCTION_SLUGS[k['k_id']],
+            'kf_params': [k['q']],
+            'gf_slug': V1_GROWTH_SLUGS[k['gf_id']],
+            'gf_params': [k['m'], k['s']],
+            'h': k['h'],
+            'c_in': k['c_in'],
+            'c_out': k['c_out'],
+        })
+    config['kernels_params'] = kernels
+    for gene in config.get('genotype', []):
+        if 'kernels_params.k' in gene['key']:
+            gene['key'] = _v2_key(gene['key'])
+    if 'phenotype' in config:
+        config['phenotype'] = [_v2_key(p) if 'kernels_params.k' in p else p for p in config['phenotype']]
+    slug = config['world_params'].get('get_state_fn_slug', 'v1')
+    algo = config.setdefault('algo', {})
+    if slug == 'v1':
+        algo['init_slug'] = 'perlin'
+    elif slug == 'v2':
+        algo['init_slug'] = 'perlin_local'
+    algo['init_param'] = []
+    return config
+
+
+__all__ = ['center_world', 'crop_zero', 'auto_center', 'center_and_crop', 'st2fracs2float', 'update_config_v1_v2']

@@ -12,8 +12,9 @@ admits numpy's array-reconstruction classes only).  For each case it writes:
 
 * ``<case>.json``      -- world/run params, v2 kernel params
                           (v1 -> v2 migration as in leniax ``utils.py:91-124``)
-                          and the fixture's encoded initial cells (``cells_code``,
-                          when the fixture gives them as a string)
+                          the fixture's own v1 kernel entries (``kernels_params_v1``)
+                          and its encoded initial cells (``cells_code``, when the
+                          fixture gives them as a string)
 * ``<case>_init.npy``  -- decoded initial cells ``[C, h, w]`` (float32)
 * ``<case>_last.npy``  -- leniax's golden state after ``max_run_iter - 1`` steps
 
@@ -158,6 +159,7 @@ def main():
             'max_run_iter': int(cfg['run_params']['max_run_iter']),
             'decimal': decimal,
             'kernels_params': kernels,
+            'kernels_params_v1': cfg['kernels_params']['k'],
         }
         if isinstance(cells, str):
             out['cells_code'] = cells

@@ -53,3 +53,29 @@ def test_center_world_rolls_each_batch_entry():
 def test_empty_state_crops_to_zeros():
     got = utils.center_and_crop(torch.zeros(3, 16, 16))
     assert tuple(got.shape) == (3, 1, 1) and float(got.abs().sum()) == 0
+
+
+def test_st2fracs2float_kat():
+    # tests/test_utils.py:11-16
+    out = utils.st2fracs2float('1/2,2/3')
+    assert out[0] == .5 and out[1] == 2 / 3
+
+
+@pytest.mark.parametrize('case', ['orbium', 'orbium_scutium', 'aquarium'])
+def test_v1_configs_migrate_to_the_golden_kernel_params(case):
+    # the fixtures' own v1 kernel entries against the v2 params the golden
+    # last frames are reproduced from
+    import copy
+    import json
+    import os
+    d = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), 'golden', f'{case}.json')))
+    cfg = {'version': 1, 'world_params': {'get_state_fn_slug': d['get_state_fn_slug']},
+           'kernels_params': {'k': copy.deepcopy(d['kernels_params_v1'])}, 'algo': {'init_slug': 'x'},
+           'genotype': [{'key': 'kernels_params.k.0.m'}, {'key': 'world_params.R'}],
+           'phenotype': ['kernels_params.k.0.s', 'mass']}
+    out = utils.update_config_v1_v2(cfg)
+    assert out['version'] == 2 and out['kernels_params'] == d['kernels_params']
+    assert [g['key'] for g in out['genotype']] == ['kernels_params.0.gf_params.0', 'world_params.R']
+    assert out['phenotype'] == ['kernels_params.0.gf_params.1', 'mass']
+    assert out['algo'] == {'init_slug': 'perlin' if d['get_state_fn_slug'] == 'v1' else 'perlin_local',
+                           'init_param': []}
