@@ -22,47 +22,10 @@ import numpy as np
 import torch
 
 from . import helpers, initializations, kernels, runner, statistics
+from .utils import get_param, set_param
 
 
 # ------------------------------------------------------------------ config paths (utils.py:153-210)
-def get_param(dic: Dict, key_string: str):
-    """utils.py:153-177"""
-    for key in key_string.split('.'):
-        dic = dic[int(key)] if key.isdigit() else dic[key]
-    if isinstance(dic, torch.Tensor):
-        return float(dic.float().mean())
-    if isinstance(dic, np.ndarray):
-        return float(np.mean(dic))
-    if type(dic) in (int, float):
-        return float(dic)
-    if type(dic) == str:
-        return dic
-    raise ValueError(f'dic type {type(dic)} not supported')
-
-
-def set_param(dic: Dict, key_string: str, value):
-    """utils.py:180-210"""
-    keys = key_string.split('.')
-    for i, key in enumerate(keys[:-1]):
-        if key.isdigit():
-            if not isinstance(dic, list):
-                raise Exception('This key should be an array')
-            idx = int(key)
-            while len(dic) < idx + 1:
-                dic.append({})
-            dic = dic[idx]
-        else:
-            dic = dic.setdefault(key, [] if keys[i + 1].isdigit() else {})
-    last = keys[-1]
-    if last.isdigit():
-        idx = int(last)
-        while len(dic) < idx + 1:
-            dic.append(None)
-        dic[idx] = value
-    else:
-        dic[last] = value
-
-
 # ------------------------------------------------------------------ individuals (lenia.py)
 def linear_scale(raw_value: float, domain: Sequence[float]) -> float:
     """lenia.py:124-136"""

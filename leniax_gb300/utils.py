@@ -3,12 +3,14 @@ onto its mass centroid and cropping it (``center_world`` 270-293,
 ``auto_center`` 320-349, ``center_and_crop`` 352-385), what the reference
 applies to a found creature before encoding it (``qd.py:422``), as torch ops
 on the state's own device (``crop_zero`` is the kernel builder's,
-``utils.py:296-317``); and the migration of version-1 configurations, whose
-kernels are described by numeric ids (``update_config_v1_v2`` 91-150,
-``st2fracs2float`` 214-225)."""
+``utils.py:296-317``); the dotted-path configuration accessors
+(``get_param`` / ``set_param`` 153-210) and the migration of version-1
+configurations, whose kernels are described by numeric ids
+(``update_config_v1_v2`` 91-150, ``st2fracs2float`` 214-225)."""
 from fractions import Fraction
 from typing import Dict, List, Sequence, Tuple
 
+import numpy as np
 import torch
 
 from .constant import EPSILON
@@ -129,4 +131,43 @@ def update_config_v1_v2(config: Dict) -> Dict:
     return config
 
 
-__all__ = ['center_world', 'crop_zero', 'auto_center', 'center_and_crop', 'st2fracs2float', 'update_config_v1_v2']
+def get_param(dic: Dict, key_string: str):
+    """utils.py:153-177"""
+    for key in key_string.split('.'):
+        dic = dic[int(key)] if key.isdigit() else dic[key]
+    if isinstance(dic, torch.Tensor):
+        return float(dic.float().mean())
+    if isinstance(dic, np.ndarray):
+        return float(np.mean(dic))
+    if type(dic) in (int, float):
+        return float(dic)
+    if type(dic) == str:
+        return dic
+    raise ValueError(f'dic type {type(dic)} not supported')
+
+
+def set_param(dic: Dict, key_string: str, value):
+    """utils.py:180-210"""
+    keys = key_string.split('.')
+    for i, key in enumerate(keys[:-1]):
+        if key.isdigit():
+            if not isinstance(dic, list):
+                raise Exception('This key should be an array')
+            idx = int(key)
+            while len(dic) < idx + 1:
+                dic.append({})
+            dic = dic[idx]
+        else:
+            dic = dic.setdefault(key, [] if keys[i + 1].isdigit() else {})
+    last = keys[-1]
+    if last.isdigit():
+        idx = int(last)
+        while len(dic) < idx + 1:
+            dic.append(None)
+        dic[idx] = value
+    else:
+        dic[last] = value
+
+
+__all__ = ['center_world', 'crop_zero', 'auto_center', 'center_and_crop', 'st2fracs2float', 'update_config_v1_v2',
+           'get_param', 'set_param']
