@@ -79,3 +79,17 @@ def test_v1_configs_migrate_to_the_golden_kernel_params(case):
     assert out['phenotype'] == ['kernels_params.0.gf_params.1', 'mass']
     assert out['algo'] == {'init_slug': 'perlin' if d['get_state_fn_slug'] == 'v1' else 'perlin_local',
                            'init_param': []}
+
+
+def test_set_param_kat():
+    # tests/test_utils.py:65-93
+    dic = {'test': {'hip': 2.}}
+    utils.set_param(dic, 'test.hop', 1.)
+    assert dic == {'test': {'hip': 2., 'hop': 1.}}
+    utils.set_param(dic, 'test.pim.pouf', 1.)
+    assert dic == {'test': {'hip': 2., 'hop': 1., 'pim': {'pouf': 1.}}}
+    utils.set_param(dic, 'test_arr.0.pouf', 1.)
+    assert dic == {'test_arr': [{'pouf': 1}], 'test': {'hip': 2., 'hop': 1., 'pim': {'pouf': 1.}}}
+    utils.set_param(dic, 'test_arr.2.woo', 2)
+    assert dic == {'test_arr': [{'pouf': 1}, {}, {'woo': 2}], 'test': {'hip': 2., 'hop': 1., 'pim': {'pouf': 1.}}}
+    assert utils.get_param(dic, 'test_arr.2.woo') == 2.0 and utils.get_param(dic, 'test.pim.pouf') == 1.0
