@@ -14,6 +14,7 @@ import ctypes
 import math
 from typing import List, Sequence, Tuple
 
+import numpy as np
 import torch
 
 from . import _lib
@@ -124,6 +125,8 @@ register = {'random_uniform': random_uniform, 'perlin': perlin, 'cropped_perlin'
 
 
 def make_array_compressible(cells: torch.Tensor) -> torch.Tensor:
-    """loader.py:16-30: round to the ``NB_CHARS**2 - 1`` grid (half to even)."""
+    """loader.py:16-30: round to the ``NB_CHARS**2 - 1`` grid (half to even);
+    a tensor or an array in, a float32 tensor out."""
     max_val = NB_CHARS**2 - 1
-    return (torch.round(cells * max_val).to(torch.int32) / max_val).to(torch.float32)
+    t = cells if isinstance(cells, torch.Tensor) else torch.as_tensor(np.asarray(cells))
+    return (torch.round(t * max_val).to(torch.int32) / max_val).to(torch.float32)

@@ -164,6 +164,11 @@ def rle_symbol(v: int) -> str:
     return chr(ord('p') + q) + chr(ord('A') + r)
 
 
+# leniax's names of the two symbol helpers (loader.py:287-304)
+char2val_deprecated = rle_value
+val2char_deprecated = rle_symbol
+
+
 def deprecated_compress_array(cells) -> str:
     """loader.py:307-320: values rounded to 0..255, runs of equal values per
     row as ``[count]symbol`` (count left out when 1), rows and blocks joined

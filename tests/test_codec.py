@@ -118,3 +118,22 @@ def test_init_places_string_encoded_cells():
     cells, K, _ = helpers.init(cfg, device=torch.device('cpu'))
     want = helpers.create_init_cells([16, 16], 1, [np.array([[[1, 1], [1, 0]]], np.float32)])
     np.testing.assert_array_equal(cells.numpy(), want)
+
+
+def test_reference_loader_tests():
+    # tests/test_loader.py:15-70, with numpy inputs as there
+    from leniax_gb300.constant import NB_CHARS
+    vals = list(range(256))
+    assert [loader.ch2val(loader.val2ch(v)) for v in vals] == vals
+    assert [loader.char2val_deprecated(loader.val2char_deprecated(v)) for v in vals] == vals
+    cells = np.arange(0, 1e5, 100) / 1e5
+    out = loader.decompress_array(loader.compress_array(cells), 1)
+    np.testing.assert_array_almost_equal(cells, out.numpy(), decimal=4)
+    out = loader.decompress_array(loader.compress_array(out), 1)
+    np.testing.assert_array_almost_equal(cells, out.numpy(), decimal=4)
+    comp = loader.make_array_compressible(cells)
+    np.testing.assert_array_almost_equal(comp.numpy(), loader.decompress_array(loader.compress_array(comp), 1).numpy(),
+                                         decimal=9)
+    grid = (np.arange(0, NB_CHARS**2, 8, dtype=np.int32) / (NB_CHARS**2 - 1)).reshape(32, 49)
+    np.testing.assert_array_almost_equal(grid, loader.decompress_array(loader.compress_array(grid)).numpy(),
+                                         decimal=4)
